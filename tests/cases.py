@@ -1,0 +1,110 @@
+"""Shared case builders: the golden fixtures as oracle case dicts.
+
+Each function loads one fixture written by tests/golden/make_golden.py and
+returns (case, golden) where ``case`` is the input description that both the
+oracle and the GPU model classes are driven with.
+"""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def ap2d_cfg1():
+    g = load("ap2d_cfg1")
+    n = 102
+    case = dict(model="ap", mesh=g["mesh"], dt=0.01, dr=0.25, t_max=50,
+                stencil="iso5",
+                stims=[dict(kind="voltage", t=0, value=1.0,
+                            box=[(0, n), (1, 6)])],
+                trackers=[dict(kind="at", threshold=0.5)])
+    return case, g
+
+
+def ap2d_aniso_spiral():
+    g = load("ap2d_aniso_spiral")
+    n = 42
+    case = dict(model="ap", mesh=g["mesh"], dt=0.01, dr=0.25, t_max=100,
+                stencil="aniso9", fibers=g["fibers"], conductivity=g["cond"],
+                stims=[dict(kind="voltage", t=0, value=1.0,
+                            box=[(0, n), (1, 4)]),
+                       dict(kind="voltage", t=22, value=1.0,
+                            box=[(n // 2, n), (0, n // 2)])],
+                trackers=[dict(kind="at", threshold=0.5),
+                          dict(kind="probe", cells=[[5, 5], [20, 30],
+                                                    [35, 10]],
+                               vars=["u"], step=7),
+                          dict(kind="probe", cells=[[10, 12], [30, 30]],
+                               vars=["u", "v"], step=3, start_time=10,
+                               end_time=60)])
+    return case, g
+
+
+MODEL_VARS = {"ap": ["u", "v"], "ms": ["u", "h"], "fk": ["u", "v", "w"]}
+
+
+def models_2d(name, aniso):
+    g = load("models_2d")
+    case = dict(model=name, mesh=g["mesh"], dt=0.01, dr=0.25, t_max=40,
+                stencil="aniso9" if aniso else "iso5", fibers=g["fibers"],
+                stims=[dict(kind="current", t=0, value=5, duration=1.0,
+                            box=[(0, 24), (1, 4)], u_max=1.0),
+                       dict(kind="current", t=2.5, value=3, duration=0.5,
+                            box=[(8, 14), (8, 14)])],
+                trackers=[dict(kind="at", threshold=0.5),
+                          dict(kind="probe", cells=[[4, 4], [12, 20]],
+                               vars=MODEL_VARS[name], step=5)])
+    key = f"{name}_{'aniso' if aniso else 'iso'}"
+    gold = {v: g[f"{key}_{v}"] for v in MODEL_VARS[name]}
+    gold.update({f"mv_{v}": g[f"{key}_mv_{v}"] for v in MODEL_VARS[name]})
+    gold["act_t"] = g[f"{key}_act_t"]
+    return case, gold
+
+
+def ap3d(aniso):
+    g = load("ap3d")
+    case = dict(model="ap", mesh=g["mesh"], dt=0.01, dr=0.25, t_max=20,
+                stencil="aniso19" if aniso else "iso7", fibers=g["fibers"],
+                stims=[dict(kind="voltage", t=0, value=1.0,
+                            box=[(0, 12), (0, 11), (1, 3)]),
+                       dict(kind="current", t=8, value=4, duration=0.6,
+                            box=[(6, 12), (0, 6), (0, 10)])],
+                trackers=[dict(kind="at", threshold=0.5)])
+    key = "aniso" if aniso else "iso"
+    return case, {"u": g[key + "_u"], "v": g[key + "_v"],
+                  "act_t": g[key + "_act_t"]}
+
+
+def trackers_cable():
+    g = load("trackers")
+    mesh = np.pad(np.ones((10, 1), np.int8), 1)
+    case = dict(model="ap", mesh=mesh, dt=0.01, dr=0.25, t_max=50,
+                stencil="iso5",
+                stims=[dict(kind="current", t=0, value=5, duration=0.5,
+                            box=[(0, 5), (0, 3)]),
+                       dict(kind="voltage", t=45, value=1,
+                            box=[(0, 5), (0, 10)])],
+                trackers=[dict(kind="lat", threshold=0.5),
+                          dict(kind="at", threshold=0.5),
+                          dict(kind="at", threshold=-40),
+                          dict(kind="at", threshold=0.2, step=4,
+                               start_time=1.0, end_time=30.0)])
+    return case, g
+
+
+def stimuli_2d():
+    g = load("stimuli")
+    case = dict(model="ap", mesh=g["mesh2d"], dt=0.01, dr=0.25, t_max=6,
+                stencil="iso5",
+                stims=[dict(kind="voltage", t=0, value=0.8, matrix=g["m1"]),
+                       dict(kind="current", t=1, value=2.5, duration=0.7,
+                            matrix=g["m2"], u_max=0.9),
+                       dict(kind="current", t=2.0, value=6.0, duration=0.4,
+                            coords=g["area_coords"], u_max=1.2)],
+                trackers=[dict(kind="at", threshold=0.5)])
+    return case, g

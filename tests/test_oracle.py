@@ -1,0 +1,116 @@
+"""Pin the CPU oracle against the golden vectors produced by the reference.
+
+The oracle (oracle/fw_oracle.c + oracle/oracle.py) is what every GPU parity
+test compares against, so it is checked here first: weights, stimuli,
+trackers and the Aliev-Panfilov / Mitchell-Schaeffer runs must be bitwise
+equal to the reference's float64 results; Fenton-Karma calls tanh, whose
+last-ulp rounding differs between numpy and the C library, so its traces get
+a 1e-14 absolute tolerance.
+"""
+import numpy as np
+import pytest
+
+import cases
+
+
+def test_weights_2d(oracle):
+    g = cases.load("weights_2d")
+    a = (float(g["D_model"]), float(g["dt"]), float(g["dr"]))
+    assert np.array_equal(oracle.weights("iso5", g["mesh"], *a),
+                          g["w_iso5_c1"])
+    assert np.array_equal(oracle.weights("iso5", g["mesh"], *a, g["cond"]),
+                          g["w_iso5_carr"])
+    assert np.array_equal(
+        oracle.weights("aniso9", g["mesh"], *a, g["cond"], g["fibers"]),
+        g["w_aniso9_carr"])
+    assert np.array_equal(
+        oracle.weights("aniso9", g["mesh"], *a, 1.0, g["fibers"],
+                       float(g["D_al_b"]), float(g["D_ac_b"])),
+        g["w_aniso9_c1_dac0111"])
+
+
+def test_weights_3d(oracle):
+    g = cases.load("weights_3d")
+    a = (float(g["D_model"]), float(g["dt"]), float(g["dr"]))
+    assert np.array_equal(oracle.weights("iso7", g["mesh"], *a),
+                          g["w_iso7_c1"])
+    assert np.array_equal(oracle.weights("iso7", g["mesh"], *a, g["cond"]),
+                          g["w_iso7_carr"])
+    assert np.array_equal(
+        oracle.weights("aniso19", g["mesh"], *a, g["cond"], g["fibers"]),
+        g["w_aniso19_carr"])
+    assert np.array_equal(
+        oracle.weights("aniso19", g["mesh"], *a, 1.0, g["fibers"],
+                       float(g["D_al_b"]), float(g["D_ac_b"])),
+        g["w_aniso19_c1_dac025"])
+
+
+def test_ap2d_aniso_spiral_bitwise(oracle):
+    case, g = cases.ap2d_aniso_spiral()
+    r = oracle.run(case)
+    assert r["step"] == int(g["step"]) == 10000
+    assert r["t"] == float(g["t"])
+    for k in ("u", "v"):
+        assert np.array_equal(r[k], g[k]), k
+    at, ap, mv = r["trackers"]
+    assert np.array_equal(at, g["act_t"])
+    assert np.array_equal(ap["u"], g["ap"])
+    assert np.array_equal(mv["u"], g["mv_u"])
+    assert np.array_equal(mv["v"], g["mv_v"])
+
+
+@pytest.mark.parametrize("name", ["ms", "fk"])
+@pytest.mark.parametrize("aniso", [False, True])
+def test_models_2d(oracle, name, aniso):
+    case, g = cases.models_2d(name, aniso)
+    r = oracle.run(case)
+    at, mv = r["trackers"]
+    assert np.array_equal(at, g["act_t"])
+    for v in cases.MODEL_VARS[name]:
+        if name == "ms":
+            assert np.array_equal(r[v], g[v]), v
+            assert np.array_equal(mv[v], g["mv_" + v]), v
+        else:
+            np.testing.assert_allclose(r[v], g[v], rtol=0, atol=1e-14)
+            np.testing.assert_allclose(mv[v], g["mv_" + v], rtol=0,
+                                       atol=1e-14)
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+def test_ap3d_bitwise(oracle, aniso):
+    case, g = cases.ap3d(aniso)
+    r = oracle.run(case)
+    for k in ("u", "v"):
+        assert np.array_equal(r[k], g[k]), k
+    assert np.array_equal(r["trackers"][0], g["act_t"])
+
+
+def test_trackers_cable(oracle):
+    case, g = cases.trackers_cable()
+    r = oracle.run(case)
+    lat, at, at_def, at_win = r["trackers"]
+    assert np.array_equal(lat, g["lat"])
+    assert lat.shape[0] == 2
+    assert np.array_equal(at, g["act_t"])
+    assert np.array_equal(at_def, g["act_t_default"])
+    assert np.array_equal(at_win, g["act_t_windowed"])
+    assert np.array_equal(r["u"], g["u"])
+
+
+def test_stimuli(oracle):
+    case, g = cases.stimuli_2d()
+    r = oracle.run(case)
+    assert np.array_equal(r["u"], g["u2d"])
+    assert np.array_equal(r["v"], g["v2d"])
+    assert np.array_equal(r["trackers"][0], g["act_t2d"])
+
+
+def test_ap2d_cfg1_bitwise(oracle):
+    """The 100x100 Aliev-Panfilov planar-wave case, 5000 steps."""
+    case, g = cases.ap2d_cfg1()
+    r = oracle.run(case)
+    assert r["step"] == int(g["step"]) == 5000
+    assert np.array_equal(r["u"], g["u"])
+    assert np.array_equal(r["v"], g["v"])
+    assert np.array_equal(r["u_new"], g["u_new"])
+    assert np.array_equal(r["trackers"][0], g["act_t"])
