@@ -1,0 +1,397 @@
+"""Benchmark: Aliev-Panfilov 2D, 4096x4096, anisotropic 9-point stencil.
+
+Workload (the 4096^2 spiral-induction configuration): a CardiacTissue2D of
+4096x4096 nodes (boundary ring included), diffuse fibrosis (code 2) with
+p = 0.2 drawn as the reference's Diffuse2DPattern draws it
+(``1 + (np.random.random(shape) <= p)`` under ``np.random.seed``), fibers at
+angle 45 deg * g / max|g| with g a seeded standard-normal field smoothed by
+a Gaussian of sigma = 64 nodes, AsymmetricStencil2D with D_al = 1,
+D_ac = 0.111, dt = 0.01, dr = 0.25, S1 = StimVoltageCoord2D(0, 1, 0, 4096,
+1, 6), S2 = StimVoltageCoord2D(31, 1, 2048, 4096, 0, 2048) and an
+activation-time tracker at threshold 0.5.  Inputs are synthetic (seeded);
+the reference publishes no dataset for this path.
+
+One bench step = ``--chunk`` time steps (default 100 = 1 ms of model time)
+of the whole tissue.  ``value`` is myocyte-steps/s of the float32 form with
+all state resident in HBM (state ~ 200 MB, larger than the 129 MB L2, so no
+flush is needed between steps); ``e2e`` is the same metric through the
+public model API with the state uploaded from pinned host memory and the
+potential and activation map read back every bench step.  The float64 plain
+form is timed beside it (``fp64_plain``).
+
+``--impl reference`` times the reference's algorithm on the host cores: the
+C restatement of its numba kernels (oracle/fw_oracle.c, OpenMP over all
+cores, float64, precomputed weights) on the same workload, a bounded number
+of steps.
+
+Multi-GPU: the path is replicated, not sharded -- each rank advances its own
+copy of the tissue (``scaling: weak``); rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("node-steps/s: batched FP32 vs plain FP64 GPU at LAT err≤1 "
+          "step; p50/p99 latency")
+UNIT = "myocyte-steps/s"
+N = 4096
+SEED = 1234
+# algorithmic bytes per myocyte-step (u and v read + written, 1 B mesh code,
+# two fiber components at the stencil precision)
+B_ALG = {"float32": 2 * (4 + 4) + 1 + 2 * 4, "float64": 2 * (8 + 8) + 1 + 2 * 8}
+
+
+def workload_inputs(n=N, seed=SEED):
+    import scipy.ndimage as nd
+    np.random.seed(seed)
+    mesh = (1 + (np.random.random((n, n)) <= 0.2)).astype(np.int8)
+    mesh[0, :] = mesh[-1, :] = mesh[:, 0] = mesh[:, -1] = 0
+    g = np.random.default_rng(seed).standard_normal((n, n)).astype(np.float32)
+    g = nd.gaussian_filter(g, 64.0)
+    theta = (np.pi / 4) * g / np.abs(g).max()
+    fibers = np.stack([np.cos(theta), np.sin(theta)], -1).astype(np.float64)
+    return mesh, fibers
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            out, _ = self.proc.communicate(timeout=10)
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, f[2:]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_model(fg, mesh, fibers, npfloat, form):
+    n = mesh.shape[0]
+    tissue = fg.CardiacTissue2D(mesh.shape)
+    tissue.mesh = mesh.copy()
+    tissue.fibers = fibers
+    model = fg.AlievPanfilov2D()
+    model.dt, model.dr = 0.01, 0.25
+    model.t_max = 1000.0
+    model.npfloat = npfloat
+    model.form = form
+    st = fg.AsymmetricStencil2D()
+    st.D_al, st.D_ac = 1.0, 0.111
+    model.stencil = st
+    model.cardiac_tissue = tissue
+    seq = fg.StimSequence()
+    seq.add_stim(fg.StimVoltageCoord2D(0, 1.0, 0, n, 1, 6))
+    seq.add_stim(fg.StimVoltageCoord2D(31, 1.0, n // 2, n, 0, n // 2))
+    model.stim_sequence = seq
+    at = fg.ActivationTime2DTracker()
+    at.threshold = 0.5
+    trs = fg.TrackerSequence()
+    trs.add_tracker(at)
+    model.tracker_sequence = trs
+    model.initialize()
+    return model, at
+
+
+def device_steps(model, chunk, iters, torch):
+    """Advance iters x chunk steps through fw_step with no host sync;
+    returns (elapsed ms by CUDA events, library launches)."""
+    from finitewave_gb300 import _ffi
+    L = _ffi.load()
+    stream = torch.cuda.current_stream()
+    l0 = L.fw_launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(iters):
+        model._run_segment(chunk, sync=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), L.fw_launch_count() - l0
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import finitewave_gb300 as fg
+    from finitewave_gb300 import _ffi
+    _ffi.load()
+
+    mesh, fibers = workload_inputs()
+    myo = int((mesh == 1).sum())
+    chunk, K, W = args.chunk, args.steps, args.warmup
+    form32 = args.form
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # --- float32 form, state resident -------------------------------------
+    model, at = build_model(fg, mesh, fibers, "float32", form32)
+    for _ in range(W):
+        model._run_segment(chunk, sync=False)
+    barrier()
+    with Clocks(local) as clk:
+        ms, launches = device_steps(model, chunk, K, torch)
+    barrier()
+    ms = max_over_ranks(ms)
+    ms_per_step = ms / K
+    value = world * myo * chunk * K / (ms / 1e3)
+
+    # dominant-kernel timing: launches of one segment averaged
+    kms, kl = device_steps(model, chunk, 3, torch)
+    steps_per_launch = (3 * chunk) / max(1, kl)
+    per_launch_s = (kms / 1e3) / max(1, kl)
+    alg_bytes = B_ALG["float32"] * myo * steps_per_launch
+    achieved = alg_bytes / per_launch_s / 1e9
+    peak, peak_kind = peaks()
+
+    # --- e2e through the public API, host buffers ----------------------------
+    u_h = torch.empty(mesh.shape, dtype=torch.float32).pin_memory()
+    v_h = torch.empty(mesh.shape, dtype=torch.float32).pin_memory()
+    u_h.copy_(model._dev["u"].cpu())
+    v_h.copy_(model._dev["v"].cpu())
+    u_out = torch.empty_like(u_h).pin_memory()
+    act_out = torch.empty(mesh.shape, dtype=torch.int32).pin_memory()
+    h2d = u_h.numel() * 4 * 2
+    d2h = u_out.numel() * 4 + act_out.numel() * 4
+
+    def e2e_step():
+        # public API: upload the state, run `chunk` more steps, read back
+        model._dev["u"].copy_(u_h, non_blocking=True)
+        model._dev["v"].copy_(v_h, non_blocking=True)
+        s0 = model.step
+        model.t_max = model.t + chunk * model.dt
+        model.run(initialize=False)
+        u_out.copy_(model._dev["u"], non_blocking=True)
+        act_out.copy_(at._act_step, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return model.step - s0
+
+    for _ in range(max(1, W // 2)):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = 0
+    for _ in range(K):
+        e2e_steps += e2e_step()
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * myo * e2e_steps / e2e_s
+    del model, at
+    torch.cuda.empty_cache()
+
+    # --- float64 plain form, same workload ----------------------------------
+    m64, _ = build_model(fg, mesh, fibers, "float64", "plain")
+    for _ in range(max(1, W // 2)):
+        m64._run_segment(chunk, sync=False)
+    barrier()
+    ms64, _ = device_steps(m64, chunk, max(1, K // 2), torch)
+    ms64 = max_over_ranks(ms64)
+    fp64_value = world * myo * chunk * max(1, K // 2) / (ms64 / 1e3)
+    del m64
+    torch.cuda.empty_cache()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(mesh, fibers, args.cpu_seconds)
+    clocks = clk.summary()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": K, "warmup": W, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded fibrosis and fibers)",
+            "config": {
+                "workload": "Aliev-Panfilov 2D 4096x4096, AsymmetricStencil2D "
+                            "(D_al 1, D_ac 0.111), 20% diffuse fibrosis, "
+                            "smooth fibers, S1-S2, activation tracker",
+                "grid": [N, N], "myocytes": myo,
+                "time_steps_per_bench_step": chunk, "form": form32 or "auto",
+                "l2": "state larger than L2 (no flush needed)",
+                "parallelism": f"replicas x{world}"},
+            "fp64_plain": {"value": fp64_value, "unit": UNIT,
+                           "speedup_fp32_over_fp64": value / fp64_value},
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind,
+                         "traffic": traffic_from_profiles(myo,
+                                                          steps_per_launch),
+                         "kernel": "fw step kernel (float32)",
+                         "alg_bytes_per_myocyte_step": B_ALG["float32"],
+                         "time_steps_per_launch": steps_per_launch},
+            "cpu_baseline": cpu,
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def traffic_from_profiles(myo, steps_per_launch):
+    """DRAM bytes per launch from the committed ncu summary, scaled to this
+    workload, or None when no summary is present."""
+    p = os.path.join(ROOT, "profiles", "traffic.json.txt")
+    if not os.path.exists(p):
+        return None
+    try:
+        with open(p) as f:
+            d = json.loads(f.read())
+        return d["dram_bytes_per_myocyte_step"] * myo * steps_per_launch
+    except (ValueError, KeyError):
+        return None
+
+
+def cpu_baseline(mesh, fibers, seconds):
+    """The oracle's C kernels (OpenMP, all host cores, float64) on the same
+    workload for a bounded number of steps."""
+    from oracle import oracle
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    w = oracle.weights("aniso9", mesh, 1.0, 0.01, 0.25, 1.0, fibers, 1.0,
+                       0.111)
+    idx = np.flatnonzero(mesh == 1).astype(np.int64)
+    u = np.zeros(mesh.shape)
+    u[:, 1:6][mesh[:, 1:6] == 1] = 1.0
+    un = np.zeros(mesh.shape)
+    v = np.zeros(mesh.shape)
+    p = oracle.MODELS["ap"]["params"]
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle._diffuse("aniso9", un, u, w, idx)
+        oracle._ionic("ap", {"v": v}, un, u, idx, 0.01, p)
+        u, un = un, u
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 10000:
+            break
+    return {"value": idx.size * steps / el, "unit": UNIT, "cores": cores,
+            "kind": "port",
+            "sample": f"{steps} float64 steps of the 4096^2 workload "
+                      f"(diffusion + ionic, OpenMP x{cores}), {el:.1f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mesh, fibers = workload_inputs()
+    total = 0.0
+    steps_done = 0
+    per = None
+    for _ in range(args.warmup + args.steps):
+        per = cpu_baseline(mesh, fibers, args.cpu_seconds / max(1, args.steps))
+    cpu = per
+    line = {
+        "metric": METRIC, "value": cpu["value"], "unit": UNIT,
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded fibrosis and fibers)",
+        "config": {"workload": "Aliev-Panfilov 2D 4096x4096, "
+                               "AsymmetricStencil2D, 20% fibrosis",
+                   "grid": [N, N]},
+        "impl": "reference",
+        "cpu_baseline": cpu,
+        "e2e": {"value": cpu["value"], "unit": UNIT,
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    del total, steps_done
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--chunk", type=int, default=100)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--form", default=None, choices=[None, "plain", "fused"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

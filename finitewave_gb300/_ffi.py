@@ -1,0 +1,160 @@
+"""ctypes binding of libfwgpu.so (the C ABI declared in include/fwgpu.h).
+
+The structures below mirror fwgpu.h field for field; ``load()`` checks their
+sizes against the library's own ``fw_struct_size`` before any call is made.
+Every non-OK status is turned into an exception carrying
+``fw_last_error()``.  There is no fallback: if the library cannot be loaded
+(no CUDA toolkit to build it, no GPU to run it) the calls raise.
+"""
+import ctypes
+import os
+import threading
+
+from . import _build
+
+FW_OK = 0
+FW_ERR_ARG = -1
+FW_ERR_CUDA = -2
+FW_ERR_UNSUPPORTED = -3
+
+FW_DEV_LAT_OVERFLOW = 1
+FW_DEV_PROBE_OVERFLOW = 2
+FW_DEV_BATCH_FAULT = 4
+
+MODEL_AP, MODEL_MS, MODEL_FK, MODEL_TP06, MODEL_CRN = 1, 2, 3, 4, 5
+ISO5, ANISO9, ISO7, ANISO19 = 1, 2, 3, 4
+F64, F32 = 0, 1
+FORM_PLAIN, FORM_FUSED = 0, 1
+STIM_VOLTAGE, STIM_CURRENT = 0, 1
+
+MAX_STATE = 24
+MAX_PARAMS = 64
+MAX_STIMS = 16
+MAX_AT = 4
+MAX_LAT = 2
+MAX_PROBE = 4
+MAX_PROBE_VARS = 8
+
+STENCIL_NW = {ISO5: 5, ANISO9: 9, ISO7: 7, ANISO19: 19}
+
+_i32, _i64, _f64, _vp = (ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
+                         ctypes.c_void_p)
+
+
+class Window(ctypes.Structure):
+    _fields_ = [("first", _i64), ("last", _i64), ("stride", _i64)]
+
+
+class Stim(ctypes.Structure):
+    _fields_ = [("kind", _i32), ("has_umax", _i32), ("first", _i64),
+                ("last", _i64), ("value", _f64), ("u_max", _f64),
+                ("lo", _i64 * 3), ("hi", _i64 * 3), ("mask", _vp)]
+
+
+class AtTracker(ctypes.Structure):
+    _fields_ = [("win", Window), ("threshold", _f64), ("act_step", _vp)]
+
+
+class LatTracker(ctypes.Structure):
+    _fields_ = [("win", Window), ("threshold", _f64), ("activated", _vp),
+                ("cross_steps", _vp), ("cross_count", _vp),
+                ("capacity", _i32)]
+
+
+class ProbeTracker(ctypes.Structure):
+    _fields_ = [("win", Window), ("n_cells", _i32), ("n_vars", _i32),
+                ("var_ids", _i32 * MAX_PROBE_VARS), ("cells", _vp),
+                ("out", _vp), ("sample_offset", _i64), ("capacity", _i64)]
+
+
+class StepArgs(ctypes.Structure):
+    _fields_ = [("model", _i32), ("stencil", _i32), ("precision", _i32),
+                ("form", _i32), ("ni", _i64), ("nj", _i64), ("nk", _i64),
+                ("mesh", _vp), ("myo", _vp), ("weights", _vp),
+                ("u", _vp * 2), ("state", _vp * MAX_STATE),
+                ("params", _f64 * MAX_PARAMS), ("dt", _f64),
+                ("n_stims", _i32), ("n_at", _i32), ("n_lat", _i32),
+                ("n_probe", _i32),
+                ("stims", Stim * MAX_STIMS), ("at", AtTracker * MAX_AT),
+                ("lat", LatTracker * MAX_LAT),
+                ("probe", ProbeTracker * MAX_PROBE),
+                ("status", _vp), ("fused_k", _i32)]
+
+
+class FwError(RuntimeError):
+    """A non-OK status from libfwgpu."""
+
+    def __init__(self, fn, code, msg):
+        super().__init__(f"{fn} failed ({code}): {msg}")
+        self.code = code
+
+
+_lib = None
+_lock = threading.Lock()
+
+_SIGS = {
+    "fw_version": ([], _i32),
+    "fw_launch_count": ([], _i64),
+    "fw_struct_size": ([_i32], ctypes.c_size_t),
+    "fw_last_error": ([], ctypes.c_char_p),
+    "fw_model_info": ([_i32, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
+                      _i32),
+    "fw_state_is_f64": ([_i32, _i32, _i32], _i32),
+    "fw_build_weights": ([_i32, _i32, _vp, _vp, _f64, _vp, _f64, _f64, _f64,
+                          _f64, _f64, _i64, _i64, _i64, _vp, _vp], _i32),
+    "fw_diffuse": ([_i32, _i32, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _i64,
+                    _vp], _i32),
+    "fw_ionic": ([_i32, _i32, _vp, _vp, _vp, _vp, _i64, _f64, _vp, _vp],
+                 _i32),
+    "fw_step": ([ctypes.POINTER(StepArgs), _i64, _i64, _vp], _i32),
+}
+
+# symbol -> ctypes structure whose size must match the library's
+_STRUCTS = {0: StepArgs, 1: Stim, 2: AtTracker, 3: LatTracker,
+            4: ProbeTracker, 5: Window}
+
+
+def load(path=None):
+    """Load (building first if needed) libfwgpu.so and return the handle."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if path is None:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise OSError(f"libfwgpu not found at {path}")
+        L = ctypes.CDLL(path)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        for which, struct in _STRUCTS.items():
+            got = L.fw_struct_size(which)
+            if got != ctypes.sizeof(struct):
+                raise RuntimeError(
+                    f"ABI mismatch for {struct.__name__}: library "
+                    f"{got} bytes, binding {ctypes.sizeof(struct)} bytes")
+        _lib = L
+        return _lib
+
+
+def check(fn, rc):
+    if rc != FW_OK:
+        msg = load().fw_last_error()
+        raise FwError(fn, rc, msg.decode() if msg else "")
+    return rc
+
+
+def call(name, *args):
+    return check(name, getattr(load(), name)(*args))
+
+
+def model_info(model):
+    ns, npar = _i32(), _i32()
+    call("fw_model_info", model, ctypes.byref(ns), ctypes.byref(npar))
+    return ns.value, npar.value
+
+
+def state_is_f64(model, precision, index):
+    return bool(load().fw_state_is_f64(model, precision, index))

@@ -1,0 +1,239 @@
+// fw_capi.cu -- the extern "C" entry points declared in include/fwgpu.h:
+// argument validation, error reporting and dispatch to the kernels.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <atomic>
+
+#include "fw_internal.cuh"
+#include "fw_model_dispatch.cuh"
+
+namespace fw {
+
+static thread_local char g_err[512] = "";
+static std::atomic<int64_t> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+int cuda_error(cudaError_t e, const char *what)
+{
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    return FW_ERR_CUDA;
+}
+
+namespace {
+
+struct Info {
+    int ns, np;
+};
+
+Info model_info(int32_t model)
+{
+    switch (model) {
+    case FW_MODEL_AP: return {ModelAP::NS, ModelAP::NP};
+    case FW_MODEL_MS: return {ModelMS::NS, ModelMS::NP};
+    case FW_MODEL_FK: return {ModelFK::NS, ModelFK::NP};
+    }
+    return {-1, -1};
+}
+
+bool valid_window(const fw_window &w) { return w.stride > 0; }
+
+int check_step_args(const fw_step_args *a, int64_t n_steps)
+{
+    if (!a) {
+        set_error("fw_step: args is NULL");
+        return FW_ERR_ARG;
+    }
+    Info mi = model_info(a->model);
+    if (mi.ns < 0) {
+        set_error("fw_step: model %d not supported", a->model);
+        return FW_ERR_UNSUPPORTED;
+    }
+    int nw = stencil_nw(a->stencil);
+    if (!nw) {
+        set_error("fw_step: unknown stencil %d", a->stencil);
+        return FW_ERR_ARG;
+    }
+    if (a->precision != FW_F64 && a->precision != FW_F32) {
+        set_error("fw_step: unknown precision %d", a->precision);
+        return FW_ERR_ARG;
+    }
+    if (a->form != FW_FORM_PLAIN && a->form != FW_FORM_FUSED) {
+        set_error("fw_step: unknown form %d", a->form);
+        return FW_ERR_ARG;
+    }
+    int dim = stencil_dim(a->stencil);
+    if (a->ni < 3 || a->nj < 3 || (dim == 3 ? a->nk < 3 : a->nk != 1)) {
+        set_error("fw_step: grid (%lld,%lld,%lld) does not fit a %dD stencil",
+                  (long long)a->ni, (long long)a->nj, (long long)a->nk, dim);
+        return FW_ERR_ARG;
+    }
+    if (a->ni * a->nj * a->nk > (int64_t)1 << 40) {
+        set_error("fw_step: grid too large");
+        return FW_ERR_ARG;
+    }
+    if (n_steps < 0 || n_steps > ((int64_t)1 << 31)) {
+        set_error("fw_step: n_steps %lld out of range", (long long)n_steps);
+        return FW_ERR_ARG;
+    }
+    if (!a->mesh || !a->myo || !a->weights || !a->u[0] || !a->u[1] ||
+        a->u[0] == a->u[1]) {
+        set_error("fw_step: mesh/myo/weights/u buffers missing or aliased");
+        return FW_ERR_ARG;
+    }
+    for (int i = 0; i < mi.ns; ++i)
+        if (!a->state[i]) {
+            set_error("fw_step: state variable %d is NULL", i);
+            return FW_ERR_ARG;
+        }
+    if (a->n_stims < 0 || a->n_stims > FW_MAX_STIMS || a->n_at < 0 ||
+        a->n_at > FW_MAX_AT || a->n_lat < 0 || a->n_lat > FW_MAX_LAT ||
+        a->n_probe < 0 || a->n_probe > FW_MAX_PROBE) {
+        set_error("fw_step: too many stimuli or trackers");
+        return FW_ERR_ARG;
+    }
+    for (int i = 0; i < a->n_stims; ++i) {
+        const fw_stim &s = a->stims[i];
+        if (s.kind != FW_STIM_VOLTAGE && s.kind != FW_STIM_CURRENT) {
+            set_error("fw_step: stimulus %d has unknown kind %d", i, s.kind);
+            return FW_ERR_ARG;
+        }
+    }
+    for (int i = 0; i < a->n_at; ++i)
+        if (!valid_window(a->at[i].win) || !a->at[i].act_step) {
+            set_error("fw_step: activation tracker %d invalid", i);
+            return FW_ERR_ARG;
+        }
+    for (int i = 0; i < a->n_lat; ++i) {
+        const fw_lat_tracker &L = a->lat[i];
+        if (!valid_window(L.win) || !L.activated || !L.cross_count ||
+            (L.capacity > 0 && !L.cross_steps) || L.capacity < 0) {
+            set_error("fw_step: local activation tracker %d invalid", i);
+            return FW_ERR_ARG;
+        }
+    }
+    for (int i = 0; i < a->n_probe; ++i) {
+        const fw_probe_tracker &P = a->probe[i];
+        if (!valid_window(P.win) || P.n_cells < 1 || !P.cells || !P.out ||
+            P.n_vars < 1 || P.n_vars > FW_MAX_PROBE_VARS || P.capacity < 0 ||
+            P.sample_offset < 0) {
+            set_error("fw_step: probe tracker %d invalid", i);
+            return FW_ERR_ARG;
+        }
+        for (int v = 0; v < P.n_vars; ++v)
+            if (P.var_ids[v] < 0 || P.var_ids[v] > mi.ns) {
+                set_error("fw_step: probe tracker %d var id %d out of range", i,
+                          P.var_ids[v]);
+                return FW_ERR_ARG;
+            }
+    }
+    return FW_OK;
+}
+
+}  // namespace
+}  // namespace fw
+
+extern "C" {
+
+int fw_version(void) { return 100; }
+
+size_t fw_struct_size(int32_t which)
+{
+    switch (which) {
+    case 0: return sizeof(fw_step_args);
+    case 1: return sizeof(fw_stim);
+    case 2: return sizeof(fw_at_tracker);
+    case 3: return sizeof(fw_lat_tracker);
+    case 4: return sizeof(fw_probe_tracker);
+    case 5: return sizeof(fw_window);
+    }
+    return 0;
+}
+
+const char *fw_last_error(void) { return fw::g_err; }
+
+int64_t fw_launch_count(void) { return fw::g_launches.load(); }
+
+int fw_model_info(int32_t model, int32_t *n_state, int32_t *n_params)
+{
+    fw::Info mi = fw::model_info(model);
+    if (mi.ns < 0) {
+        fw::set_error("fw_model_info: model %d not supported", model);
+        return FW_ERR_UNSUPPORTED;
+    }
+    if (n_state) *n_state = mi.ns;
+    if (n_params) *n_params = mi.np;
+    return FW_OK;
+}
+
+int fw_state_is_f64(int32_t model, int32_t precision, int32_t index)
+{
+    (void)index;
+    if (precision == FW_F64) return 1;
+    switch (model) {
+    default: return 0;
+    }
+}
+
+int fw_build_weights(int32_t stencil, int32_t precision, const int8_t *mesh,
+                     const double *cond, double cond_scalar,
+                     const double *fibers, double D_al, double D_ac,
+                     double D_model, double dt, double dr2, int64_t ni,
+                     int64_t nj, int64_t nk, void *w_out, void *stream)
+{
+    return fw::build_weights(stencil, precision, mesh, cond, cond_scalar,
+                             fibers, D_al, D_ac, D_model, dt, dr2, ni, nj, nk,
+                             w_out, (cudaStream_t)stream);
+}
+
+int fw_diffuse(int32_t stencil, int32_t precision, void *u_new, const void *u,
+               const void *w, const int64_t *idx, int64_t n_idx, int64_t ni,
+               int64_t nj, int64_t nk, void *stream)
+{
+    return fw::diffuse(stencil, precision, u_new, u, w, idx, n_idx, ni, nj, nk,
+                       (cudaStream_t)stream);
+}
+
+int fw_ionic(int32_t model, int32_t precision, void *u_new, const void *u,
+             void *const *state, const int64_t *idx, int64_t n_idx,
+             double dt, const double *params, void *stream)
+{
+    fw::Info mi = fw::model_info(model);
+    if (mi.ns < 0) {
+        fw::set_error("fw_ionic: model %d not supported", model);
+        return FW_ERR_UNSUPPORTED;
+    }
+    if (!u_new || !u || !state || !params || (n_idx > 0 && !idx)) {
+        fw::set_error("fw_ionic: null pointer");
+        return FW_ERR_ARG;
+    }
+    for (int i = 0; i < mi.ns; ++i)
+        if (!state[i]) {
+            fw::set_error("fw_ionic: state variable %d is NULL", i);
+            return FW_ERR_ARG;
+        }
+    return fw::ionic(model, precision, u_new, u, state, idx, n_idx, dt, params,
+                     (cudaStream_t)stream);
+}
+
+int fw_step(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+            void *stream)
+{
+    int rc = fw::check_step_args(a, n_steps);
+    if (rc) return rc;
+    if (n_steps == 0) return FW_OK;
+    if (a->form == FW_FORM_FUSED)
+        return fw::step_fused(a, n_begin, n_steps, (cudaStream_t)stream);
+    return fw::step_plain(a, n_begin, n_steps, (cudaStream_t)stream);
+}
+
+}  // extern "C"

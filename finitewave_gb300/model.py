@@ -1,0 +1,556 @@
+"""Cardiac models: device-resident state and the chunked run loop.
+
+``CardiacModel.run`` keeps the reference's semantics (``core/model/
+cardiac_model.py:130-189``) -- per step: stimuli, diffusion, ionic update,
+trackers, ``t += dt``, ``step += 1``, swap, commands, state saver,
+termination -- but runs the steps on the GPU in segments: the host replays
+the float64 time accumulation, cuts the run at every step where host-side
+work is due (a command, a state save, termination), and hands each segment
+to ``fw_step`` with the stimulus windows and tracker windows that fall into
+it.  Between segments nothing is copied back unless a host object asks for
+a state variable.
+
+State variables (``u``, ``v``, ...) live in device tensors; reading
+``model.u`` returns a host numpy copy and assigning ``model.u = array``
+uploads it, so state loaders, savers and commands work unchanged.
+"""
+import copy
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _ffi
+from .stencil import (AsymmetricStencil2D, AsymmetricStencil3D,
+                      IsotropicStencil2D, IsotropicStencil3D)
+from .stimulation import Stim
+from .tracker import (ActivationTime2DTracker, LocalActivationTime2DTracker,
+                      _ProbeTracker)
+
+_NP = {"float64": np.float64, "float32": np.float32}
+_MAX_SEGMENT = 1 << 20
+
+
+def _np_name(npfloat):
+    name = np.dtype(npfloat).name
+    if name not in _NP:
+        raise ValueError(f"npfloat must be float64 or float32, got {npfloat}")
+    return name
+
+
+class _StateVar:
+    """Descriptor: a state variable held on the device, seen as numpy."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __get__(self, obj, cls=None):
+        if obj is None:
+            return self
+        dev = obj.__dict__.get("_dev")
+        if dev and self.name in dev:
+            return dev[self.name].cpu().numpy()
+        return obj.__dict__.get("_host", {}).get(self.name, np.ndarray)
+
+    def __set__(self, obj, value):
+        dev = obj.__dict__.get("_dev")
+        if dev and self.name in dev and isinstance(value, np.ndarray):
+            t = dev[self.name]
+            if value.shape != tuple(t.shape):
+                raise ValueError(f"{self.name}: shape {value.shape} != "
+                                 f"{tuple(t.shape)}")
+            t.copy_(torch.as_tensor(np.ascontiguousarray(value)).to(t.dtype))
+            return
+        obj.__dict__.setdefault("_host", {})[self.name] = value
+
+
+class CardiacModel:
+    """Base class of the GPU models (core/model/cardiac_model.py:9-239).
+
+    Subclasses define ``_model_id`` (fwgpu.h fw_model), ``_state_names``
+    (state variables after ``u``, in the library's order), ``_param_names``
+    (parameters in the library's order) and ``select_stencil``.
+
+    Extra attributes over the reference: ``device`` (CUDA device, default
+    the current one) and ``form`` ('plain', 'fused' or None for automatic:
+    fused for float32 where the library has it, plain otherwise).
+    """
+
+    _model_id = None
+    _state_names = ()
+    _param_names = ()
+    _reset_u_new = False
+
+    u = _StateVar("u")
+    u_new = _StateVar("u_new")
+
+    def __init_subclass__(cls, **kw):
+        super().__init_subclass__(**kw)
+        for name in cls._state_names:
+            if not isinstance(cls.__dict__.get(name), _StateVar):
+                setattr(cls, name, _StateVar(name))
+
+    def __init__(self):
+        self.meta = {}
+        self.cardiac_tissue = None
+        self.stim_sequence = None
+        self.tracker_sequence = None
+        self.command_sequence = None
+        self.state_loader = None
+        self.state_saver = None
+        self.stencil = None
+        self.diffusion_kernel = None
+        self.ionic_kernel = None
+        self.weights = None
+        self.dt = 0.
+        self.dr = 0.
+        self.t_max = 0.
+        self.t = 0
+        self.step = 0
+        self.D_model = 1.
+        self.prog_bar = True
+        self.npfloat = np.float64
+        self.state_vars = []
+        self.device = None
+        self.form = None
+        self.fused_k = 0
+        self._dev = {}
+        self._t_hist = []
+
+    # ------------------------------------------------------------ helpers
+    def _device(self):
+        if self.device is not None:
+            return torch.device(self.device)
+        if not torch.cuda.is_available():
+            raise RuntimeError("finitewave_gb300 needs a CUDA device")
+        return torch.device("cuda", torch.cuda.current_device())
+
+    def _np_dtype(self):
+        return _NP[_np_name(self.npfloat)]
+
+    def _precision(self):
+        return _ffi.F64 if _np_name(self.npfloat) == "float64" else _ffi.F32
+
+    def _torch_dtype(self, state_index=None):
+        if state_index is not None and _ffi.state_is_f64(
+                self._model_id, self._precision(), state_index):
+            return torch.float64
+        return torch.float64 if self._precision() == _ffi.F64 \
+            else torch.float32
+
+    def _shape(self):
+        return tuple(np.asarray(self.cardiac_tissue.mesh).shape)
+
+    def _params(self):
+        return [float(getattr(self, n)) for n in self._param_names]
+
+    def _time_of_steps(self, steps):
+        """Model time t at the given global step indices (the float64
+        accumulation t += dt, as the reference computes it)."""
+        hist = self._t_hist_array()
+        return hist[np.asarray(steps, dtype=np.int64)]
+
+    def _t_hist_array(self):
+        if len(self._t_hist) != 1:
+            self._t_hist = [np.concatenate(self._t_hist)] if self._t_hist \
+                else [np.zeros(0)]
+        return self._t_hist[0]
+
+    # ---------------------------------------------------------- lifecycle
+    def initialize(self):
+        """Allocate state on the device, build weights, set up stimuli,
+        trackers, commands and state I/O (cardiac_model.py:91-117) and
+        then the model's initial values."""
+        dev = self._device()
+        shape = self._shape()
+        dtype = self._torch_dtype()
+        self._dev = {}
+        u = torch.zeros(shape, dtype=dtype, device=dev)
+        self._dev["u"] = u
+        self._dev["u_new"] = u.clone()
+        self.step = 0
+        self.t = 0
+        self._t_hist = []
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.compute_weights()
+        self.diffusion_kernel = self.stencil.select_diffusion_kernel()
+        if self.stim_sequence:
+            self.stim_sequence.initialize(self)
+        if self.tracker_sequence:
+            self.tracker_sequence.initialize(self)
+        if self.command_sequence:
+            self.command_sequence.initialize(self)
+        if self.state_loader:
+            self.state_loader.initialize(self)
+        if self.state_saver:
+            self.state_saver.initialize(self)
+        init_u = float(getattr(self, "init_u", 0.0))
+        self._dev["u"].fill_(init_u)
+        if self._reset_u_new:
+            self._dev["u_new"].copy_(self._dev["u"])
+        for i, name in enumerate(self._state_names):
+            t = torch.empty(shape, dtype=self._torch_dtype(i), device=dev)
+            t.fill_(float(getattr(self, "init_" + name)))
+            self._dev[name] = t
+
+    def compute_weights(self):
+        """Myocyte indices, stencil choice and device weights
+        (cardiac_model.py:119-128)."""
+        tissue = self.cardiac_tissue
+        tissue.compute_myo_indexes()
+        mesh = np.asarray(tissue.mesh)
+        myo = mesh == 1
+        if tissue.special_boundaries is not None:
+            myo &= np.asarray(tissue.special_boundaries) == 0
+        ring = np.zeros(mesh.shape, dtype=bool)
+        for ax in range(mesh.ndim):
+            sl = [slice(None)] * mesh.ndim
+            sl[ax] = 0
+            ring[tuple(sl)] = True
+            sl[ax] = -1
+            ring[tuple(sl)] = True
+        if (myo & ring).any():
+            raise ValueError("myocytes (mesh == 1) on the outer ring of the "
+                             "grid are not supported: the stencil would "
+                             "read outside the grid")
+        dev = self._device()
+        self._mesh_d = torch.as_tensor(np.ascontiguousarray(mesh, np.int8),
+                                       device=dev)
+        self._myo_d = torch.as_tensor(myo.astype(np.int8), device=dev)
+        self._special = tissue.special_boundaries is not None and bool(
+            (np.asarray(tissue.special_boundaries)[mesh == 1] != 0).any())
+        if self.stencil is None:
+            self.stencil = self.select_stencil(tissue)
+        self.weights = self.stencil.compute_weights(self, tissue)
+
+    def select_stencil(self, cardiac_tissue):
+        raise NotImplementedError
+
+    def run_diffusion_kernel(self):
+        """One diffusion pass u_new = W u over the myocytes
+        (cardiac_model.py:205-211)."""
+        idx = torch.as_tensor(self.cardiac_tissue.myo_indexes,
+                              device=self._device())
+        self.diffusion_kernel(self._dev["u_new"], self._dev["u"],
+                              self.weights, idx)
+
+    def run_ionic_kernel(self):
+        """One ionic pass over the myocytes (the models' run_ionic_kernel)."""
+        idx = torch.as_tensor(
+            np.asarray(self.cardiac_tissue.myo_indexes, dtype=np.int64),
+            device=self._device())
+        ptrs = [self._dev[n].data_ptr() for n in self._state_names]
+        arr = (ctypes.c_void_p * max(1, len(ptrs)))(*ptrs)
+        par = (ctypes.c_double * max(1, len(self._param_names)))(
+            *self._params())
+        _ffi.call("fw_ionic", self._model_id, self._precision(),
+                  self._dev["u_new"].data_ptr(), self._dev["u"].data_ptr(),
+                  arr, idx.data_ptr(), idx.numel(), float(self.dt), par,
+                  torch.cuda.current_stream().cuda_stream)
+
+    def check_termination(self):
+        max_iters = int(np.ceil(self.t_max / self.dt))
+        return (self.t > self.t_max) or (self.step > max_iters)
+
+    def clone(self):
+        return copy.deepcopy(self)
+
+    # ---------------------------------------------------------------- run
+    def run(self, initialize=True, num_of_theads=None):
+        """Run the simulation to t_max (cardiac_model.py:130-189).
+
+        ``num_of_theads`` is accepted for interface compatibility; the work
+        runs on the GPU.
+        """
+        if initialize:
+            self.initialize()
+        if self.t_max < self.t:
+            raise ValueError("t_max must be greater than current t.")
+        if self.state_loader:
+            self.state_loader.load()
+        iters = int(np.ceil((self.t_max - self.t) / self.dt))
+        remaining = iters
+        while remaining > 0:
+            n_seg = self._run_segment(min(remaining, _MAX_SEGMENT),
+                                      sync=False)
+            remaining -= n_seg
+            if self.command_sequence:
+                self.command_sequence.execute_next()
+            if self.state_saver:
+                self.state_saver.save()
+            if self.check_termination():
+                if self.state_saver:
+                    self.state_saver.save()
+                break
+        self._check_status()
+
+    def _segment_times(self, limit):
+        """Times t_n of the next `limit` steps and the segment length: the
+        first step after which a command, a state save or termination is
+        due ends the segment."""
+        acc = np.empty(limit + 1)
+        acc[0] = self.t
+        acc[1:] = self.dt
+        ts_all = np.add.accumulate(acc)
+        after = ts_all[1:]
+        steps_after = self.step + 1 + np.arange(limit)
+        stop = (after > self.t_max) | (steps_after >
+                                       int(np.ceil(self.t_max / self.dt)))
+        if self.command_sequence:
+            for c in self.command_sequence.sequence:
+                if not c.passed and c.t is not None:
+                    stop |= after >= c.t
+        saver = self.state_saver
+        if saver is not None:
+            savers = getattr(saver, "savers", None) or [saver]
+            for s in savers:
+                if getattr(s, "passed", True):
+                    continue
+                if s.time < 0:
+                    stop |= after >= self.t_max
+                else:
+                    stop |= after >= s.time
+        n_seg = int(np.argmax(stop)) + 1 if stop.any() else limit
+        return ts_all[:n_seg], float(ts_all[n_seg]), n_seg
+
+    def _form(self):
+        if self.form is not None:
+            return _ffi.FORM_FUSED if self.form == "fused" else \
+                _ffi.FORM_PLAIN
+        return _ffi.FORM_PLAIN
+
+    def _check_status(self):
+        st = int(self._status.item())
+        if st & _ffi.FW_DEV_PROBE_OVERFLOW:
+            raise RuntimeError("probe tracker buffer overflow")
+        if st & _ffi.FW_DEV_LAT_OVERFLOW:
+            raise RuntimeError("LocalActivationTimeTracker: a node crossed "
+                               "the threshold more often than its capacity")
+
+    def _run_segment(self, limit, sync=True):
+        """Advance up to `limit` steps on the device (one fw_step call);
+        returns the number of steps taken.  With sync=False the device
+        status word is not read back (no host synchronisation)."""
+        ts, t_end, n_seg = self._segment_times(limit)
+        n0 = int(self.step)
+        self._t_hist.append(ts)
+        a = _ffi.StepArgs()
+        a.model = self._model_id
+        a.stencil = self.stencil.kind
+        a.precision = self._precision()
+        shape = self._shape()
+        a.ni, a.nj = shape[0], shape[1]
+        a.nk = shape[2] if len(shape) == 3 else 1
+        a.mesh = self._mesh_d.data_ptr()
+        a.myo = self._myo_d.data_ptr()
+        a.weights = self.weights.data_ptr()
+        a.u[0] = self._dev["u"].data_ptr()
+        a.u[1] = self._dev["u_new"].data_ptr()
+        for i, name in enumerate(self._state_names):
+            a.state[i] = self._dev[name].data_ptr()
+        for i, p in enumerate(self._params()):
+            a.params[i] = p
+        a.dt = float(self.dt)
+        a.fused_k = int(self.fused_k)
+        a.form = self._form()
+        if a.form == _ffi.FORM_FUSED and self._special:
+            a.form = _ffi.FORM_PLAIN
+        keep = []
+
+        # stimuli (stim_sequence.py:65-77)
+        n_st = 0
+        if self.stim_sequence:
+            for stim in self.stim_sequence.sequence:
+                if not isinstance(stim, Stim) or not hasattr(stim, "_region"):
+                    raise TypeError(f"{type(stim).__name__} is not a "
+                                    "finitewave_gb300 stimulus")
+                wins = stim._windows(ts, n0)
+                if not wins:
+                    continue
+                lo, hi, mask = stim._region(self)
+                if mask is not None:
+                    keep.append(mask)
+                for first, last, k in wins:
+                    if n_st >= _ffi.MAX_STIMS:
+                        raise RuntimeError("too many stimulus windows in one "
+                                           "segment")
+                    kind, value, has_umax, u_max = stim._kind_value(self, k)
+                    s = a.stims[n_st]
+                    s.kind, s.value = kind, value
+                    s.has_umax, s.u_max = has_umax, u_max
+                    s.first, s.last = first, last
+                    for d in range(3):
+                        s.lo[d] = lo[d] if d < len(lo) else 0
+                        s.hi[d] = hi[d] if d < len(hi) else 1
+                    s.mask = mask.data_ptr() if mask is not None else None
+                    n_st += 1
+        a.n_stims = n_st
+
+        # trackers (tracker.py:70-83)
+        n_at = n_lat = n_pr = 0
+        if self.tracker_sequence:
+            for tr in self.tracker_sequence.sequence:
+                win = tr._window(ts, n0)
+                if win is None:
+                    continue
+                first, last, count = win
+                if isinstance(tr, ActivationTime2DTracker):
+                    d = a.at[n_at]
+                    n_at += 1
+                    d.win.first, d.win.last, d.win.stride = first, last, \
+                        int(tr.step)
+                    d.threshold = float(tr.threshold)
+                    d.act_step = tr._act_step.data_ptr()
+                elif isinstance(tr, LocalActivationTime2DTracker):
+                    d = a.lat[n_lat]
+                    n_lat += 1
+                    d.win.first, d.win.last, d.win.stride = first, last, \
+                        int(tr.step)
+                    d.threshold = float(tr.threshold)
+                    d.activated = tr._activated.data_ptr()
+                    d.cross_steps = tr._steps.data_ptr()
+                    d.cross_count = tr._count.data_ptr()
+                    d.capacity = int(tr.capacity)
+                elif isinstance(tr, _ProbeTracker):
+                    buf = tr._reserve(count)
+                    d = a.probe[n_pr]
+                    n_pr += 1
+                    d.win.first, d.win.last, d.win.stride = first, last, \
+                        int(tr.step)
+                    d.n_cells = tr._n_cells
+                    d.n_vars = len(tr._var_ids)
+                    for i, v in enumerate(tr._var_ids):
+                        d.var_ids[i] = v
+                    d.cells = tr._cells.data_ptr()
+                    d.out = buf.data_ptr()
+                    d.sample_offset = 0
+                    d.capacity = count
+                else:
+                    raise TypeError(f"{type(tr).__name__} is not a "
+                                    "finitewave_gb300 tracker")
+        a.n_at, a.n_lat, a.n_probe = n_at, n_lat, n_pr
+        a.status = self._status.data_ptr()
+        stream = torch.cuda.current_stream().cuda_stream
+        _ffi.call("fw_step", ctypes.byref(a), n0, n_seg, stream)
+        if sync:
+            self._check_status()
+        del keep
+        if n_seg % 2 == 1:
+            self._dev["u"], self._dev["u_new"] = (self._dev["u_new"],
+                                                  self._dev["u"])
+        self.t = t_end
+        self.step = n0 + n_seg
+        return n_seg
+
+
+# ------------------------------------------------------------------ models
+
+def _stencil_2d(tissue):
+    return IsotropicStencil2D() if tissue.fibers is None \
+        else AsymmetricStencil2D()
+
+
+def _stencil_3d(tissue):
+    return IsotropicStencil3D() if tissue.fibers is None \
+        else AsymmetricStencil3D()
+
+
+class AlievPanfilov2D(CardiacModel):
+    """Aliev-Panfilov (cpuwave2D/model/aliev_panfilov_2d.py:10-335)."""
+
+    _model_id = _ffi.MODEL_AP
+    _state_names = ("v",)
+    _param_names = ("a", "k", "eap", "mu_1", "mu_2")
+
+    def __init__(self):
+        super().__init__()
+        self.D_model = 1.
+        self.state_vars = ["u", "v"]
+        self.npfloat = "float64"
+        self.a = 0.1
+        self.k = 8.0
+        self.eap = 0.01
+        self.mu_1 = 0.2
+        self.mu_2 = 0.3
+        self.init_u = 0.0
+        self.init_v = 0.0
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_2d(cardiac_tissue)
+
+
+class AlievPanfilov3D(AlievPanfilov2D):
+    """(cpuwave3D/model/aliev_panfilov_3d.py)"""
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_3d(cardiac_tissue)
+
+
+class MitchellSchaeffer2D(CardiacModel):
+    """Mitchell-Schaeffer (cpuwave2D/model/mitchell_schaeffer_2d.py)."""
+
+    _model_id = _ffi.MODEL_MS
+    _state_names = ("h",)
+    _param_names = ("tau_close", "tau_open", "tau_in", "tau_out", "u_gate")
+
+    def __init__(self):
+        super().__init__()
+        self.D_model = 1.
+        self.state_vars = ["u", "h"]
+        self.npfloat = "float64"
+        self.tau_close = 150
+        self.tau_open = 120
+        self.tau_out = 6
+        self.tau_in = 0.3
+        self.u_gate = 0.13
+        self.init_u = 0.0
+        self.init_h = 1.0
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_2d(cardiac_tissue)
+
+
+class MitchellSchaeffer3D(MitchellSchaeffer2D):
+    """(cpuwave3D/model/mitchell_schaeffer_3d.py)"""
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_3d(cardiac_tissue)
+
+
+class FentonKarma2D(CardiacModel):
+    """Fenton-Karma MLR-I (cpuwave2D/model/fenton_karma_2d.py)."""
+
+    _model_id = _ffi.MODEL_FK
+    _state_names = ("v", "w")
+    _param_names = ("tau_d", "tau_o", "tau_r", "tau_si", "tau_v_m",
+                    "tau_v_p", "tau_w_m", "tau_w_p", "k", "u_c", "uc_si")
+
+    def __init__(self):
+        super().__init__()
+        self.D_model = 1.
+        self.state_vars = ["u", "v", "w"]
+        self.npfloat = "float64"
+        self.tau_r = 130
+        self.tau_o = 12.5
+        self.tau_d = 0.172
+        self.tau_si = 127
+        self.tau_v_m = 18.2
+        self.tau_v_p = 10
+        self.tau_w_m = 80
+        self.tau_w_p = 1020
+        self.k = 10
+        self.u_c = 0.13
+        self.uc_si = 0.85
+        self.init_u = 0.0
+        self.init_v = 1.0
+        self.init_w = 1.0
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_2d(cardiac_tissue)
+
+
+class FentonKarma3D(FentonKarma2D):
+    """(cpuwave3D/model/fenton_karma_3d.py)"""
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_3d(cardiac_tissue)

@@ -1,0 +1,255 @@
+/*
+ * fwgpu.h -- C ABI of the GB300 (sm_103a) monodomain-step library.
+ *
+ * The library advances Finitewave's explicit monodomain scheme on one GPU:
+ * stimulus application, the finite-difference diffusion stencil, the per-node
+ * ionic update and the activation-time / probe trackers, for the models and
+ * stencils of the reference's cpuwave2D / cpuwave3D packages.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: FW_OK (0) or a negative FW_ERR_*
+ *    code; fw_last_error() gives a message for the calling thread.  No C++
+ *    exception, exit() or abort() crosses this interface.
+ *  - All array arguments are caller-owned device pointers (plain pointers plus
+ *    sizes).  The library allocates no device memory of its own.
+ *  - Arrays are C-order over the grid shape (ni, nj) or (ni, nj, nk), exactly
+ *    the reference's numpy layout.  A grid of N = ni*nj*nk nodes.  Per-node
+ *    stencil weights are stored weight-major ("structure of arrays"):
+ *    w[k*N + p] is weight k of node p, k in the reference's point order.
+ *  - Every call takes a stream (a cudaStream_t passed as void*) and is
+ *    asynchronous with respect to the host.  Results that depend on device
+ *    data (tracker overflow, bad input) go to a device status word that the
+ *    caller reads when it next synchronises.
+ *  - Calls on different streams with disjoint buffers may run concurrently.
+ */
+#ifndef FWGPU_H
+#define FWGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define FW_API __attribute__((visibility("default")))
+#else
+#define FW_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------- status codes */
+#define FW_OK 0
+#define FW_ERR_ARG (-1)         /* invalid argument (pointer, size, enum)   */
+#define FW_ERR_CUDA (-2)        /* a CUDA runtime call failed               */
+#define FW_ERR_UNSUPPORTED (-3) /* valid but not implemented combination    */
+
+/* bits of the device status word (int32, OR-ed by kernels) */
+#define FW_DEV_LAT_OVERFLOW 1   /* a cell crossed more often than capacity  */
+#define FW_DEV_PROBE_OVERFLOW 2 /* a probe sample index beyond capacity     */
+#define FW_DEV_BATCH_FAULT 4    /* a batch tile descriptor out of range     */
+
+/* ------------------------------------------------------------ enumerations */
+enum fw_model {
+    FW_MODEL_AP = 1,   /* Aliev-Panfilov       cpuwave2D/model/aliev_panfilov_2d.py  */
+    FW_MODEL_MS = 2,   /* Mitchell-Schaeffer   cpuwave2D/model/mitchell_schaeffer_2d.py */
+    FW_MODEL_FK = 3,   /* Fenton-Karma (MLR-I) cpuwave2D/model/fenton_karma_2d.py    */
+    FW_MODEL_TP06 = 4, /* ten Tusscher-Panfilov 2006 cpuwave2D/model/tp06_2d.py      */
+    FW_MODEL_CRN = 5   /* Courtemanche 1998    cpuwave2D/model/courtemanche_2d.py    */
+};
+
+enum fw_stencil {
+    FW_STENCIL_ISO5 = 1,    /* IsotropicStencil2D   (i-1,j),(i,j-1),(i,j),(i,j+1),(i+1,j) */
+    FW_STENCIL_ANISO9 = 2,  /* AsymmetricStencil2D  (i-1,j-1)...(i+1,j+1)                 */
+    FW_STENCIL_ISO7 = 3,    /* IsotropicStencil3D   order of isotropic_stencil_3d.py:16-23  */
+    FW_STENCIL_ANISO19 = 4  /* AsymmetricStencil3D  order of asymmetric_stencil_3d.py:25-44 */
+};
+
+/* Arithmetic policy.  FW_F64: every array float64 (the reference's default
+ * npfloat).  FW_F32: u, gates and weights float32; for TP06 / Courtemanche
+ * the ion-concentration state variables stay float64 (see fw_state_is_f64). */
+enum fw_precision { FW_F64 = 0, FW_F32 = 1 };
+
+/* Execution form.  FW_FORM_PLAIN: one launch per time step (plus a stimulus
+ * launch on steps where a stimulus fires), reference operation order.
+ * FW_FORM_FUSED: 2D FP32 Aliev-Panfilov / Mitchell-Schaeffer / Fenton-Karma
+ * only; several time steps per launch on shared-memory tiles (temporal
+ * blocking), stimuli and trackers applied inside the launch. */
+enum fw_form { FW_FORM_PLAIN = 0, FW_FORM_FUSED = 1 };
+
+enum fw_stim_kind { FW_STIM_VOLTAGE = 0, FW_STIM_CURRENT = 1 };
+
+#define FW_MAX_STATE 24
+#define FW_MAX_PARAMS 64
+#define FW_MAX_STIMS 16
+#define FW_MAX_AT 4
+#define FW_MAX_LAT 2
+#define FW_MAX_PROBE 4
+#define FW_MAX_PROBE_VARS 8
+
+/* A set of global step indices n with first <= n <= last and
+ * n % stride == 0.  Trackers are active on exactly those steps; the host
+ * derives first/last from the tracker's start_time/end_time by replaying the
+ * float64 time accumulation t += dt (core/tracker/tracker.py:70-83). */
+typedef struct fw_window {
+    int64_t first, last, stride;
+} fw_window;
+
+/* One stimulus.  Replaces StimVoltageCoord2D/3D, StimCurrentCoord2D/3D,
+ * StimVoltageMatrix2D/3D, StimCurrentMatrix2D/3D, StimCurrentArea2D/3D
+ * (cpuwave2D/stimulation/, cpuwave3D/stimulation/) as driven by
+ * StimSequence.stimulate_next (core/stimulation/stim_sequence.py:65-77).
+ * Applied on steps first..last (inclusive) to nodes p inside the half-open
+ * box with mesh[p] == 1 and (mask == NULL || mask[p] != 0):
+ *   voltage: u[p] = value
+ *   current: u[p] += value (value = dt * curr_value), then
+ *            u[p] = min(u[p], u_max) when has_umax. */
+typedef struct fw_stim {
+    int32_t kind;
+    int32_t has_umax;
+    int64_t first, last;
+    double value;
+    double u_max;
+    int64_t lo[3], hi[3];
+    const int8_t *mask;
+} fw_stim;
+
+/* ActivationTime2D/3DTracker (cpuwave2D/tracker/activation_time_2d_tracker.py:
+ * 51-63): on active steps n, act_step[p] = n where act_step[p] < 0 and
+ * u[p] > threshold (u read after stimuli, before diffusion).  act_step is
+ * int32, initialised to -1 by the caller; the host maps n to its time. */
+typedef struct fw_at_tracker {
+    fw_window win;
+    double threshold;
+    int32_t *act_step;
+} fw_at_tracker;
+
+/* LocalActivationTime2D/3DTracker (local_activation_time_2d_tracker.py:58-89):
+ * on active steps, cross = u >= threshold && !activated[p]: activated[p] = 1
+ * and n is appended to the cell's crossing list; backcross = u < threshold &&
+ * activated[p]: activated[p] = 0.  cross_steps is (capacity, N) int32,
+ * cross_count is N int32; the host rebuilds the reference's layered output.
+ * More than `capacity` crossings set FW_DEV_LAT_OVERFLOW. */
+typedef struct fw_lat_tracker {
+    fw_window win;
+    double threshold;
+    uint8_t *activated;
+    int32_t *cross_steps;
+    int32_t *cross_count;
+    int32_t capacity;
+} fw_lat_tracker;
+
+/* ActionPotential*Tracker / MultiVariable*Tracker / Variable*Tracker
+ * (action_potential_2d_tracker.py:46-53, multi_variable_2d_tracker.py:58-69):
+ * on active steps, out[((s * n_vars) + v) * n_cells + c] = var_v[cells[c]]
+ * with sample index s = sample_offset + (n - win.first) / win.stride
+ * (win.first must be the first active step).  var id 0 is u (the value the
+ * trackers see: after stimuli, before the step); id k >= 1 is state var k-1
+ * (already advanced by the ionic update, as in the reference). */
+typedef struct fw_probe_tracker {
+    fw_window win;
+    int32_t n_cells;
+    int32_t n_vars;
+    int32_t var_ids[FW_MAX_PROBE_VARS];
+    const int64_t *cells;
+    double *out;
+    int64_t sample_offset;
+    int64_t capacity; /* samples */
+} fw_probe_tracker;
+
+/* Everything one model instance needs to advance.  Replaces the body of
+ * CardiacModel.run (core/model/cardiac_model.py:164-189) together with the
+ * model's run_diffusion_kernel / run_ionic_kernel. */
+typedef struct fw_step_args {
+    int32_t model;      /* enum fw_model   */
+    int32_t stencil;    /* enum fw_stencil */
+    int32_t precision;  /* enum fw_precision */
+    int32_t form;       /* enum fw_form    */
+    int64_t ni, nj, nk; /* nk = 1 for 2D grids */
+    const int8_t *mesh; /* tissue mesh codes 0/1/2 (stimuli test mesh == 1)  */
+    const int8_t *myo;  /* 1 where mesh == 1 and special_boundaries == 0     */
+    const void *weights;         /* (nw, N), float64 or float32 by precision */
+    void *u[2];                  /* u[0]: u at n_begin, u[1]: the other buffer */
+    void *state[FW_MAX_STATE];   /* the model's state variables after u      */
+    double params[FW_MAX_PARAMS];
+    double dt;
+    int32_t n_stims;
+    int32_t n_at;
+    int32_t n_lat;
+    int32_t n_probe;
+    fw_stim stims[FW_MAX_STIMS];
+    fw_at_tracker at[FW_MAX_AT];
+    fw_lat_tracker lat[FW_MAX_LAT];
+    fw_probe_tracker probe[FW_MAX_PROBE];
+    int32_t *status;  /* device int32 status word (may be NULL)             */
+    int32_t fused_k;  /* FW_FORM_FUSED time steps per launch (0 = default)  */
+} fw_step_args;
+
+/* Library version (major*10000 + minor*100 + patch). */
+FW_API int fw_version(void);
+
+/* sizeof of the ABI structs as compiled into the library, so a binding can
+ * check its own layout: which = 0 fw_step_args, 1 fw_stim, 2 fw_at_tracker,
+ * 3 fw_lat_tracker, 4 fw_probe_tracker, 5 fw_window.  0 for unknown. */
+FW_API size_t fw_struct_size(int32_t which);
+
+/* Number of kernels this library has launched in the process so far
+ * (a monotonic statistics counter, for benchmarks and tests). */
+FW_API int64_t fw_launch_count(void);
+
+/* Message for the last non-OK status returned on the calling thread. */
+FW_API const char *fw_last_error(void);
+
+/* Number of state variables after u, and the parameter count, of a model;
+ * the order is that of the reference class's state_vars (minus "u") and of
+ * the parameter list documented in fw_models.cuh. */
+FW_API int fw_model_info(int32_t model, int32_t *n_state, int32_t *n_params);
+
+/* 1 when state variable `index` of `model` is stored as float64 under
+ * `precision` (always 1 for FW_F64). */
+FW_API int fw_state_is_f64(int32_t model, int32_t precision, int32_t index);
+
+/* Stencil weights.  Replaces Stencil.compute_weights (core/stencil/stencil.py:
+ * 14) as implemented by IsotropicStencil2D (isotropic_stencil_2d.py:41-69),
+ * AsymmetricStencil2D (asymmetric_stencil_2d.py:46-84), IsotropicStencil3D
+ * (isotropic_stencil_3d.py:45-74) and AsymmetricStencil3D
+ * (asymmetric_stencil_3d.py:61-105).  Computed in float64 with the
+ * reference's operation order (bitwise equal to it), then stored as float64
+ * or rounded to float32 by `precision`.
+ *   mesh       int8 codes (N)
+ *   cond       float64 conductivity per node (N), or NULL for cond_scalar
+ *   fibers     float64 (N, ndim) unit vectors; NULL for isotropic stencils
+ *   dr2        dr**2 as the host language computes it
+ *   w_out      (nw, N) float64 or float32 */
+FW_API int fw_build_weights(int32_t stencil, int32_t precision, const int8_t *mesh,
+                     const double *cond, double cond_scalar,
+                     const double *fibers, double D_al, double D_ac,
+                     double D_model, double dt, double dr2, int64_t ni,
+                     int64_t nj, int64_t nk, void *w_out, void *stream);
+
+/* One diffusion pass u_new[p] = sum_k w[k][p] * u[nbr_k(p)] over the flat
+ * myocyte list idx.  Replaces the stencils' diffusion_kernel(u_new, u, w,
+ * indexes) callables (isotropic_stencil_2d.py:97-132, asymmetric_stencil_2d.py
+ * :164-201, isotropic_stencil_3d.py:78-109, asymmetric_stencil_3d.py:108-160),
+ * which the ECG trackers also call (ecg_2d_tracker.py:61-79). */
+FW_API int fw_diffuse(int32_t stencil, int32_t precision, void *u_new, const void *u,
+               const void *w, const int64_t *idx, int64_t n_idx, int64_t ni,
+               int64_t nj, int64_t nk, void *stream);
+
+/* One ionic pass over idx: state updated in place and u_new[p] += dt * I(p).
+ * Replaces the models' ionic_kernel_2d/3d (e.g. aliev_panfilov_2d.py:376-406)
+ * as called by run_ionic_kernel.  state and params as in fw_step_args. */
+FW_API int fw_ionic(int32_t model, int32_t precision, void *u_new, const void *u,
+             void *const *state, const int64_t *idx, int64_t n_idx,
+             double dt, const double *params, void *stream);
+
+/* Advance n_steps time steps starting at global step n_begin (the model's
+ * step counter).  On return the current u is a->u[n_steps & 1]. */
+FW_API int fw_step(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+            void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FWGPU_H */

@@ -93,13 +93,14 @@ static void half_aniso(const double *c, const double *f, const int64_t *shape,
     }
 }
 
-/* weights * D_model * dt / dr**2, then +1 on the centre
+/* weights * D_model * dt / dr**2, then +1 on the centre.  dr2 is the
+ * caller's `dr**2` as Python computes it (libm pow, which differs from dr*dr
+ * in the last ulp for some dr)
  * (isotropic_stencil_2d.py:66-67, asymmetric_stencil_2d.py:81-82, and the
  * 3D equivalents). */
 static void scale_weights(double *w, int64_t n, int nw, int centre,
-                          double D_model, double dt, double dr)
+                          double D_model, double dt, double dr2)
 {
-    double dr2 = dr * dr;
     #pragma omp parallel for schedule(static)
     for (int64_t p = 0; p < n; ++p) {
         for (int k = 0; k < nw; ++k)
@@ -124,7 +125,7 @@ static inline double icomp(double d, int m0, int m1)
  * 161-204).  Order: (i-1,j), (i,j-1), (i,j), (i,j+1), (i+1,j). */
 EXPORT void fwo_weights_2d_iso5(const int8_t *mesh, const double *cond,
                                 int64_t ni, int64_t nj, double D_model,
-                                double dt, double dr, double *w)
+                                double dt, double dr2, double *w)
 {
     int64_t n = ni * nj, shape[2] = {ni, nj};
     double *dxx = malloc(sizeof(double) * n), *dyy = malloc(sizeof(double) * n);
@@ -144,7 +145,7 @@ EXPORT void fwo_weights_2d_iso5(const int8_t *mesh, const double *cond,
         o[4] = icomp(dxx[p], m01(mesh, ip), m01(mesh, im));
         o[2] = -(o[0] + o[1] + o[3] + o[4]);
     }
-    scale_weights(w, n, 5, 2, D_model, dt, dr);
+    scale_weights(w, n, 5, 2, D_model, dt, dr2);
     free(dxx);
     free(dyy);
 }
@@ -153,7 +154,7 @@ EXPORT void fwo_weights_2d_iso5(const int8_t *mesh, const double *cond,
  * .py:45-74, 113-149).  Order: (i-1), (j-1), (k-1), c, (k+1), (j+1), (i+1). */
 EXPORT void fwo_weights_3d_iso7(const int8_t *mesh, const double *cond,
                                 int64_t ni, int64_t nj, int64_t nk,
-                                double D_model, double dt, double dr,
+                                double D_model, double dt, double dr2,
                                 double *w)
 {
     int64_t n = ni * nj * nk, shape[3] = {ni, nj, nk};
@@ -176,7 +177,7 @@ EXPORT void fwo_weights_3d_iso7(const int8_t *mesh, const double *cond,
         o[6] = icomp(dxx[p], m01(mesh, p + si), m01(mesh, p - si));
         o[3] = -(o[0] + o[1] + o[2] + o[4] + o[5] + o[6]);
     }
-    scale_weights(w, n, 7, 3, D_model, dt, dr);
+    scale_weights(w, n, 7, 3, D_model, dt, dr2);
     free(dxx);
     free(dyy);
     free(dzz);
@@ -213,7 +214,7 @@ static inline void minor(double d, int m0, int m1, int m2, int m3, int m4,
 EXPORT void fwo_weights_2d_aniso9(const int8_t *mesh, const double *cond,
                                   const double *fibers, int64_t ni, int64_t nj,
                                   double D_al, double D_ac, double D_model,
-                                  double dt, double dr, double *w)
+                                  double dt, double dr2, double *w)
 {
     int64_t n = ni * nj, shape[2] = {ni, nj};
     double *dxx = malloc(sizeof(double) * n), *dxy = malloc(sizeof(double) * n),
@@ -261,7 +262,7 @@ EXPORT void fwo_weights_2d_aniso9(const int8_t *mesh, const double *cond,
 #undef M
 #undef AT
     }
-    scale_weights(w, n, 9, 4, D_model, dt, dr);
+    scale_weights(w, n, 9, 4, D_model, dt, dr2);
     free(dxx); free(dxy); free(dyx); free(dyy);
 }
 
@@ -273,7 +274,7 @@ EXPORT void fwo_weights_3d_aniso19(const int8_t *mesh, const double *cond,
                                    const double *fibers, int64_t ni,
                                    int64_t nj, int64_t nk, double D_al,
                                    double D_ac, double D_model, double dt,
-                                   double dr, double *w)
+                                   double dr2, double *w)
 {
     int64_t n = ni * nj * nk, shape[3] = {ni, nj, nk};
     double *d[3][3];
@@ -359,7 +360,7 @@ EXPORT void fwo_weights_3d_aniso19(const int8_t *mesh, const double *cond,
 #undef M
 #undef AT
     }
-    scale_weights(w, n, 19, 4, D_model, dt, dr);
+    scale_weights(w, n, 19, 4, D_model, dt, dr2);
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) free(d[a][b]);
 }

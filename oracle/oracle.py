@@ -112,21 +112,21 @@ def weights(kind, mesh, D_model, dt, dr, conductivity=1.0, fibers=None,
     if kind == "iso5":
         w = np.zeros((*mesh.shape, 5))
         L.fwo_weights_2d_iso5(_p(mesh), _p(cond), *mesh.shape, D_model, dt,
-                              dr, _p(w))
+                              dr ** 2, _p(w))
     elif kind == "iso7":
         w = np.zeros((*mesh.shape, 7))
         L.fwo_weights_3d_iso7(_p(mesh), _p(cond), *mesh.shape, D_model, dt,
-                              dr, _p(w))
+                              dr ** 2, _p(w))
     elif kind == "aniso9":
         f = np.ascontiguousarray(fibers, dtype=np.float64)
         w = np.zeros((*mesh.shape, 9))
         L.fwo_weights_2d_aniso9(_p(mesh), _p(cond), _p(f), *mesh.shape,
-                                D_al, D_ac, D_model, dt, dr, _p(w))
+                                D_al, D_ac, D_model, dt, dr ** 2, _p(w))
     elif kind == "aniso19":
         f = np.ascontiguousarray(fibers, dtype=np.float64)
         w = np.zeros((*mesh.shape, 19))
         L.fwo_weights_3d_aniso19(_p(mesh), _p(cond), _p(f), *mesh.shape,
-                                 D_al, D_ac, D_model, dt, dr, _p(w))
+                                 D_al, D_ac, D_model, dt, dr ** 2, _p(w))
     else:
         raise ValueError(kind)
     return w

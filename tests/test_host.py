@@ -1,0 +1,179 @@
+"""CPU-side tests: the C ABI library loads and exports what fwgpu.h declares,
+argument validation, and the host scheduling logic (stimulus and tracker
+windows, time accumulation, LAT layer reconstruction) against naive
+restatements of the reference's per-step rules."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from finitewave_gb300 import _ffi
+    return _ffi.load()
+
+
+def _declared():
+    with open(os.path.join(ROOT, "include", "fwgpu.h")) as f:
+        src = f.read()
+    return sorted(set(re.findall(r"FW_API\s+[\w\s\*]+?\b(fw_\w+)\s*\(", src)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = _declared()
+    assert "fw_step" in names and "fw_build_weights" in names
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_struct_layout_matches(lib):
+    from finitewave_gb300 import _ffi
+    for which, st in _ffi._STRUCTS.items():
+        assert lib.fw_struct_size(which) == ctypes.sizeof(st)
+
+
+def test_version_and_model_info(lib):
+    from finitewave_gb300 import _ffi
+    assert lib.fw_version() >= 100
+    assert _ffi.model_info(_ffi.MODEL_AP) == (1, 5)
+    assert _ffi.model_info(_ffi.MODEL_FK) == (2, 11)
+    with pytest.raises(_ffi.FwError) as e:
+        _ffi.model_info(99)
+    assert e.value.code == _ffi.FW_ERR_UNSUPPORTED
+
+
+def test_step_rejects_bad_args(lib):
+    """Validation happens before any CUDA call, so it runs without a GPU."""
+    from finitewave_gb300 import _ffi
+    assert lib.fw_step(None, 0, 1, None) == _ffi.FW_ERR_ARG
+    a = _ffi.StepArgs()
+    a.model, a.stencil, a.precision = _ffi.MODEL_AP, _ffi.ISO5, _ffi.F64
+    a.ni, a.nj, a.nk = 10, 10, 1
+    rc = lib.fw_step(ctypes.byref(a), 0, 1, None)
+    assert rc == _ffi.FW_ERR_ARG
+    assert b"missing" in lib.fw_last_error()
+    a.stencil = 77
+    assert lib.fw_step(ctypes.byref(a), 0, 1, None) == _ffi.FW_ERR_ARG
+    a.stencil, a.nk = _ffi.ISO7, 1
+    assert lib.fw_step(ctypes.byref(a), 0, 1, None) == _ffi.FW_ERR_ARG
+    assert b"does not fit" in lib.fw_last_error()
+
+
+def _times(t0, dt, n):
+    ts, t = [], t0
+    for _ in range(n):
+        ts.append(t)
+        t += dt
+    return np.array(ts), t
+
+
+def test_time_accumulation_matches_python_loop():
+    """np.add.accumulate replays `t += dt` exactly (cardiac_model.py:176)."""
+    for dt in (0.01, 0.0015, 0.001, 0.02):
+        n = 100000
+        acc = np.empty(n + 1)
+        acc[0] = 0
+        acc[1:] = dt
+        a = np.add.accumulate(acc)
+        ref, last = _times(0, dt, n)
+        assert np.array_equal(a[:n], ref)
+        assert a[n] == last
+
+
+def _naive_stim_steps(t_stim, dur, ts):
+    passed, out = False, []
+    for n, t in enumerate(ts):
+        if t >= t_stim and not passed:
+            out.append(n)
+            passed = t >= t_stim + dur
+    return out
+
+
+@pytest.mark.parametrize("t_stim,dur", [(0, 0.0), (31, 0.0), (5, 0.5),
+                                         (2.5, 0.7), (0.004, 0.01)])
+def test_stim_windows(t_stim, dur):
+    from finitewave_gb300.stimulation import StimCurrentCoord2D
+    ts, _ = _times(0, 0.01, 5000)
+    expect = _naive_stim_steps(t_stim, dur, ts)
+    s = StimCurrentCoord2D(t_stim, 1.0, dur, 0, 3, 0, 3)
+    got = []
+    # two segments, to cover a window that spans a segment boundary
+    cut = expect[len(expect) // 2] if expect else 100
+    for lo, hi in ((0, cut), (cut, len(ts))):
+        for first, last, _ in s._windows(ts[lo:hi], lo):
+            got.extend(range(first, last + 1))
+    assert got == expect
+
+
+def test_tracker_windows():
+    from finitewave_gb300.tracker import ActivationTime2DTracker
+    ts, _ = _times(0, 0.01, 3000)
+    tr = ActivationTime2DTracker()
+    tr.start_time, tr.end_time, tr.step = 1.0, 20.0, 7
+    first, last, count = tr._window(ts[500:], 500)
+    expect = [n for n, t in enumerate(ts) if n >= 500 and 1.0 <= t <= 20.0
+              and n % 7 == 0]
+    assert (first, last, count) == (expect[0], expect[-1], len(expect))
+
+
+class _FakeModel:
+    def __init__(self, shape, ts):
+        self.shape, self.ts = shape, ts
+
+    def _shape(self):
+        return self.shape
+
+    def _device(self):
+        return torch.device("cpu")
+
+    def _np_dtype(self):
+        return np.float64
+
+    def _time_of_steps(self, steps):
+        return self.ts[np.asarray(steps)]
+
+
+def test_lat_layer_reconstruction():
+    """Rebuild the reference's LAT layers from per-node crossing lists and
+    compare with a direct restatement of local_activation_time_2d_tracker.py
+    :58-89 on random crossing sequences."""
+    from finitewave_gb300.tracker import LocalActivationTime2DTracker
+    rng = np.random.default_rng(3)
+    shape = (6, 7)
+    n = 42
+    nsteps = 400
+    ts, _ = _times(0, 0.01, nsteps)
+    above = rng.random((nsteps, n)) < 0.08
+    # smear crossings into plateaus so nodes cross, stay, return
+    for k in range(1, nsteps):
+        above[k] |= above[k - 1] & (rng.random(n) < 0.8)
+    # reference semantics
+    act = [-np.ones(n)]
+    activated = np.zeros(n, bool)
+    events = [[] for _ in range(n)]
+    for k in range(nsteps):
+        cross = above[k] & ~activated
+        activated = np.where(cross, True, activated)
+        back = ~above[k] & activated
+        activated = np.where(back, False, activated)
+        if np.any(act[-1][cross] > -1):
+            act.append(-np.ones(n))
+        act[-1] = np.where(cross, ts[k], act[-1])
+        for c in np.flatnonzero(cross):
+            events[c].append(k)
+    tr = LocalActivationTime2DTracker()
+    tr.capacity = max(len(e) for e in events)
+    tr.initialize(_FakeModel(shape, ts))
+    for c, ev in enumerate(events):
+        tr._count[c] = len(ev)
+        for j, k in enumerate(ev):
+            tr._steps[j, c] = k
+    out = tr.output
+    assert out.shape == (len(act), *shape)
+    assert np.array_equal(out, np.array(act).reshape(len(act), *shape))
