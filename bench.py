@@ -179,7 +179,7 @@ def run_gb300(args):
     from finitewave_gb300 import _ffi
     _ffi.load()
 
-    mesh, fibers = workload_inputs()
+    mesh, fibers = workload_inputs(args.grid)
     myo = int((mesh == 1).sum())
     chunk, K, W = args.chunk, args.steps, args.warmup
     form32 = args.form
@@ -198,6 +198,8 @@ def run_gb300(args):
 
     # --- float32 form, state resident -------------------------------------
     model, at = build_model(fg, mesh, fibers, "float32", form32)
+    model.fused_k = args.fused_k
+    model.fused_variant = args.fused_variant
     for _ in range(W):
         model._run_segment(chunk, sync=False)
     barrier()
@@ -215,6 +217,16 @@ def run_gb300(args):
     alg_bytes = B_ALG["float32"] * myo * steps_per_launch
     achieved = alg_bytes / per_launch_s / 1e9
     peak, peak_kind = peaks()
+    if args.kernel_only:
+        if rank == 0:
+            print(json.dumps({"kernel_only": True, "grid": args.grid,
+                              "fused_k": args.fused_k,
+                              "fused_variant": args.fused_variant,
+                              "value": value, "ms_per_step": ms_per_step,
+                              "achieved_gbs": achieved,
+                              "frac": achieved / peak,
+                              "launches": int(launches)}), flush=True)
+        return
 
     # --- e2e through the public API, host buffers ----------------------------
     u_h = torch.empty(mesh.shape, dtype=torch.float32).pin_memory()
@@ -382,6 +394,12 @@ def main():
     ap.add_argument("--chunk", type=int, default=100)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--form", default=None, choices=[None, "plain", "fused"])
+    ap.add_argument("--fused-k", type=int, default=0)
+    ap.add_argument("--fused-variant", type=int, default=0)
+    ap.add_argument("--grid", type=int, default=N,
+                    help="grid side (profiling runs use a smaller one)")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="time only the float32 form (profiling)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -78,7 +78,8 @@ class StepArgs(ctypes.Structure):
                 ("stims", Stim * MAX_STIMS), ("at", AtTracker * MAX_AT),
                 ("lat", LatTracker * MAX_LAT),
                 ("probe", ProbeTracker * MAX_PROBE),
-                ("status", _vp), ("fused_k", _i32)]
+                ("status", _vp), ("fused_k", _i32),
+                ("fused_variant", _i32)]
 
 
 class FwError(RuntimeError):

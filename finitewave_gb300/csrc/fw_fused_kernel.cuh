@@ -1,0 +1,638 @@
+// fw_fused_kernel.cuh -- the fused, temporally blocked FP32 form of the 2D
+// step.
+//
+// One CTA owns a tile of TI x TJ grid nodes and advances it up to KMAX time
+// steps per launch.  It stages a (TI + 2 KMAX) x (TJ + 2 KMAX) region once:
+// the off-centre stencil weights and the potential go to shared memory with
+// cp.async (no register staging), the ionic state and the myocyte flags of
+// the nodes a thread owns go to registers.  The sub-steps then run on chip:
+// after sub-step s every node at distance >= s from the region's edge is
+// exact, so after KMAX sub-steps the tile interior is; the halo is computed
+// redundantly by the neighbouring CTAs.  Per launch the tile's weights,
+// state and potential cross HBM once instead of once per time step.
+//
+// Each thread owns a strip of R nodes in one column.  Per sub-step it reads
+// the (R + 2) x 3 window of the current potential into registers first, then
+// updates its R nodes into the other buffer, so no shared load waits behind a
+// shared store.
+//
+// The centre weight is not read: every stencil row sums to one (each major
+// flux moves weight between a neighbour and the centre, each six-point minor
+// flux sums to zero -- asymmetric_stencil_2d.py:204-288 -- and the centre gets
+// +1), so  sum_k w_k u_k = u + sum_{k != c} w_k (u_k - u).
+//
+// Inside each sub-step (global step n), in the reference's order
+// (core/model/cardiac_model.py:164-178): stimuli on u (every node of the
+// region with mesh == 1), trackers on the tile interior (they read u after
+// the stimuli), then diffusion + ionic update into the other buffer.  Which
+// stimuli and trackers act on which sub-step of a launch is decided on the
+// host (bit s of `on`).
+// Requirements (checked by the host): no special boundaries, and u and
+// u_new equal at non-myocytes, so that a non-myocyte's value is the same in
+// both buffers.
+//
+// Arithmetic: float32 with FMA contraction and fast division; compared with
+// the float64 path by tolerance, not bitwise.
+#pragma once
+
+#include <stdio.h>
+#include <string.h>
+
+#include "fw_internal.cuh"
+#include "fw_models.cuh"
+
+namespace fw {
+namespace fused {
+
+constexpr int kMaxFusedStims = 8;
+constexpr int kMaxFusedProbeEntries = 128;
+// trackers evaluated in the fused kernel (more -> the host uses the plain
+// form); kept small so that their state stays in registers
+constexpr int kMaxFusedAt = 2;
+constexpr int kMaxFusedLat = 1;
+
+struct FStim {
+    uint32_t on;  // bit s: applied on sub-step s of this launch
+    int32_t kind, has_umax;
+    float value, u_max;
+    int32_t lo0, hi0, lo1, hi1;
+    const int8_t *mask;
+};
+
+struct FAt {
+    uint32_t on;
+    float thr;
+    int32_t *act;
+};
+
+struct FLat {
+    uint32_t on;
+    float thr;
+    uint8_t *activated;
+    int32_t *steps;
+    int32_t *count;
+    int32_t cap;
+};
+
+struct FProbe {
+    uint32_t on;
+    int64_t sample0;  // sample index of the first active sub-step
+    const int64_t *cells;
+    double *out;
+    int64_t capacity;
+    int32_t n_cells, n_vars;
+    int32_t var_ids[FW_MAX_PROBE_VARS];
+};
+
+struct FusedK {
+    const float *w;
+    const int8_t *myo;
+    const float *u_in;
+    float *u_out;
+    void *state[FW_MAX_STATE];
+    // float32 parameters, rounded on the host: in the kernel they are plain
+    // constant-bank operands (no float64 conversion on the device)
+    float params[FW_MAX_PARAMS];
+    float dt;
+    int32_t ni, nj;
+    int64_t n;
+    int64_t n0;
+    int32_t ksteps;
+    int32_t tiles_j;
+    int32_t n_stims, n_at, n_lat, n_probe;
+    uint32_t stim_on, probe_on;  // OR of the stimuli's / probes' masks
+    FStim stims[kMaxFusedStims];
+    FAt at[kMaxFusedAt];
+    FLat lat[kMaxFusedLat];
+    FProbe probe[FW_MAX_PROBE];
+    int32_t *status;
+};
+
+struct ProbeEntry {
+    int16_t lr, col;
+    int16_t tracker;
+    int32_t cell;
+};
+
+// Off-centre weights held in shared memory, and the index of the centre plane
+// in the global weight array.
+template <int ST>
+struct Stencil2D {
+    static constexpr int NWO = ST == FW_STENCIL_ISO5 ? 4 : 8;
+    static constexpr int CENTRE = ST == FW_STENCIL_ISO5 ? 2 : 4;
+};
+
+// Weights are grouped four per node (float4), so a node's off-centre weights
+// are one (ISO5) or two (ANISO9) 16-byte shared loads.
+template <int LW, int LH, int NWO>
+struct Smem {
+    float4 w[NWO / 4][LH][LW];
+    float u[2][LH][LW];
+    uint32_t probe_bits[(LH * LW + 31) / 32];
+    ProbeEntry probe_list[kMaxFusedProbeEntries];
+    int probe_count;
+};
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem,
+                                          bool valid)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s),
+                 "l"(gmem), "r"(valid ? 4 : 0));
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+}
+
+// Append step n to the crossing list of node p (rare: once per crossing).
+static __device__ __noinline__ void lat_record(const FLat &L, int64_t p,
+                                               int64_t n_nodes, int64_t n,
+                                               int32_t *status)
+{
+    const int32_t c = L.count[p];
+    if (c < L.cap)
+        L.steps[(int64_t)c * n_nodes + p] = (int32_t)n;
+    else if (status)
+        atomicOr(status, FW_DEV_LAT_OVERFLOW);
+    L.count[p] = c + 1;
+}
+
+// Probe trackers at node (lr, col) on sub-step s: u after stimuli (u_c) and
+// the state variables after the update, or, at a non-myocyte, the unchanging
+// stored state (action_potential_2d_tracker.py:46-53, multi_variable_2d_
+// tracker.py:58-69).  Rare path, kept out of line.
+template <class M>
+__device__ __noinline__ void write_probes(
+    const FusedK &k, const ProbeEntry *list, int count, int lr, int col, int s,
+    float u_c, const typename M::template St<float> &st, bool myo, int64_t p)
+{
+    for (int e = 0; e < count && e < kMaxFusedProbeEntries; ++e) {
+        const ProbeEntry pe = list[e];
+        if (pe.lr != lr || pe.col != col) continue;
+        const FProbe &PR = k.probe[pe.tracker];
+        if (!((PR.on >> s) & 1u)) continue;
+        const int64_t smp = PR.sample0 + __popc(PR.on & ((1u << s) - 1u));
+        if (smp >= PR.capacity) {
+            if (k.status) atomicOr(k.status, FW_DEV_PROBE_OVERFLOW);
+            continue;
+        }
+        for (int v = 0; v < PR.n_vars; ++v) {
+            const int id = PR.var_ids[v];
+            double x;
+            if (id == 0)
+                x = (double)u_c;
+            else if (myo)
+                x = M::probe(st, id - 1);
+            else
+                x = (double)((const float *)k.state[id - 1])[p];
+            PR.out[(smp * PR.n_vars + v) * (int64_t)PR.n_cells + pe.cell] = x;
+        }
+    }
+}
+
+template <class M, int ST, int KMAX, int LW, int LH, int R, int MINB>
+__global__ void __launch_bounds__(LW *(LH / R), MINB)
+    k_fused(const __grid_constant__ FusedK k)
+{
+    constexpr int NT = LW * (LH / R);
+    constexpr int TI = LH - 2 * KMAX, TJ = LW - 2 * KMAX;
+    constexpr int NWO = Stencil2D<ST>::NWO;
+    constexpr int CEN = Stencil2D<ST>::CENTRE;
+    static_assert(LH % R == 0 && NT % LW == 0, "strip layout");
+    static_assert(TI > 0 && TJ > 0, "halo larger than the region");
+    static_assert(R <= 8 && KMAX <= 32, "bit masks");
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem<LW, LH, NWO> &S = *reinterpret_cast<Smem<LW, LH, NWO> *>(smem_raw);
+
+    const int tid = threadIdx.x;
+    const int col = tid % LW;
+    const int strip = tid / LW;
+    const int r0 = strip * R;
+    const int tile = blockIdx.x;
+    const int bi = tile / k.tiles_j, bj = tile % k.tiles_j;
+    const int oi = bi * TI - KMAX;   // global row of region row 0
+    const int oj = bj * TJ - KMAX;   // global column of region column 0
+    const int gj = oj + col;
+    const bool col_in = gj >= 0 && gj < k.nj;
+    const bool col_interior = col >= KMAX && col < KMAX + TJ;
+
+    // ---- stage the region ------------------------------------------------------
+    // Thread tid stages column `col` at rows tid / LW + i * (NT / LW):
+    // the potential and the off-centre weight planes, cp.async straight into
+    // shared memory; nodes outside the grid are zero-filled.
+    {
+        constexpr int ROWS = NT / LW, PER = LH / ROWS;
+        const int lr0 = tid / LW;
+        const float *wbase[NWO];
+#pragma unroll
+        for (int q = 0; q < NWO; ++q)
+            wbase[q] = k.w + (int64_t)(q < CEN ? q : q + 1) * k.n;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const int lr = lr0 + i * ROWS;
+            const int gi = oi + lr;
+            const bool in = col_in && gi >= 0 && gi < k.ni;
+            const int64_t p = in ? (int64_t)gi * k.nj + gj : 0;
+            cp_async4(&S.u[0][lr][col], k.u_in + p, in);
+#pragma unroll
+            for (int q = 0; q < NWO; ++q)
+                cp_async4(reinterpret_cast<float *>(&S.w[q >> 2][lr][col]) + (q & 3),
+                          wbase[q] + p, in);
+        }
+    }
+    // state and myocyte flags of the nodes this thread owns
+    typename M::template St<float> st[R];
+    uint32_t myo_bits = 0, own = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int lr = r0 + r, gi = oi + lr;
+        const bool in = col_in && gi >= 0 && gi < k.ni;
+        const int64_t p = in ? (int64_t)gi * k.nj + gj : 0;
+        const int8_t m = k.myo[p];
+        st[r] = M::template load<float>(k.state, p);
+        if (in && m) myo_bits |= 1u << r;
+        if (in && col_interior && lr >= KMAX && lr < KMAX + TI) own |= 1u << r;
+    }
+    if (k.n_probe) {
+        for (int i = tid; i < (LH * LW + 31) / 32; i += NT) S.probe_bits[i] = 0;
+        if (tid == 0) S.probe_count = 0;
+    }
+    // local activation state of owned nodes: bit (l * 8 + r)
+    uint32_t lat_act = 0, at_done = 0;
+#pragma unroll
+    for (int l = 0; l < kMaxFusedLat; ++l)
+        if (l < k.n_lat) {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if ((own >> r) & 1u) {
+                    const int64_t p = (int64_t)(oi + r0 + r) * k.nj + gj;
+                    if (k.lat[l].activated[p]) lat_act |= 1u << (l * 8 + r);
+                }
+        }
+    cp_async_wait_all();
+    __syncthreads();
+    // (buffer 1 needs no copy: every sub-step writes every node of the other
+    // buffer, non-myocytes with their unchanged value)
+
+    // ---- probe cells inside this tile's interior ------------------------------------
+    uint32_t probe_mine = 0;
+    if (k.n_probe) {
+        for (int t = 0; t < k.n_probe; ++t) {
+            const FProbe &pr = k.probe[t];
+            for (int c = tid; c < pr.n_cells; c += NT) {
+                const int64_t p = pr.cells[c];
+                const int gi = (int)(p / k.nj), gjj = (int)(p % k.nj);
+                const int lr = gi - oi, lc = gjj - oj;
+                if (lr >= KMAX && lr < KMAX + TI && lc >= KMAX &&
+                    lc < KMAX + TJ) {
+                    const int e = atomicAdd(&S.probe_count, 1);
+                    if (e < kMaxFusedProbeEntries) {
+                        S.probe_list[e] = ProbeEntry{(int16_t)lr, (int16_t)lc,
+                                                     (int16_t)t, c};
+                        const int bit = lr * LW + lc;
+                        atomicOr(&S.probe_bits[bit >> 5], 1u << (bit & 31));
+                    } else if (k.status) {
+                        atomicOr(k.status, FW_DEV_PROBE_OVERFLOW);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int bit = (r0 + r) * LW + col;
+            if ((S.probe_bits[bit >> 5] >> (bit & 31)) & 1u)
+                probe_mine |= 1u << r;
+        }
+    }
+
+    Params<float, M::NP> P;
+#pragma unroll
+    for (int i = 0; i < M::NP; ++i) P.v[i] = k.params[i];
+    const float dt = k.dt;
+    const int cm = col > 0 ? col - 1 : 0;
+    const int cp = col < LW - 1 ? col + 1 : LW - 1;
+    // rows whose update is defined (the region's outer ring is never read)
+    uint32_t upd = 0;
+    if (col > 0 && col < LW - 1) {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (r0 + r > 0 && r0 + r < LH - 1) upd |= 1u << r;
+    }
+    upd &= myo_bits;
+
+    // ---- sub-steps ----------------------------------------------------------------
+    for (int s = 0; s < k.ksteps; ++s) {
+        const int64_t n = k.n0 + s;
+        const int cb = s & 1;
+        float(*cur)[LW] = S.u[cb];
+        float(*nxt)[LW] = S.u[cb ^ 1];
+
+        // stimuli (stim_sequence.py:65-77) on every node of the region
+        if ((k.stim_on >> s) & 1u) {
+            for (int i = 0; i < k.n_stims; ++i) {
+                const FStim &F = k.stims[i];
+                if (!((F.on >> s) & 1u)) continue;
+                if (gj < F.lo1 || gj >= F.hi1) continue;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if (!((myo_bits >> r) & 1u)) continue;
+                    const int lr = r0 + r, gi = oi + lr;
+                    if (gi < F.lo0 || gi >= F.hi0) continue;
+                    if (F.mask && !F.mask[(int64_t)gi * k.nj + gj]) continue;
+                    float x = cur[lr][col];
+                    if (F.kind == FW_STIM_VOLTAGE) {
+                        x = F.value;
+                    } else {
+                        x = x + F.value;
+                        if (F.has_umax && x > F.u_max) x = F.u_max;
+                    }
+                    cur[lr][col] = x;
+                }
+            }
+            __syncthreads();
+        }
+
+        // the (R + 2) x 3 window of u: rows r0 - 1 .. r0 + R (clamped)
+        float wl[R + 2], wc[R + 2], wr[R + 2];
+#pragma unroll
+        for (int i = 0; i < R + 2; ++i) {
+            int lr = r0 - 1 + i;
+            lr = lr < 0 ? 0 : (lr > LH - 1 ? LH - 1 : lr);
+            wl[i] = cur[lr][cm];
+            wc[i] = cur[lr][col];
+            wr[i] = cur[lr][cp];
+        }
+
+        // trackers on the owned interior nodes (tracker.py:70-83)
+        if (own) {
+#pragma unroll
+            for (int a = 0; a < kMaxFusedAt; ++a) {
+                if (a >= k.n_at || !((k.at[a].on >> s) & 1u)) continue;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const uint32_t bit = 1u << (a * 8 + r);
+                    if (!((own >> r) & 1u) || (at_done & bit)) continue;
+                    if (wc[r + 1] > k.at[a].thr) {
+                        // (act_t < 0) & (u > threshold)
+                        // (activation_time_2d_tracker.py:61-63)
+                        const int64_t p = (int64_t)(oi + r0 + r) * k.nj + gj;
+                        if (k.at[a].act[p] < 0) k.at[a].act[p] = (int32_t)n;
+                        at_done |= bit;
+                    }
+                }
+            }
+#pragma unroll
+            for (int l = 0; l < kMaxFusedLat; ++l) {
+                if (l >= k.n_lat || !((k.lat[l].on >> s) & 1u)) continue;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if (!((own >> r) & 1u)) continue;
+                    const uint32_t bit = 1u << (l * 8 + r);
+                    const bool was = (lat_act & bit) != 0;
+                    const float x = wc[r + 1];
+                    if (x >= k.lat[l].thr && !was) {
+                        // cross_threshold (local_activation_time_2d_tracker
+                        // .py:71-89)
+                        lat_act |= bit;
+                        lat_record(k.lat[l], (int64_t)(oi + r0 + r) * k.nj + gj,
+                                   k.n, n, k.status);
+                    } else if (x < k.lat[l].thr && was) {
+                        lat_act &= ~bit;
+                    }
+                }
+            }
+        }
+
+        // diffusion + ionic update of the strip into the other buffer
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float b1 = wc[r + 1];
+            float un = b1;
+            if ((upd >> r) & 1u) {
+                const int lr = r0 + r;
+                float d;
+                const float4 wa = S.w[0][lr][col];
+                if constexpr (ST == FW_STENCIL_ISO5) {
+                    d = wa.x * (wc[r] - b1) + wa.y * (wl[r + 1] - b1) +
+                        wa.z * (wr[r + 1] - b1) + wa.w * (wc[r + 2] - b1);
+                } else {
+                    const float4 wb = S.w[1][lr][col];
+                    d = wa.x * (wl[r] - b1) + wa.y * (wc[r] - b1) +
+                        wa.z * (wr[r] - b1) + wa.w * (wl[r + 1] - b1) +
+                        wb.x * (wr[r + 1] - b1) + wb.y * (wl[r + 2] - b1) +
+                        wb.z * (wc[r + 2] - b1) + wb.w * (wr[r + 2] - b1);
+                }
+                un = M::template update<float>(b1, b1 + d, st[r], P, dt);
+            }
+            if (((probe_mine >> r) & 1u) && ((k.probe_on >> s) & 1u))
+                write_probes<M>(k, S.probe_list, S.probe_count, r0 + r, col, s,
+                                b1, st[r], ((myo_bits >> r) & 1u) != 0,
+                                (int64_t)(oi + r0 + r) * k.nj + gj);
+            nxt[r0 + r][col] = un;
+        }
+        __syncthreads();
+    }
+
+    // ---- write the interior back --------------------------------------------------
+    const int fb = k.ksteps & 1;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (!((own >> r) & 1u)) continue;
+        const int lr = r0 + r;
+        const int64_t p = (int64_t)(oi + lr) * k.nj + gj;
+        if ((myo_bits >> r) & 1u) {
+            k.u_out[p] = S.u[fb][lr][col];
+            M::template store<float>(k.state, p, st[r]);
+        }
+#pragma unroll
+        for (int l = 0; l < kMaxFusedLat; ++l)
+            if (l < k.n_lat)
+                k.lat[l].activated[p] = (lat_act >> (l * 8 + r)) & 1u;
+    }
+}
+
+// ---------------------------------------------------------------- host side
+
+// Bit s set when step n0 + s (s < ks) is in [first, last] and a multiple of
+// stride.
+inline uint32_t sub_step_mask(int64_t n0, int64_t ks, int64_t first,
+                              int64_t last, int64_t stride)
+{
+    uint32_t m = 0;
+    for (int64_t s = 0; s < ks; ++s) {
+        const int64_t n = n0 + s;
+        if (n >= first && n <= last && n % stride == 0) m |= 1u << s;
+    }
+    return m;
+}
+
+template <class M, int ST, int KMAX, int LW, int LH, int R, int MINB>
+int launch_fused(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                 cudaStream_t stream)
+{
+    constexpr int TI = LH - 2 * KMAX, TJ = LW - 2 * KMAX;
+    constexpr int NT = LW * (LH / R);
+    constexpr size_t SMEM = sizeof(Smem<LW, LH, Stencil2D<ST>::NWO>);
+    auto kern = k_fused<M, ST, KMAX, LW, LH, R, MINB>;
+    // per call (cheap), so that it holds on whichever device is current
+    FW_CUDA_CHECK(cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM));
+    if (a->n_lat > kMaxFusedLat) {
+        set_error("fw_step (fused): at most %d local activation tracker",
+                  kMaxFusedLat);
+        return FW_ERR_UNSUPPORTED;
+    }
+    FusedK k;
+    memset(&k, 0, sizeof k);
+    k.w = (const float *)a->weights;
+    k.myo = a->myo;
+    for (int i = 0; i < FW_MAX_STATE; ++i) k.state[i] = a->state[i];
+    for (int i = 0; i < FW_MAX_PARAMS; ++i) k.params[i] = (float)a->params[i];
+    k.dt = (float)a->dt;
+    k.ni = (int32_t)a->ni;
+    k.nj = (int32_t)a->nj;
+    k.n = a->ni * a->nj;
+    k.status = a->status;
+    const int tiles_i = (int)((a->ni + TI - 1) / TI);
+    k.tiles_j = (int)((a->nj + TJ - 1) / TJ);
+    const int64_t blocks = (int64_t)tiles_i * k.tiles_j;
+    int64_t probe_samples[FW_MAX_PROBE];
+    for (int i = 0; i < a->n_probe; ++i) probe_samples[i] = a->probe[i].sample_offset;
+
+    // launch sizes: L launches of <= KMAX steps with L == n_steps (mod 2), so
+    // that the result ends in u[n_steps & 1] as in the plain form.
+    int64_t L = (n_steps + KMAX - 1) / KMAX;
+    if ((L & 1) != (n_steps & 1)) ++L;
+    int64_t done = 0;
+    for (int64_t li = 0; li < L; ++li) {
+        const int64_t left = n_steps - done, launches_left = L - li;
+        int64_t ks = (left + launches_left - 1) / launches_left;
+        if (ks > KMAX) ks = KMAX;
+        const int64_t n0 = n_begin + done;
+        const int64_t n1 = n0 + ks - 1;
+        k.n0 = n0;
+        k.ksteps = (int32_t)ks;
+        k.u_in = (const float *)a->u[li & 1];
+        k.u_out = (float *)a->u[(li + 1) & 1];
+        k.n_stims = 0;
+        k.stim_on = 0;
+        for (int i = 0; i < a->n_stims; ++i) {
+            const fw_stim &St = a->stims[i];
+            if (St.last < n0 || St.first > n1) continue;
+            if (k.n_stims >= kMaxFusedStims) {
+                set_error("fw_step (fused): more than %d stimuli active in one "
+                          "launch", kMaxFusedStims);
+                return FW_ERR_UNSUPPORTED;
+            }
+            FStim &f = k.stims[k.n_stims++];
+            f.on = sub_step_mask(n0, ks, St.first, St.last, 1);
+            f.kind = St.kind;
+            f.has_umax = St.has_umax;
+            f.value = (float)St.value;
+            f.u_max = (float)St.u_max;
+            f.lo0 = (int32_t)(St.lo[0] < 0 ? 0 : St.lo[0]);
+            f.hi0 = (int32_t)(St.hi[0] > a->ni ? a->ni : St.hi[0]);
+            f.lo1 = (int32_t)(St.lo[1] < 0 ? 0 : St.lo[1]);
+            f.hi1 = (int32_t)(St.hi[1] > a->nj ? a->nj : St.hi[1]);
+            f.mask = St.mask;
+            k.stim_on |= f.on;
+        }
+        k.n_at = 0;
+        for (int i = 0; i < a->n_at; ++i) {
+            const fw_at_tracker &A = a->at[i];
+            const uint32_t on = sub_step_mask(n0, ks, A.win.first, A.win.last,
+                                              A.win.stride);
+            if (!on) continue;
+            if (k.n_at >= kMaxFusedAt) {
+                set_error("fw_step (fused): more than %d activation trackers "
+                          "active in one launch", kMaxFusedAt);
+                return FW_ERR_UNSUPPORTED;
+            }
+            k.at[k.n_at++] = FAt{on, (float)A.threshold, A.act_step};
+        }
+        k.n_lat = 0;
+        for (int i = 0; i < a->n_lat; ++i) {
+            const fw_lat_tracker &Lt = a->lat[i];
+            k.lat[k.n_lat++] = FLat{sub_step_mask(n0, ks, Lt.win.first,
+                                                  Lt.win.last, Lt.win.stride),
+                                    (float)Lt.threshold, Lt.activated,
+                                    Lt.cross_steps, Lt.cross_count,
+                                    Lt.capacity};
+        }
+        k.n_probe = 0;
+        k.probe_on = 0;
+        for (int i = 0; i < a->n_probe; ++i) {
+            const fw_probe_tracker &Pp = a->probe[i];
+            const uint32_t on = sub_step_mask(n0, ks, Pp.win.first, Pp.win.last,
+                                              Pp.win.stride);
+            if (!on) continue;
+            FProbe &f = k.probe[k.n_probe++];
+            f.on = on;
+            f.sample0 = probe_samples[i];
+            probe_samples[i] += __builtin_popcount(on);
+            f.cells = Pp.cells;
+            f.out = Pp.out;
+            f.capacity = Pp.capacity;
+            f.n_cells = Pp.n_cells;
+            f.n_vars = Pp.n_vars;
+            for (int v = 0; v < FW_MAX_PROBE_VARS; ++v)
+                f.var_ids[v] = Pp.var_ids[v];
+            k.probe_on |= on;
+        }
+        kern<<<(unsigned)blocks, NT, SMEM, stream>>>(k);
+        FW_CHECK_LAUNCH("k_fused");
+        done += ks;
+    }
+    return FW_OK;
+}
+
+// Region shapes of the fused kernel (64 columns = two warps wide), 8-node
+// column strips:
+//   variant 0: 64 x 32 nodes, 256 threads, two CTAs per SM (~82 KB shared
+//              memory each: one stages while the other computes);
+//   variant 1: 64 x 64 nodes, 512 threads, one CTA per SM (less halo).
+// KMAX in {2, 4, 8} time steps per launch.
+template <class M, int ST>
+int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                   cudaStream_t stream)
+{
+    const int k = a->fused_k ? a->fused_k : 4;
+    const int v = a->fused_variant;
+#define FW_FUSED_CASE(KK, LH, MINB)                                            \
+    return launch_fused<M, ST, KK, 64, LH, 8, MINB>(a, n_begin, n_steps, stream)
+    if (v == 0) {
+        if (k == 2) FW_FUSED_CASE(2, 32, 2);
+        if (k == 4) FW_FUSED_CASE(4, 32, 2);
+        if (k == 8) FW_FUSED_CASE(8, 32, 2);
+    } else if (v == 1) {
+        if (k == 2) FW_FUSED_CASE(2, 64, 1);
+        if (k == 4) FW_FUSED_CASE(4, 64, 1);
+        if (k == 8) FW_FUSED_CASE(8, 64, 1);
+    }
+#undef FW_FUSED_CASE
+    set_error("fw_step (fused): no kernel for fused_k=%d fused_variant=%d "
+              "(k in 2, 4, 8; variant in 0, 1)", k, v);
+    return FW_ERR_UNSUPPORTED;
+}
+
+template <class M>
+int fused_model(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                cudaStream_t stream)
+{
+    switch (a->stencil) {
+    case FW_STENCIL_ISO5:
+        return fused_dispatch<M, FW_STENCIL_ISO5>(a, n_begin, n_steps, stream);
+    case FW_STENCIL_ANISO9:
+        return fused_dispatch<M, FW_STENCIL_ANISO9>(a, n_begin, n_steps, stream);
+    }
+    set_error("fw_step (fused): 2D stencils only");
+    return FW_ERR_UNSUPPORTED;
+}
+
+}  // namespace fused
+}  // namespace fw

@@ -133,5 +133,11 @@ int step_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                cudaStream_t stream);
 int step_fused(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                cudaStream_t stream);
+int step_fused_ap(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                  cudaStream_t stream);
+int step_fused_ms(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                  cudaStream_t stream);
+int step_fused_fk(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                  cudaStream_t stream);
 
 }  // namespace fw

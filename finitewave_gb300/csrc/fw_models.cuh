@@ -27,6 +27,17 @@ struct Params {
     T v[N];
 };
 
+// Precision-matched transcendental calls (float -> the float functions, so
+// that no float64 arithmetic sneaks into the float32 kernels).
+__device__ __forceinline__ float fw_tanh(float x) { return tanhf(x); }
+__device__ __forceinline__ double fw_tanh(double x) { return tanh(x); }
+__device__ __forceinline__ float fw_exp(float x) { return expf(x); }
+__device__ __forceinline__ double fw_exp(double x) { return exp(x); }
+__device__ __forceinline__ float fw_log(float x) { return logf(x); }
+__device__ __forceinline__ double fw_log(double x) { return log(x); }
+__device__ __forceinline__ float fw_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double fw_sqrt(double x) { return sqrt(x); }
+
 template <class T, int N>
 __device__ __forceinline__ Params<T, N> load_params(const double *p)
 {
@@ -55,6 +66,11 @@ struct ModelAP {
                                                  const St<T> &x)
     {
         ((T *)s[0])[p] = x.v;
+    }
+    template <class T>
+    __device__ static __forceinline__ double probe(const St<T> &x, int)
+    {
+        return (double)x.v;
     }
     template <class T>
     __device__ static __forceinline__ T update(T u, T un, St<T> &x,
@@ -89,6 +105,11 @@ struct ModelMS {
                                                  const St<T> &x)
     {
         ((T *)s[0])[p] = x.h;
+    }
+    template <class T>
+    __device__ static __forceinline__ double probe(const St<T> &x, int)
+    {
+        return (double)x.h;
     }
     template <class T>
     __device__ static __forceinline__ T update(T u, T un, St<T> &x,
@@ -130,6 +151,11 @@ struct ModelFK {
         ((T *)s[1])[p] = x.w;
     }
     template <class T>
+    __device__ static __forceinline__ double probe(const St<T> &x, int i)
+    {
+        return i == 0 ? (double)x.v : (double)x.w;
+    }
+    template <class T>
     __device__ static __forceinline__ T update(T u, T un, St<T> &x,
                                                const Params<T, NP> &P, T dt)
     {
@@ -146,7 +172,7 @@ struct ModelFK {
         x.w = w;
         T J_fi = -(v * H2 * (one - u) * (u - u_c)) / tau_d;
         T J_so = u * H1 / tau_o + H2 / tau_r;
-        T J_si = (-v) * (one + tanh(k * (u - uc_si))) / ((T)2 * tau_si);
+        T J_si = (-v) * (one + fw_tanh(k * (u - uc_si))) / ((T)2 * tau_si);
         return un + dt * (-J_fi - J_so - J_si);
     }
 };

@@ -60,6 +60,7 @@ class _StateVar:
                 raise ValueError(f"{self.name}: shape {value.shape} != "
                                  f"{tuple(t.shape)}")
             t.copy_(torch.as_tensor(np.ascontiguousarray(value)).to(t.dtype))
+            obj.__dict__["_nonmyo_equal"] = None
             return
         obj.__dict__.setdefault("_host", {})[self.name] = value
 
@@ -114,6 +115,7 @@ class CardiacModel:
         self.device = None
         self.form = None
         self.fused_k = 0
+        self.fused_variant = 0
         self._dev = {}
         self._t_hist = []
 
@@ -268,6 +270,7 @@ class CardiacModel:
             raise ValueError("t_max must be greater than current t.")
         if self.state_loader:
             self.state_loader.load()
+        self._nonmyo_equal = None
         iters = int(np.ceil((self.t_max - self.t) / self.dt))
         remaining = iters
         while remaining > 0:
@@ -313,11 +316,36 @@ class CardiacModel:
         n_seg = int(np.argmax(stop)) + 1 if stop.any() else limit
         return ts_all[:n_seg], float(ts_all[n_seg]), n_seg
 
+    _FUSED_MODELS = (_ffi.MODEL_AP, _ffi.MODEL_MS, _ffi.MODEL_FK)
+
+    def _fused_ok(self):
+        """The fused form covers 2D float32 AP/MS/FK without special
+        boundaries, with u and u_new equal at non-myocytes."""
+        if (self._precision() != _ffi.F32 or self._special or
+                self._model_id not in self._FUSED_MODELS or
+                self.stencil.kind not in (_ffi.ISO5, _ffi.ANISO9)):
+            return False
+        trs = self.tracker_sequence.sequence if self.tracker_sequence else []
+        if (sum(isinstance(t, ActivationTime2DTracker) for t in trs) > 2 or
+                sum(isinstance(t, LocalActivationTime2DTracker)
+                    for t in trs) > 1):
+            return False
+        if getattr(self, "_nonmyo_equal", None) is None:
+            off = self._myo_d == 0
+            self._nonmyo_equal = bool(torch.equal(self._dev["u"][off],
+                                                  self._dev["u_new"][off]))
+        return self._nonmyo_equal
+
     def _form(self):
-        if self.form is not None:
-            return _ffi.FORM_FUSED if self.form == "fused" else \
-                _ffi.FORM_PLAIN
-        return _ffi.FORM_PLAIN
+        if self.form == "plain":
+            return _ffi.FORM_PLAIN
+        if self.form == "fused":
+            if not self._fused_ok():
+                raise ValueError("form='fused' needs a 2D float32 Aliev-"
+                                 "Panfilov / Mitchell-Schaeffer / Fenton-"
+                                 "Karma model without special boundaries")
+            return _ffi.FORM_FUSED
+        return _ffi.FORM_FUSED if self._fused_ok() else _ffi.FORM_PLAIN
 
     def _check_status(self):
         st = int(self._status.item())
@@ -352,9 +380,8 @@ class CardiacModel:
             a.params[i] = p
         a.dt = float(self.dt)
         a.fused_k = int(self.fused_k)
+        a.fused_variant = int(self.fused_variant)
         a.form = self._form()
-        if a.form == _ffi.FORM_FUSED and self._special:
-            a.form = _ffi.FORM_PLAIN
         keep = []
 
         # stimuli (stim_sequence.py:65-77)

@@ -182,7 +182,10 @@ typedef struct fw_step_args {
     fw_lat_tracker lat[FW_MAX_LAT];
     fw_probe_tracker probe[FW_MAX_PROBE];
     int32_t *status;  /* device int32 status word (may be NULL)             */
-    int32_t fused_k;  /* FW_FORM_FUSED time steps per launch (0 = default)  */
+    int32_t fused_k;  /* FW_FORM_FUSED time steps per launch: 2, 4 or 8
+                         (0 = 4)                                            */
+    int32_t fused_variant; /* FW_FORM_FUSED region shape: 0 = 64x64 nodes,
+                              512 threads; 1 = 64x32 nodes, 256 threads     */
 } fw_step_args;
 
 /* Library version (major*10000 + minor*100 + patch). */

@@ -13,7 +13,7 @@ def register(name, cls2d, cls3d):
     _MODELS[(name, 3)] = cls3d
 
 
-def build(case, npfloat="float64", form=None, fused_k=0):
+def build(case, npfloat="float64", form=None, fused_k=0, fused_variant=0):
     mesh = np.asarray(case["mesh"])
     dim = mesh.ndim
     tissue = fg.CardiacTissue2D(mesh.shape) if dim == 2 \
@@ -28,6 +28,7 @@ def build(case, npfloat="float64", form=None, fused_k=0):
     model.npfloat = npfloat
     model.form = form
     model.fused_k = fused_k
+    model.fused_variant = fused_variant
     for k, v in case.get("params", {}).items():
         setattr(model, k, v)
     if "D_model" in case:
