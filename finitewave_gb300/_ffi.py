@@ -79,7 +79,7 @@ class StepArgs(ctypes.Structure):
                 ("lat", LatTracker * MAX_LAT),
                 ("probe", ProbeTracker * MAX_PROBE),
                 ("status", _vp), ("fused_k", _i32),
-                ("fused_variant", _i32)]
+                ("fused_variant", _i32), ("weights_packed", _vp)]
 
 
 class FwError(RuntimeError):
@@ -108,6 +108,7 @@ _SIGS = {
     "fw_ionic": ([_i32, _i32, _vp, _vp, _vp, _vp, _i64, _f64, _vp, _vp],
                  _i32),
     "fw_step": ([ctypes.POINTER(StepArgs), _i64, _i64, _vp], _i32),
+    "fw_pack_weights": ([_i32, _vp, _i64, _vp, _vp], _i32),
 }
 
 # symbol -> ctypes structure whose size must match the library's

@@ -225,6 +225,12 @@ int fw_ionic(int32_t model, int32_t precision, void *u_new, const void *u,
                      (cudaStream_t)stream);
 }
 
+int fw_pack_weights(int32_t stencil, const float *w, int64_t n, float *out,
+                    void *stream)
+{
+    return fw::pack_weights(stencil, w, n, out, (cudaStream_t)stream);
+}
+
 int fw_step(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
             void *stream)
 {

@@ -127,7 +127,9 @@ struct Stencil2D {
 template <int LW, int LH, int NWO>
 struct Smem {
     float4 w[NWO / 4][LH][LW];
-    float u[2][LH][LW];
+    // potential, ping-pong, with a one-node pad on every side so that the
+    // 3x3 window of any region node needs no index clamping
+    float u[2][LH + 2][LW + 2];
     uint32_t probe_bits[(LH * LW + 31) / 32];
     ProbeEntry probe_list[kMaxFusedProbeEntries];
     int probe_count;
@@ -167,7 +169,7 @@ static __device__ __noinline__ void lat_record(const FLat &L, int64_t p,
 template <class M>
 __device__ __noinline__ void write_probes(
     const FusedK &k, const ProbeEntry *list, int count, int lr, int col, int s,
-    float u_c, const typename M::template St<float> &st, bool myo, int64_t p)
+    float u_c, const typename M::template St<float> st, bool myo, int64_t p)
 {
     for (int e = 0; e < count && e < kMaxFusedProbeEntries; ++e) {
         const ProbeEntry pe = list[e];
@@ -237,7 +239,7 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
             const int gi = oi + lr;
             const bool in = col_in && gi >= 0 && gi < k.ni;
             const int64_t p = in ? (int64_t)gi * k.nj + gj : 0;
-            cp_async4(&S.u[0][lr][col], k.u_in + p, in);
+            cp_async4(&S.u[0][lr + 1][col + 1], k.u_in + p, in);
 #pragma unroll
             for (int q = 0; q < NWO; ++q)
                 cp_async4(reinterpret_cast<float *>(&S.w[q >> 2][lr][col]) + (q & 3),
@@ -260,6 +262,17 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
     if (k.n_probe) {
         for (int i = tid; i < (LH * LW + 31) / 32; i += NT) S.probe_bits[i] = 0;
         if (tid == 0) S.probe_count = 0;
+    }
+    // zero the pad ring of both potential buffers (read, never used)
+    for (int i = tid; i < 2 * (LW + 2); i += NT) {
+        const int b = i / (LW + 2), c = i % (LW + 2);
+        S.u[b][0][c] = 0.f;
+        S.u[b][LH + 1][c] = 0.f;
+    }
+    for (int i = tid; i < 2 * LH; i += NT) {
+        const int b = i / LH, rr = i % LH + 1;
+        S.u[b][rr][0] = 0.f;
+        S.u[b][rr][LW + 1] = 0.f;
     }
     // local activation state of owned nodes: bit (l * 8 + r)
     uint32_t lat_act = 0, at_done = 0;
@@ -314,8 +327,6 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
 #pragma unroll
     for (int i = 0; i < M::NP; ++i) P.v[i] = k.params[i];
     const float dt = k.dt;
-    const int cm = col > 0 ? col - 1 : 0;
-    const int cp = col < LW - 1 ? col + 1 : LW - 1;
     // rows whose update is defined (the region's outer ring is never read)
     uint32_t upd = 0;
     if (col > 0 && col < LW - 1) {
@@ -329,8 +340,9 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
     for (int s = 0; s < k.ksteps; ++s) {
         const int64_t n = k.n0 + s;
         const int cb = s & 1;
-        float(*cur)[LW] = S.u[cb];
-        float(*nxt)[LW] = S.u[cb ^ 1];
+        // padded buffers: region node (lr, c) lives at [lr + 1][c + 1]
+        float(*cur)[LW + 2] = S.u[cb];
+        float(*nxt)[LW + 2] = S.u[cb ^ 1];
 
         // stimuli (stim_sequence.py:65-77) on every node of the region
         if ((k.stim_on >> s) & 1u) {
@@ -344,28 +356,26 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
                     const int lr = r0 + r, gi = oi + lr;
                     if (gi < F.lo0 || gi >= F.hi0) continue;
                     if (F.mask && !F.mask[(int64_t)gi * k.nj + gj]) continue;
-                    float x = cur[lr][col];
+                    float x = cur[lr + 1][col + 1];
                     if (F.kind == FW_STIM_VOLTAGE) {
                         x = F.value;
                     } else {
                         x = x + F.value;
                         if (F.has_umax && x > F.u_max) x = F.u_max;
                     }
-                    cur[lr][col] = x;
+                    cur[lr + 1][col + 1] = x;
                 }
             }
             __syncthreads();
         }
 
-        // the (R + 2) x 3 window of u: rows r0 - 1 .. r0 + R (clamped)
+        // the (R + 2) x 3 window of u: region rows r0 - 1 .. r0 + R
         float wl[R + 2], wc[R + 2], wr[R + 2];
 #pragma unroll
         for (int i = 0; i < R + 2; ++i) {
-            int lr = r0 - 1 + i;
-            lr = lr < 0 ? 0 : (lr > LH - 1 ? LH - 1 : lr);
-            wl[i] = cur[lr][cm];
-            wc[i] = cur[lr][col];
-            wr[i] = cur[lr][cp];
+            wl[i] = cur[r0 + i][col];
+            wc[i] = cur[r0 + i][col + 1];
+            wr[i] = cur[r0 + i][col + 2];
         }
 
         // trackers on the owned interior nodes (tracker.py:70-83)
@@ -379,9 +389,13 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
                     if (!((own >> r) & 1u) || (at_done & bit)) continue;
                     if (wc[r + 1] > k.at[a].thr) {
                         // (act_t < 0) & (u > threshold)
-                        // (activation_time_2d_tracker.py:61-63)
+                        // (activation_time_2d_tracker.py:61-63): the first
+                        // crossing has the smallest step and "never" (-1) is
+                        // the largest unsigned value, so an unsigned atomic
+                        // minimum keeps the first step without reading it
                         const int64_t p = (int64_t)(oi + r0 + r) * k.nj + gj;
-                        if (k.at[a].act[p] < 0) k.at[a].act[p] = (int32_t)n;
+                        atomicMin(reinterpret_cast<unsigned *>(k.at[a].act) + p,
+                                  (unsigned)n);
                         at_done |= bit;
                     }
                 }
@@ -408,32 +422,33 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
             }
         }
 
-        // diffusion + ionic update of the strip into the other buffer
+        // diffusion + ionic update of the strip into the other buffer.  The
+        // update is computed for every node and kept only where it is defined
+        // (myocytes off the region's ring); the state of the other nodes is
+        // never written back.
+        const bool probes_now = probe_mine && ((k.probe_on >> s) & 1u);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const float b1 = wc[r + 1];
-            float un = b1;
-            if ((upd >> r) & 1u) {
-                const int lr = r0 + r;
-                float d;
-                const float4 wa = S.w[0][lr][col];
-                if constexpr (ST == FW_STENCIL_ISO5) {
-                    d = wa.x * (wc[r] - b1) + wa.y * (wl[r + 1] - b1) +
-                        wa.z * (wr[r + 1] - b1) + wa.w * (wc[r + 2] - b1);
-                } else {
-                    const float4 wb = S.w[1][lr][col];
-                    d = wa.x * (wl[r] - b1) + wa.y * (wc[r] - b1) +
-                        wa.z * (wr[r] - b1) + wa.w * (wl[r + 1] - b1) +
-                        wb.x * (wr[r + 1] - b1) + wb.y * (wl[r + 2] - b1) +
-                        wb.z * (wc[r + 2] - b1) + wb.w * (wr[r + 2] - b1);
-                }
-                un = M::template update<float>(b1, b1 + d, st[r], P, dt);
+            const int lr = r0 + r;
+            float d;
+            const float4 wa = S.w[0][lr][col];
+            if constexpr (ST == FW_STENCIL_ISO5) {
+                d = wa.x * (wc[r] - b1) + wa.y * (wl[r + 1] - b1) +
+                    wa.z * (wr[r + 1] - b1) + wa.w * (wc[r + 2] - b1);
+            } else {
+                const float4 wb = S.w[1][lr][col];
+                d = wa.x * (wl[r] - b1) + wa.y * (wc[r] - b1) +
+                    wa.z * (wr[r] - b1) + wa.w * (wl[r + 1] - b1) +
+                    wb.x * (wr[r + 1] - b1) + wb.y * (wl[r + 2] - b1) +
+                    wb.z * (wc[r + 2] - b1) + wb.w * (wr[r + 2] - b1);
             }
-            if (((probe_mine >> r) & 1u) && ((k.probe_on >> s) & 1u))
-                write_probes<M>(k, S.probe_list, S.probe_count, r0 + r, col, s,
-                                b1, st[r], ((myo_bits >> r) & 1u) != 0,
-                                (int64_t)(oi + r0 + r) * k.nj + gj);
-            nxt[r0 + r][col] = un;
+            const float uu = M::template update<float>(b1, b1 + d, st[r], P, dt);
+            nxt[lr + 1][col + 1] = ((upd >> r) & 1u) ? uu : b1;
+            if (probes_now && ((probe_mine >> r) & 1u))
+                write_probes<M>(k, S.probe_list, S.probe_count, lr, col, s, b1,
+                                st[r], ((myo_bits >> r) & 1u) != 0,
+                                (int64_t)(oi + lr) * k.nj + gj);
         }
         __syncthreads();
     }
@@ -446,7 +461,7 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
         const int lr = r0 + r;
         const int64_t p = (int64_t)(oi + lr) * k.nj + gj;
         if ((myo_bits >> r) & 1u) {
-            k.u_out[p] = S.u[fb][lr][col];
+            k.u_out[p] = S.u[fb][lr + 1][col + 1];
             M::template store<float>(k.state, p, st[r]);
         }
 #pragma unroll
@@ -469,6 +484,79 @@ inline uint32_t sub_step_mask(int64_t n0, int64_t ks, int64_t first,
         if (n >= first && n <= last && n % stride == 0) m |= 1u << s;
     }
     return m;
+}
+
+// Stimuli and trackers acting during the launch of steps n0..n1 (ks steps):
+// per sub-step activity masks, computed on the host.
+inline int fill_events(const fw_step_args *a, FusedK &k, int64_t n0, int64_t n1,
+                       int64_t ks, int64_t *probe_samples)
+{
+    k.n_stims = 0;
+    k.stim_on = 0;
+    for (int i = 0; i < a->n_stims; ++i) {
+        const fw_stim &St = a->stims[i];
+        if (St.last < n0 || St.first > n1) continue;
+        if (k.n_stims >= kMaxFusedStims) {
+            set_error("fw_step (fused): more than %d stimuli active in one "
+                      "launch", kMaxFusedStims);
+            return FW_ERR_UNSUPPORTED;
+        }
+        FStim &f = k.stims[k.n_stims++];
+        f.on = sub_step_mask(n0, ks, St.first, St.last, 1);
+        f.kind = St.kind;
+        f.has_umax = St.has_umax;
+        f.value = (float)St.value;
+        f.u_max = (float)St.u_max;
+        f.lo0 = (int32_t)(St.lo[0] < 0 ? 0 : St.lo[0]);
+        f.hi0 = (int32_t)(St.hi[0] > a->ni ? a->ni : St.hi[0]);
+        f.lo1 = (int32_t)(St.lo[1] < 0 ? 0 : St.lo[1]);
+        f.hi1 = (int32_t)(St.hi[1] > a->nj ? a->nj : St.hi[1]);
+        f.mask = St.mask;
+        k.stim_on |= f.on;
+    }
+    k.n_at = 0;
+    for (int i = 0; i < a->n_at; ++i) {
+        const fw_at_tracker &A = a->at[i];
+        const uint32_t on = sub_step_mask(n0, ks, A.win.first, A.win.last,
+                                          A.win.stride);
+        if (!on) continue;
+        if (k.n_at >= kMaxFusedAt) {
+            set_error("fw_step (fused): more than %d activation trackers "
+                      "active in one launch", kMaxFusedAt);
+            return FW_ERR_UNSUPPORTED;
+        }
+        k.at[k.n_at++] = FAt{on, (float)A.threshold, A.act_step};
+    }
+    k.n_lat = 0;
+    for (int i = 0; i < a->n_lat; ++i) {
+        const fw_lat_tracker &Lt = a->lat[i];
+        k.lat[k.n_lat++] = FLat{sub_step_mask(n0, ks, Lt.win.first,
+                                              Lt.win.last, Lt.win.stride),
+                                (float)Lt.threshold, Lt.activated,
+                                Lt.cross_steps, Lt.cross_count,
+                                Lt.capacity};
+    }
+    k.n_probe = 0;
+    k.probe_on = 0;
+    for (int i = 0; i < a->n_probe; ++i) {
+        const fw_probe_tracker &Pp = a->probe[i];
+        const uint32_t on = sub_step_mask(n0, ks, Pp.win.first, Pp.win.last,
+                                          Pp.win.stride);
+        if (!on) continue;
+        FProbe &f = k.probe[k.n_probe++];
+        f.on = on;
+        f.sample0 = probe_samples[i];
+        probe_samples[i] += __builtin_popcount(on);
+        f.cells = Pp.cells;
+        f.out = Pp.out;
+        f.capacity = Pp.capacity;
+        f.n_cells = Pp.n_cells;
+        f.n_vars = Pp.n_vars;
+        for (int v = 0; v < FW_MAX_PROBE_VARS; ++v)
+            f.var_ids[v] = Pp.var_ids[v];
+        k.probe_on |= on;
+    }
+    return FW_OK;
 }
 
 template <class M, int ST, int KMAX, int LW, int LH, int R, int MINB>
@@ -519,119 +607,13 @@ int launch_fused(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         k.ksteps = (int32_t)ks;
         k.u_in = (const float *)a->u[li & 1];
         k.u_out = (float *)a->u[(li + 1) & 1];
-        k.n_stims = 0;
-        k.stim_on = 0;
-        for (int i = 0; i < a->n_stims; ++i) {
-            const fw_stim &St = a->stims[i];
-            if (St.last < n0 || St.first > n1) continue;
-            if (k.n_stims >= kMaxFusedStims) {
-                set_error("fw_step (fused): more than %d stimuli active in one "
-                          "launch", kMaxFusedStims);
-                return FW_ERR_UNSUPPORTED;
-            }
-            FStim &f = k.stims[k.n_stims++];
-            f.on = sub_step_mask(n0, ks, St.first, St.last, 1);
-            f.kind = St.kind;
-            f.has_umax = St.has_umax;
-            f.value = (float)St.value;
-            f.u_max = (float)St.u_max;
-            f.lo0 = (int32_t)(St.lo[0] < 0 ? 0 : St.lo[0]);
-            f.hi0 = (int32_t)(St.hi[0] > a->ni ? a->ni : St.hi[0]);
-            f.lo1 = (int32_t)(St.lo[1] < 0 ? 0 : St.lo[1]);
-            f.hi1 = (int32_t)(St.hi[1] > a->nj ? a->nj : St.hi[1]);
-            f.mask = St.mask;
-            k.stim_on |= f.on;
-        }
-        k.n_at = 0;
-        for (int i = 0; i < a->n_at; ++i) {
-            const fw_at_tracker &A = a->at[i];
-            const uint32_t on = sub_step_mask(n0, ks, A.win.first, A.win.last,
-                                              A.win.stride);
-            if (!on) continue;
-            if (k.n_at >= kMaxFusedAt) {
-                set_error("fw_step (fused): more than %d activation trackers "
-                          "active in one launch", kMaxFusedAt);
-                return FW_ERR_UNSUPPORTED;
-            }
-            k.at[k.n_at++] = FAt{on, (float)A.threshold, A.act_step};
-        }
-        k.n_lat = 0;
-        for (int i = 0; i < a->n_lat; ++i) {
-            const fw_lat_tracker &Lt = a->lat[i];
-            k.lat[k.n_lat++] = FLat{sub_step_mask(n0, ks, Lt.win.first,
-                                                  Lt.win.last, Lt.win.stride),
-                                    (float)Lt.threshold, Lt.activated,
-                                    Lt.cross_steps, Lt.cross_count,
-                                    Lt.capacity};
-        }
-        k.n_probe = 0;
-        k.probe_on = 0;
-        for (int i = 0; i < a->n_probe; ++i) {
-            const fw_probe_tracker &Pp = a->probe[i];
-            const uint32_t on = sub_step_mask(n0, ks, Pp.win.first, Pp.win.last,
-                                              Pp.win.stride);
-            if (!on) continue;
-            FProbe &f = k.probe[k.n_probe++];
-            f.on = on;
-            f.sample0 = probe_samples[i];
-            probe_samples[i] += __builtin_popcount(on);
-            f.cells = Pp.cells;
-            f.out = Pp.out;
-            f.capacity = Pp.capacity;
-            f.n_cells = Pp.n_cells;
-            f.n_vars = Pp.n_vars;
-            for (int v = 0; v < FW_MAX_PROBE_VARS; ++v)
-                f.var_ids[v] = Pp.var_ids[v];
-            k.probe_on |= on;
-        }
+        int rc = fill_events(a, k, n0, n1, ks, probe_samples);
+        if (rc) return rc;
         kern<<<(unsigned)blocks, NT, SMEM, stream>>>(k);
         FW_CHECK_LAUNCH("k_fused");
         done += ks;
     }
     return FW_OK;
-}
-
-// Region shapes of the fused kernel (64 columns = two warps wide), 8-node
-// column strips:
-//   variant 0: 64 x 32 nodes, 256 threads, two CTAs per SM (~82 KB shared
-//              memory each: one stages while the other computes);
-//   variant 1: 64 x 64 nodes, 512 threads, one CTA per SM (less halo).
-// KMAX in {2, 4, 8} time steps per launch.
-template <class M, int ST>
-int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
-                   cudaStream_t stream)
-{
-    const int k = a->fused_k ? a->fused_k : 4;
-    const int v = a->fused_variant;
-#define FW_FUSED_CASE(KK, LH, MINB)                                            \
-    return launch_fused<M, ST, KK, 64, LH, 8, MINB>(a, n_begin, n_steps, stream)
-    if (v == 0) {
-        if (k == 2) FW_FUSED_CASE(2, 32, 2);
-        if (k == 4) FW_FUSED_CASE(4, 32, 2);
-        if (k == 8) FW_FUSED_CASE(8, 32, 2);
-    } else if (v == 1) {
-        if (k == 2) FW_FUSED_CASE(2, 64, 1);
-        if (k == 4) FW_FUSED_CASE(4, 64, 1);
-        if (k == 8) FW_FUSED_CASE(8, 64, 1);
-    }
-#undef FW_FUSED_CASE
-    set_error("fw_step (fused): no kernel for fused_k=%d fused_variant=%d "
-              "(k in 2, 4, 8; variant in 0, 1)", k, v);
-    return FW_ERR_UNSUPPORTED;
-}
-
-template <class M>
-int fused_model(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
-                cudaStream_t stream)
-{
-    switch (a->stencil) {
-    case FW_STENCIL_ISO5:
-        return fused_dispatch<M, FW_STENCIL_ISO5>(a, n_begin, n_steps, stream);
-    case FW_STENCIL_ANISO9:
-        return fused_dispatch<M, FW_STENCIL_ANISO9>(a, n_begin, n_steps, stream);
-    }
-    set_error("fw_step (fused): 2D stencils only");
-    return FW_ERR_UNSUPPORTED;
 }
 
 }  // namespace fused

@@ -1,0 +1,610 @@
+// fw_fused_tma.cuh -- the fused FP32 2D step with a TMA pipeline.
+//
+// Same per-tile algorithm as fw_fused_kernel.cuh (temporal blocking of up to
+// KMAX steps on a 64 x LH region, halo recomputed), organised for Blackwell:
+//   * one persistent CTA per SM walks the tiles (tile, tile + gridDim.x, ...);
+//   * its region is staged by the Tensor Memory Accelerator: thread 0 issues
+//     cp.async.bulk.tensor copies (packed weights, potential, state,
+//     myocyte flags) that complete on an mbarrier;
+//   * two stages: while the CTA computes tile i from one stage, the TMA
+//     fills the other with tile i + 1, so HBM traffic overlaps compute.
+// Every wait on an mbarrier is bounded; a timeout sets FW_DEV_TIMEOUT in the
+// status word and the CTA returns.
+//
+// Layout requirements (checked by the host): nj % 16 == 0 (TMA row strides
+// and the int8 myocyte rows) and the packed weight array of fw_pack_weights.
+// Boxes start at 16-byte aligned x coordinates (x rounded down, the data is
+// addressed at an offset inside the box), negative and past-the-end
+// coordinates read zeros.
+#pragma once
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "fw_fused_kernel.cuh"
+
+namespace fw {
+namespace fused {
+
+constexpr int kTW = 64;    // region width (nodes)
+constexpr int kBoxF = 72;  // f32 box width: columns oj - 1 .. oj + 64 from a 4-aligned start
+constexpr int kBoxB = 80;  // int8 box width: columns oj .. oj + 63 from a 16-aligned start
+constexpr int kMaxTmaState = 2;
+
+template <int LH, int NS, int NWO>
+struct TmaStage {
+    alignas(128) float4 wa[LH][kTW];                   // weights 0..3
+    alignas(128) float4 wb[NWO == 8 ? LH : 1][kTW];    // weights 4..7
+    alignas(128) float u[LH + 2][kBoxF];               // rows oi - 1 .. oi + LH
+    alignas(128) float s[NS][LH][kBoxF];               // rows oi .. oi + LH - 1
+    alignas(128) int8_t myo[LH][kBoxB];
+};
+
+template <int LH, int NS, int NWO>
+struct TmaSmem {
+    TmaStage<LH, NS, NWO> stage[2];
+    alignas(128) float u1[LH + 2][kBoxF];              // ping-pong partner
+    uint32_t probe_bits[(LH * kTW + 31) / 32];
+    ProbeEntry probe_list[kMaxFusedProbeEntries];
+    int probe_count;
+    alignas(8) uint64_t bar[2];
+};
+
+struct TmaMaps {
+    CUtensorMap w;      // packed weights: dims (NWO, nj, ni)
+    CUtensorMap myo;    // int8 (nj, ni)
+    CUtensorMap u[2];   // f32 (nj, ni), the two potential buffers
+    CUtensorMap s[kMaxTmaState];
+};
+
+struct TmaK {
+    TmaMaps maps;
+    FusedK f;
+    int32_t in_buf;     // potential buffer holding step n0
+    int32_t tiles;
+};
+
+// ---- PTX wrappers ------------------------------------------------------------
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)),
+                 "r"(count));
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile(
+        "mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;\n" ::"r"(
+            smem_u32(bar)),
+        "r"(bytes)
+        : "memory");
+}
+
+// Bounded wait for phase `parity` of the barrier; false on timeout.  Each
+// try_wait suspends for at most ~1 us (the hint), so the bound is ~2 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+{
+    const unsigned a = smem_u32(bar);
+    for (int i = 0; i < (1 << 21); ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n"
+            " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity), "r"(1000)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *map, int x,
+                                       int y, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::"
+        "bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_3d(void *dst, const CUtensorMap *map, int x,
+                                       int y, int z, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::"
+        "bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ int floor_to(int x, int m)
+{
+    return x >= 0 ? x - x % m : -((-x + m - 1) / m) * m;
+}
+
+// ---- kernel ----------------------------------------------------------------------
+
+template <int KMAX, int LH, int NS, int NWO>
+__device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> &G,
+                                           uint64_t *bar, int tile)
+{
+    constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
+    const int bi = tile / k.f.tiles_j, bj = tile % k.f.tiles_j;
+    const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
+    const int x4 = floor_to(oj - 1, 4), x16 = floor_to(oj, 16);
+    constexpr unsigned bytes =
+        sizeof(G.wa) + (NWO == 8 ? sizeof(G.wb) : 0) + sizeof(G.u) +
+        sizeof(G.s) + sizeof(G.myo);
+    mbar_expect_tx(bar, bytes);
+    tma_3d(&G.wa[0][0], &k.maps.w, 0, oj, oi, bar);
+    if constexpr (NWO == 8) tma_3d(&G.wb[0][0], &k.maps.w, 4, oj, oi, bar);
+    tma_2d(&G.u[0][0], &k.maps.u[k.in_buf], x4, oi - 1, bar);
+#pragma unroll
+    for (int q = 0; q < NS; ++q) tma_2d(&G.s[q][0][0], &k.maps.s[q], x4, oi, bar);
+    tma_2d(&G.myo[0][0], &k.maps.myo, x16, oi, bar);
+}
+
+template <class M, int ST, int KMAX, int LH, int R>
+__global__ void __launch_bounds__(kTW *(LH / R), 1)
+    k_fused_tma(const __grid_constant__ TmaK k)
+{
+    constexpr int LW = kTW;
+    constexpr int NT = LW * (LH / R);
+    constexpr int TI = LH - 2 * KMAX, TJ = LW - 2 * KMAX;
+    constexpr int NS = M::NS;
+    constexpr int NWO = Stencil2D<ST>::NWO;
+    static_assert(LH % R == 0 && R <= 8 && TI > 0 && TJ > 0, "tile shape");
+    static_assert(NS <= kMaxTmaState, "state arrays");
+
+    // TMA destinations are 128-byte aligned: round the dynamic shared window
+    // up (the launch reserves 1 KB of slack for this)
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned mis = smem_u32(smem_raw) & 127u;
+    TmaSmem<LH, NS, NWO> &S = *reinterpret_cast<TmaSmem<LH, NS, NWO> *>(
+        smem_raw + (mis ? 128u - mis : 0u));
+    const FusedK &f = k.f;
+
+    const int tid = threadIdx.x;
+    const int col = tid % LW;
+    const int r0 = (tid / LW) * R;
+    const bool col_interior = col >= KMAX && col < KMAX + TJ;
+
+    if (tid == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    int tile = blockIdx.x;
+    if (tid == 0 && tile < k.tiles) issue_tile<KMAX>(k, S.stage[0], &S.bar[0], tile);
+
+    Params<float, M::NP> P;
+#pragma unroll
+    for (int i = 0; i < M::NP; ++i) P.v[i] = f.params[i];
+    const float dt = f.dt;
+    unsigned parity = 0u;  // bit sg: phase parity expected next on bar[sg]
+
+    for (int it = 0; tile < k.tiles; ++it, tile += gridDim.x) {
+        const int sg = it & 1;
+        TmaStage<LH, NS, NWO> &G = S.stage[sg];
+        // prefetch the next tile into the other stage (its readers finished
+        // at the barrier that closed the previous iteration)
+        const int next = tile + gridDim.x;
+        if (tid == 0 && next < k.tiles) {
+            fence_proxy_async();
+            issue_tile<KMAX>(k, S.stage[sg ^ 1], &S.bar[sg ^ 1], next);
+        }
+        const bool ok = mbar_wait(&S.bar[sg], (parity >> sg) & 1u);
+        parity ^= 1u << sg;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0 && f.status) atomicOr(f.status, FW_DEV_TIMEOUT);
+            return;
+        }
+
+        const int bi = tile / f.tiles_j, bj = tile % f.tiles_j;
+        const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
+        const int xo = oj - floor_to(oj - 1, 4);   // 1..4
+        const int xo8 = oj - floor_to(oj, 16);     // 0..15
+        const int gj = oj + col;
+        const bool col_in = gj >= 0 && gj < f.nj;
+
+        // per-thread flags and state of the strip
+        typename M::template St<float> st[R];
+        uint32_t myo_bits = 0, own = 0, upd = 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int lr = r0 + r, gi = oi + lr;
+            const bool in = col_in && gi >= 0 && gi < f.ni;
+            if (in && G.myo[lr][col + xo8]) myo_bits |= 1u << r;
+            if (in && col_interior && lr >= KMAX && lr < KMAX + TI) own |= 1u << r;
+            if (col > 0 && col < LW - 1 && lr > 0 && lr < LH - 1) upd |= 1u << r;
+            float sv[kMaxTmaState];
+#pragma unroll
+            for (int q = 0; q < NS; ++q) sv[q] = G.s[q][lr][col + xo];
+            st[r] = M::template from_array<float>(sv);
+        }
+        upd &= myo_bits;
+
+        // probe cells of this tile
+        uint32_t probe_mine = 0;
+        if (f.n_probe) {
+            for (int i = tid; i < (LH * LW + 31) / 32; i += NT) S.probe_bits[i] = 0;
+            if (tid == 0) S.probe_count = 0;
+            __syncthreads();
+            for (int t = 0; t < f.n_probe; ++t) {
+                const FProbe &pr = f.probe[t];
+                for (int c = tid; c < pr.n_cells; c += NT) {
+                    const int64_t p = pr.cells[c];
+                    const int gi = (int)(p / f.nj), gjj = (int)(p % f.nj);
+                    const int lr = gi - oi, lc = gjj - oj;
+                    if (lr >= KMAX && lr < KMAX + TI && lc >= KMAX &&
+                        lc < KMAX + TJ) {
+                        const int e = atomicAdd(&S.probe_count, 1);
+                        if (e < kMaxFusedProbeEntries) {
+                            S.probe_list[e] = ProbeEntry{(int16_t)lr, (int16_t)lc,
+                                                         (int16_t)t, c};
+                            const int bit = lr * LW + lc;
+                            atomicOr(&S.probe_bits[bit >> 5], 1u << (bit & 31));
+                        } else if (f.status) {
+                            atomicOr(f.status, FW_DEV_PROBE_OVERFLOW);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int bit = (r0 + r) * LW + col;
+                if ((S.probe_bits[bit >> 5] >> (bit & 31)) & 1u)
+                    probe_mine |= 1u << r;
+            }
+        }
+        uint32_t lat_act = 0, at_done = 0;
+#pragma unroll
+        for (int l = 0; l < kMaxFusedLat; ++l)
+            if (l < f.n_lat) {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+                    if ((own >> r) & 1u) {
+                        const int64_t p = (int64_t)(oi + r0 + r) * f.nj + gj;
+                        if (f.lat[l].activated[p]) lat_act |= 1u << (l * 8 + r);
+                    }
+            }
+
+        // ---- sub-steps ----
+        for (int s = 0; s < f.ksteps; ++s) {
+            const int64_t n = f.n0 + s;
+            float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
+            float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;
+
+            if ((f.stim_on >> s) & 1u) {
+                for (int i = 0; i < f.n_stims; ++i) {
+                    const FStim &F = f.stims[i];
+                    if (!((F.on >> s) & 1u)) continue;
+                    if (gj < F.lo1 || gj >= F.hi1) continue;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        if (!((myo_bits >> r) & 1u)) continue;
+                        const int lr = r0 + r, gi = oi + lr;
+                        if (gi < F.lo0 || gi >= F.hi0) continue;
+                        if (F.mask && !F.mask[(int64_t)gi * f.nj + gj]) continue;
+                        float x = cur[lr + 1][col + xo];
+                        if (F.kind == FW_STIM_VOLTAGE) {
+                            x = F.value;
+                        } else {
+                            x = x + F.value;
+                            if (F.has_umax && x > F.u_max) x = F.u_max;
+                        }
+                        cur[lr + 1][col + xo] = x;
+                    }
+                }
+                __syncthreads();
+            }
+
+            float wl[R + 2], wc[R + 2], wr[R + 2];
+#pragma unroll
+            for (int i = 0; i < R + 2; ++i) {
+                wl[i] = cur[r0 + i][col + xo - 1];
+                wc[i] = cur[r0 + i][col + xo];
+                wr[i] = cur[r0 + i][col + xo + 1];
+            }
+
+            if (own) {
+#pragma unroll
+                for (int a = 0; a < kMaxFusedAt; ++a) {
+                    if (a >= f.n_at || !((f.at[a].on >> s) & 1u)) continue;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const uint32_t bit = 1u << (a * 8 + r);
+                        if (!((own >> r) & 1u) || (at_done & bit)) continue;
+                        if (wc[r + 1] > f.at[a].thr) {
+                            // first crossing: unsigned minimum, "never" = -1
+                            // (activation_time_2d_tracker.py:61-63)
+                            const int64_t p = (int64_t)(oi + r0 + r) * f.nj + gj;
+                            atomicMin(reinterpret_cast<unsigned *>(f.at[a].act) + p,
+                                      (unsigned)n);
+                            at_done |= bit;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int l = 0; l < kMaxFusedLat; ++l) {
+                    if (l >= f.n_lat || !((f.lat[l].on >> s) & 1u)) continue;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        if (!((own >> r) & 1u)) continue;
+                        const uint32_t bit = 1u << (l * 8 + r);
+                        const bool was = (lat_act & bit) != 0;
+                        const float x = wc[r + 1];
+                        if (x >= f.lat[l].thr && !was) {
+                            // (local_activation_time_2d_tracker.py:71-89)
+                            lat_act |= bit;
+                            lat_record(f.lat[l], (int64_t)(oi + r0 + r) * f.nj + gj,
+                                       f.n, n, f.status);
+                        } else if (x < f.lat[l].thr && was) {
+                            lat_act &= ~bit;
+                        }
+                    }
+                }
+            }
+
+            const bool probes_now = probe_mine && ((f.probe_on >> s) & 1u);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float b1 = wc[r + 1];
+                const int lr = r0 + r;
+                float d;
+                const float4 wa = G.wa[lr][col];
+                if constexpr (ST == FW_STENCIL_ISO5) {
+                    d = wa.x * (wc[r] - b1) + wa.y * (wl[r + 1] - b1) +
+                        wa.z * (wr[r + 1] - b1) + wa.w * (wc[r + 2] - b1);
+                } else {
+                    const float4 wb = G.wb[lr][col];
+                    d = wa.x * (wl[r] - b1) + wa.y * (wc[r] - b1) +
+                        wa.z * (wr[r] - b1) + wa.w * (wl[r + 1] - b1) +
+                        wb.x * (wr[r + 1] - b1) + wb.y * (wl[r + 2] - b1) +
+                        wb.z * (wc[r + 2] - b1) + wb.w * (wr[r + 2] - b1);
+                }
+                const float uu = M::template update<float>(b1, b1 + d, st[r], P, dt);
+                nxt[lr + 1][col + xo] = ((upd >> r) & 1u) ? uu : b1;
+                if (probes_now && ((probe_mine >> r) & 1u))
+                    write_probes<M>(f, S.probe_list, S.probe_count, lr, col, s, b1,
+                                    st[r], ((myo_bits >> r) & 1u) != 0,
+                                    (int64_t)(oi + lr) * f.nj + gj);
+            }
+            __syncthreads();
+        }
+
+        // ---- write the interior back ----
+        float(*fin)[kBoxF] = (f.ksteps & 1) ? S.u1 : G.u;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (!((own >> r) & 1u)) continue;
+            const int lr = r0 + r;
+            const int64_t p = (int64_t)(oi + lr) * f.nj + gj;
+            if ((myo_bits >> r) & 1u) {
+                f.u_out[p] = fin[lr + 1][col + xo];
+                M::template store<float>(f.state, p, st[r]);
+            }
+#pragma unroll
+            for (int l = 0; l < kMaxFusedLat; ++l)
+                if (l < f.n_lat)
+                    f.lat[l].activated[p] = (lat_act >> (l * 8 + r)) & 1u;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- host side -------------------------------------------------------------------
+
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+inline bool encode_2d(CUtensorMap *m, CUtensorMapDataType t, size_t esize,
+                      const void *base, int64_t nj, int64_t ni, int bw, int bh)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)nj, (cuuint64_t)ni};
+    cuuint64_t strides[1] = {(cuuint64_t)(nj * esize)};
+    cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
+    cuuint32_t es[2] = {1, 1};
+    return enc(m, t, 2, const_cast<void *>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+inline bool encode_weights(CUtensorMap *m, const void *base, int nwo, int64_t nj,
+                           int64_t ni, int bh)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)nwo, (cuuint64_t)nj, (cuuint64_t)ni};
+    cuuint64_t strides[2] = {(cuuint64_t)(nwo * 4), (cuuint64_t)(nj * nwo * 4)};
+    cuuint32_t box[3] = {4, (cuuint32_t)kTW, (cuuint32_t)bh};
+    cuuint32_t es[3] = {1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(base), dims,
+               strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+inline int sm_count()
+{
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+// True when the TMA form can run this configuration.
+inline bool tma_usable(const fw_step_args *a)
+{
+    return a->weights_packed && a->nj % 16 == 0 && a->ni < (1 << 30) &&
+           a->nj < (1 << 30) && tensor_map_encoder() != nullptr;
+}
+
+template <class M, int ST, int KMAX, int LH, int R>
+int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                     cudaStream_t stream)
+{
+    constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
+    constexpr int NT = kTW * (LH / R);
+    constexpr int NWO = Stencil2D<ST>::NWO;
+    constexpr size_t SMEM = sizeof(TmaSmem<LH, M::NS, NWO>) + 1024;
+    auto kern = k_fused_tma<M, ST, KMAX, LH, R>;
+    FW_CUDA_CHECK(cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM));
+    if (a->n_lat > kMaxFusedLat) {
+        set_error("fw_step (fused): at most %d local activation tracker",
+                  kMaxFusedLat);
+        return FW_ERR_UNSUPPORTED;
+    }
+    TmaK k;  // kernel argument, copied at each launch
+    memset(&k, 0, sizeof k);
+    bool ok = encode_weights(&k.maps.w, a->weights_packed, NWO, a->nj, a->ni, LH) &&
+              encode_2d(&k.maps.myo, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a->myo,
+                        a->nj, a->ni, kBoxB, LH) &&
+              encode_2d(&k.maps.u[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->u[0],
+                        a->nj, a->ni, kBoxF, LH + 2) &&
+              encode_2d(&k.maps.u[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->u[1],
+                        a->nj, a->ni, kBoxF, LH + 2);
+    for (int q = 0; q < M::NS && ok; ++q)
+        ok = encode_2d(&k.maps.s[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->state[q],
+                       a->nj, a->ni, kBoxF, LH);
+    if (!ok) {
+        set_error("fw_step (fused TMA): tensor map encoding failed");
+        return FW_ERR_UNSUPPORTED;
+    }
+    FusedK &f = k.f;
+    f.w = nullptr;
+    f.myo = a->myo;
+    for (int i = 0; i < FW_MAX_STATE; ++i) f.state[i] = a->state[i];
+    for (int i = 0; i < FW_MAX_PARAMS; ++i) f.params[i] = (float)a->params[i];
+    f.dt = (float)a->dt;
+    f.ni = (int32_t)a->ni;
+    f.nj = (int32_t)a->nj;
+    f.n = a->ni * a->nj;
+    f.status = a->status;
+    const int tiles_i = (int)((a->ni + TI - 1) / TI);
+    f.tiles_j = (int)((a->nj + TJ - 1) / TJ);
+    k.tiles = tiles_i * f.tiles_j;
+    int sms = sm_count();
+    if (sms <= 0) sms = 152;
+    const int grid = k.tiles < sms ? k.tiles : sms;
+    int64_t probe_samples[FW_MAX_PROBE];
+    for (int i = 0; i < a->n_probe; ++i) probe_samples[i] = a->probe[i].sample_offset;
+
+    int64_t L = (n_steps + KMAX - 1) / KMAX;
+    if ((L & 1) != (n_steps & 1)) ++L;
+    int64_t done = 0;
+    for (int64_t li = 0; li < L; ++li) {
+        const int64_t left = n_steps - done, launches_left = L - li;
+        int64_t ks = (left + launches_left - 1) / launches_left;
+        if (ks > KMAX) ks = KMAX;
+        const int64_t n0 = n_begin + done;
+        const int64_t n1 = n0 + ks - 1;
+        f.n0 = n0;
+        f.ksteps = (int32_t)ks;
+        k.in_buf = (int32_t)(li & 1);
+        f.u_in = (const float *)a->u[li & 1];
+        f.u_out = (float *)a->u[(li + 1) & 1];
+        int rc = fill_events(a, f, n0, n1, ks, probe_samples);
+        if (rc) return rc;
+        kern<<<grid, NT, SMEM, stream>>>(k);
+        FW_CHECK_LAUNCH("k_fused_tma");
+        done += ks;
+    }
+    return FW_OK;
+}
+
+// Kernel choice (fw_step_args.fused_variant):
+//   0: automatic -- the TMA pipeline when it can run, else 1;
+//   1: cp.async staging, 64 x 32 regions, 256 threads, two CTAs per SM;
+//   2: cp.async staging, 64 x 64 regions, 512 threads, one CTA per SM;
+//   3: TMA pipeline: persistent CTAs, 64 x 32 regions, 512 threads with
+//      4-node strips, two stages in shared memory.
+// KMAX (fused_k) in {2, 4, 8} time steps per launch.
+template <class M, int ST>
+int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                   cudaStream_t stream)
+{
+    const int k = a->fused_k ? a->fused_k : 4;
+    int v = a->fused_variant;
+    if (v == 0) v = tma_usable(a) ? 3 : 1;
+    if (v == 3 && !tma_usable(a)) {
+        set_error("fw_step (fused): the TMA kernel needs packed weights and "
+                  "nj %% 16 == 0");
+        return FW_ERR_UNSUPPORTED;
+    }
+#define FW_CP_CASE(KK, LH, MINB)                                               \
+    return launch_fused<M, ST, KK, 64, LH, 8, MINB>(a, n_begin, n_steps, stream)
+#define FW_TMA_CASE(KK)                                                        \
+    return launch_fused_tma<M, ST, KK, 32, 4>(a, n_begin, n_steps, stream)
+    if (v == 1) {
+        if (k == 2) FW_CP_CASE(2, 32, 2);
+        if (k == 4) FW_CP_CASE(4, 32, 2);
+        if (k == 8) FW_CP_CASE(8, 32, 2);
+    } else if (v == 2) {
+        if (k == 2) FW_CP_CASE(2, 64, 1);
+        if (k == 4) FW_CP_CASE(4, 64, 1);
+        if (k == 8) FW_CP_CASE(8, 64, 1);
+    } else if (v == 3) {
+        if (k == 2) FW_TMA_CASE(2);
+        if (k == 4) FW_TMA_CASE(4);
+        if (k == 8) FW_TMA_CASE(8);
+    }
+#undef FW_CP_CASE
+#undef FW_TMA_CASE
+    set_error("fw_step (fused): no kernel for fused_k=%d fused_variant=%d "
+              "(k in 2, 4, 8; variant in 0..3)", k, a->fused_variant);
+    return FW_ERR_UNSUPPORTED;
+}
+
+template <class M>
+int fused_model(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                cudaStream_t stream)
+{
+    switch (a->stencil) {
+    case FW_STENCIL_ISO5:
+        return fused_dispatch<M, FW_STENCIL_ISO5>(a, n_begin, n_steps, stream);
+    case FW_STENCIL_ANISO9:
+        return fused_dispatch<M, FW_STENCIL_ANISO9>(a, n_begin, n_steps, stream);
+    }
+    set_error("fw_step (fused): 2D stencils only");
+    return FW_ERR_UNSUPPORTED;
+}
+
+}  // namespace fused
+}  // namespace fw

@@ -133,6 +133,8 @@ int step_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                cudaStream_t stream);
 int step_fused(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                cudaStream_t stream);
+int pack_weights(int32_t stencil, const float *w, int64_t n, float *out,
+                 cudaStream_t stream);
 int step_fused_ap(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                   cudaStream_t stream);
 int step_fused_ms(const fw_step_args *a, int64_t n_begin, int64_t n_steps,

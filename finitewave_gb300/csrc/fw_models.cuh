@@ -73,6 +73,11 @@ struct ModelAP {
         return (double)x.v;
     }
     template <class T>
+    __device__ static __forceinline__ St<T> from_array(const T *a)
+    {
+        return {a[0]};
+    }
+    template <class T>
     __device__ static __forceinline__ T update(T u, T un, St<T> &x,
                                                const Params<T, NP> &P, T dt)
     {
@@ -110,6 +115,11 @@ struct ModelMS {
     __device__ static __forceinline__ double probe(const St<T> &x, int)
     {
         return (double)x.h;
+    }
+    template <class T>
+    __device__ static __forceinline__ St<T> from_array(const T *a)
+    {
+        return {a[0]};
     }
     template <class T>
     __device__ static __forceinline__ T update(T u, T un, St<T> &x,
@@ -154,6 +164,11 @@ struct ModelFK {
     __device__ static __forceinline__ double probe(const St<T> &x, int i)
     {
         return i == 0 ? (double)x.v : (double)x.w;
+    }
+    template <class T>
+    __device__ static __forceinline__ St<T> from_array(const T *a)
+    {
+        return {a[0], a[1]};
     }
     template <class T>
     __device__ static __forceinline__ T update(T u, T un, St<T> &x,

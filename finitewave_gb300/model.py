@@ -224,6 +224,26 @@ class CardiacModel:
         if self.stencil is None:
             self.stencil = self.select_stencil(tissue)
         self.weights = self.stencil.compute_weights(self, tissue)
+        self._pack_weights()
+
+    def _pack_weights(self):
+        """Node-major copy of the off-centre weights for the TMA form of the
+        fused kernel (fw_pack_weights); only for 2D float32 grids whose row
+        length is a multiple of 16 nodes."""
+        self._wpack = None
+        kind = self.stencil.kind
+        shape = self._shape()
+        if (self._precision() != _ffi.F32 or kind not in (_ffi.ISO5, _ffi.ANISO9)
+                or self._model_id not in self._FUSED_MODELS
+                or shape[1] % 16 != 0 or self.form == "plain"):
+            return
+        nwo = 4 if kind == _ffi.ISO5 else 8
+        n = shape[0] * shape[1]
+        self._wpack = torch.empty(n * nwo, dtype=torch.float32,
+                                  device=self._device())
+        _ffi.call("fw_pack_weights", kind, self.weights.data_ptr(), n,
+                  self._wpack.data_ptr(),
+                  torch.cuda.current_stream().cuda_stream)
 
     def select_stencil(self, cardiac_tissue):
         raise NotImplementedError
@@ -372,6 +392,8 @@ class CardiacModel:
         a.mesh = self._mesh_d.data_ptr()
         a.myo = self._myo_d.data_ptr()
         a.weights = self.weights.data_ptr()
+        wpack = getattr(self, "_wpack", None)
+        a.weights_packed = wpack.data_ptr() if wpack is not None else None
         a.u[0] = self._dev["u"].data_ptr()
         a.u[1] = self._dev["u_new"].data_ptr()
         for i, name in enumerate(self._state_names):

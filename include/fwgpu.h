@@ -48,6 +48,7 @@ extern "C" {
 #define FW_DEV_LAT_OVERFLOW 1   /* a cell crossed more often than capacity  */
 #define FW_DEV_PROBE_OVERFLOW 2 /* a probe sample index beyond capacity     */
 #define FW_DEV_BATCH_FAULT 4    /* a batch tile descriptor out of range     */
+#define FW_DEV_TIMEOUT 8        /* a bounded on-chip wait gave up           */
 
 /* ------------------------------------------------------------ enumerations */
 enum fw_model {
@@ -184,8 +185,16 @@ typedef struct fw_step_args {
     int32_t *status;  /* device int32 status word (may be NULL)             */
     int32_t fused_k;  /* FW_FORM_FUSED time steps per launch: 2, 4 or 8
                          (0 = 4)                                            */
-    int32_t fused_variant; /* FW_FORM_FUSED region shape: 0 = 64x64 nodes,
-                              512 threads; 1 = 64x32 nodes, 256 threads     */
+    int32_t fused_variant; /* FW_FORM_FUSED kernel: 0 = automatic (the TMA
+                              pipeline when weights_packed is given and
+                              nj % 16 == 0, else 1); 1 = cp.async staging,
+                              64x32-node regions, two CTAs per SM; 2 = same,
+                              64x64 regions; 3 = TMA pipeline (persistent
+                              CTAs, double-buffered 64x32 regions)          */
+    const void *weights_packed; /* FW_FORM_FUSED: off-centre float32 weights
+                                   node-major, (N, 4) for ISO5 or (N, 8)
+                                   for ANISO9, from fw_pack_weights; NULL
+                                   when not available                       */
 } fw_step_args;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -245,6 +254,13 @@ FW_API int fw_diffuse(int32_t stencil, int32_t precision, void *u_new, const voi
 FW_API int fw_ionic(int32_t model, int32_t precision, void *u_new, const void *u,
              void *const *state, const int64_t *idx, int64_t n_idx,
              double dt, const double *params, void *stream);
+
+/* Repack float32 weight-major weights (nw, N) into the node-major layout of
+ * the fused TMA kernel: out[p * nwo + q] = w[plane_q * N + p] over the
+ * off-centre planes (nwo = 4 for ISO5, 8 for ANISO9; the centre weight is
+ * implied because each stencil row sums to one).  2D stencils only. */
+FW_API int fw_pack_weights(int32_t stencil, const float *w, int64_t n,
+                           float *out, void *stream);
 
 /* Advance n_steps time steps starting at global step n_begin (the model's
  * step counter).  On return the current u is a->u[n_steps & 1]. */

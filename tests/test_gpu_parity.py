@@ -212,13 +212,16 @@ def test_f32_close_to_f64(gc, form):
 @pytest.mark.parametrize("name", ["ap", "ms", "fk"])
 @pytest.mark.parametrize("aniso", [False, True])
 @pytest.mark.parametrize("k", [2, 4, 8])
-def test_fused_matches_plain_f32(gc, name, aniso, k):
+@pytest.mark.parametrize("variant,nj", [(1, 140), (2, 140), (3, 144)])
+def test_fused_matches_plain_f32(gc, name, aniso, k, variant, nj):
     """Fused temporal blocking vs the plain FP32 form on a grid of several
-    tiles (150 x 140), S1 plus a cross-field S2, 777 steps (an odd count, not
+    tiles (150 x nj), S1 plus a cross-field S2, 777 steps (an odd count, not
     a multiple of k): same activation steps within one step, fields within
-    a tolerance that covers FMA-vs-no-FMA rounding."""
+    a tolerance that covers FMA-vs-no-FMA rounding.  Variants 1 and 2 stage
+    with cp.async; variant 3 is the persistent TMA pipeline (rows of a
+    multiple of 16 nodes)."""
     rng = np.random.default_rng(11)
-    ni, nj = 150, 140
+    ni = 150
     mesh = np.where(rng.random((ni, nj)) < 0.15, 2, 1).astype(np.int8)
     ang = rng.uniform(-np.pi, np.pi, (ni, nj))
     fibers = np.stack([np.cos(ang), np.sin(ang)], -1)
@@ -233,7 +236,9 @@ def test_fused_matches_plain_f32(gc, name, aniso, k):
                                                     [149, 139], [56, 56]],
                                vars=cases.MODEL_VARS[name], step=3)])
     ref = gc.run(case, npfloat="float32", form="plain")
-    r = gc.run(case, npfloat="float32", form="fused", fused_k=k)
+    r = gc.run(case, npfloat="float32", form="fused", fused_k=k,
+               fused_variant=variant)
+    assert int(r["model"]._status.item()) == 0
     assert r["step"] == ref["step"] == 777
     assert _at_agree(r["trackers"][0], ref["trackers"][0], 0.01) >= 0.999
     for v in cases.MODEL_VARS[name]:
