@@ -212,6 +212,10 @@ def run_gb300(args):
 
     # dominant-kernel timing: launches of one segment averaged
     kms, kl = device_steps(model, chunk, 3, torch)
+    form_used = model._form()
+    kernel_name = ("k_fused_tma" if form_used == 1 and model._wpack is not None
+                   and args.fused_variant in (0, 3) else
+                   "k_fused" if form_used == 1 else "k_step")
     steps_per_launch = (3 * chunk) / max(1, kl)
     per_launch_s = (kms / 1e3) / max(1, kl)
     alg_bytes = B_ALG["float32"] * myo * steps_per_launch
@@ -268,9 +272,10 @@ def run_gb300(args):
     for _ in range(max(1, W // 2)):
         m64._run_segment(chunk, sync=False)
     barrier()
-    ms64, _ = device_steps(m64, chunk, max(1, K // 2), torch)
+    k64 = max(3, K // 20)
+    ms64, _ = device_steps(m64, chunk, k64, torch)
     ms64 = max_over_ranks(ms64)
-    fp64_value = world * myo * chunk * max(1, K // 2) / (ms64 / 1e3)
+    fp64_value = world * myo * chunk * k64 / (ms64 / 1e3)
     del m64
     torch.cuda.empty_cache()
 
@@ -301,7 +306,7 @@ def run_gb300(args):
                          "peak_source": peak_kind,
                          "traffic": traffic_from_profiles(myo,
                                                           steps_per_launch),
-                         "kernel": "fw step kernel (float32)",
+                         "kernel": kernel_name,
                          "alg_bytes_per_myocyte_step": B_ALG["float32"],
                          "time_steps_per_launch": steps_per_launch},
             "cpu_baseline": cpu,
@@ -389,7 +394,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--chunk", type=int, default=100)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])

@@ -582,6 +582,7 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         if (k == 8) FW_CP_CASE(8, 64, 1);
     } else if (v == 3) {
         if (k == 2) FW_TMA_CASE(2);
+        if (k == 3) FW_TMA_CASE(3);
         if (k == 4) FW_TMA_CASE(4);
         if (k == 8) FW_TMA_CASE(8);
     }
