@@ -327,3 +327,69 @@ def step_count(t_max, dt, t0=0):
         if t > t_max or step > int(math.ceil(t_max / dt)):
             break
     return step
+
+
+# ------------------------------------------------------------------ detailed
+# Parameters in the reference kernels' argument order and initial values
+# (tp06_2d.py:81-170 with the signature at :1003-1012; courtemanche_2d.py:
+# 122-178 with the signature at :569-577).
+
+TP06_PARAMS = dict(
+    ko=5.4, cao=2.0, nao=140.0, Vc=0.016404, Vsr=0.001094, Vss=0.00005468,
+    Bufc=0.2, Kbufc=0.001, Bufsr=10.0, Kbufsr=0.3, Bufss=0.4,
+    Kbufss=0.00025, Vmaxup=0.006375, Kup=0.00025, Vrel=0.102, k1_=0.15,
+    k2_=0.045, k3=0.060, k4=0.005, EC=1.5, maxsr=2.5, minsr=1.0,
+    Vleak=0.00036, Vxfer=0.0038, R=8314.472, F=96485.3415, T=310.0,
+    RTONF=26.71376, CAPACITANCE=0.185, gkr=0.153, pKNa=0.03, gk1=5.405,
+    gna=14.838, gbna=0.00029, KmK=1.0, KmNa=40.0, knak=2.724,
+    gcal=0.00003980, gbca=0.000592, knaca=1000, KmNai=87.5, KmCa=1.38,
+    ksat=0.1, n_=0.35, gpca=0.1238, KpCa=0.0005, gpk=0.0146, gto=0.294,
+    gks=0.392)
+TP06_STATE = ["cai", "casr", "cass", "nai", "Ki", "m", "h", "j", "xr1",
+              "xr2", "xs", "r", "s", "d", "f", "f2", "fcass", "rr", "oo"]
+TP06_INIT = dict(u=-84.5, cai=0.00007, casr=1.3, cass=0.00007, nai=7.67,
+                 Ki=138.3, m=0.0, h=0.75, j=0.75, xr1=0.0, xr2=1.0, xs=0.0,
+                 r=0.0, s=1.0, d=0.0, f=1.0, f2=1.0, fcass=1.0, rr=1.0,
+                 oo=0.0)
+
+_vc = 20100
+_vj = _vc * 0.68
+CRN_PARAMS = dict(
+    gna=7.8, gnab=0.000674, gk1=0.09, gkr=0.0294, gks=0.129, gto=0.1652,
+    gcal=0.1238, gcab=0.00113, gkur_coeff=1, F=96485.0, T=310.0, R=8314.0,
+    Vc=_vc, Vj=_vj, Vup=_vj * 0.06 * 0.92, Vrel=_vj * 0.06 * 0.08, ibk=0.0,
+    cao=1.8, nao=140, ko=5.4, caupmax=15, kup=0.00092, kmnai=10, kmko=1.5,
+    kmnancx=87.5, kmcancx=1.38, ksatncx=0.1, kmcmdn=0.00238,
+    kmtrpn=0.0005, kmcsqn=0.8, trpnmax=0.07, cmdnmax=0.05, csqnmax=10.0,
+    inacamax=1600, inakmax=0.6, ipcamax=0.275, krel=30, iupmax=0.005,
+    kq10=3)
+CRN_STATE = ["nai", "ki", "cai", "caup", "carel", "m", "h", "j_", "d", "f",
+             "oa", "oi", "ua", "ui", "xr", "xs", "fca", "irel", "vrel",
+             "urel", "wrel"]
+CRN_INIT = dict(u=-84.5, nai=11.2, ki=139, cai=0.000102, caup=1.6,
+                carel=1.1, m=0.00291, h=0.965, j_=0.978, d=0.000137,
+                f=0.999837, oa=0.000592, oi=0.9992, ua=0.003519, ui=0.9987,
+                xs=0.0187, xr=3.29e-05, fca=0.775, irel=0, vrel=1, urel=0,
+                wrel=0.9)
+
+
+def _detailed_ionic(fn_name, names):
+    def ionic(L, un, u, st, idx, dt, p):
+        ptrs = (ctypes.c_void_p * len(names))(
+            *[st[n].ctypes.data for n in names])
+        par = (ctypes.c_double * len(p))(*p.values())
+        fn = getattr(L, fn_name)
+        fn.argtypes = [_P, _P, _P, _P, _I, _D, _P]
+        fn(_p(un), _p(u), ptrs, _p(idx), idx.size, dt, par)
+    return ionic
+
+
+register_model("tp06", dict(params=TP06_PARAMS,
+                            init={k: TP06_INIT[k] for k in ["u"] + TP06_STATE},
+                            D_model=0.154, reset_u_new=True,
+                            ionic=_detailed_ionic("fwo_ionic_tp06",
+                                                  TP06_STATE)))
+register_model("crn", dict(params=CRN_PARAMS,
+                           init={k: CRN_INIT[k] for k in ["u"] + CRN_STATE},
+                           D_model=0.154, reset_u_new=True,
+                           ionic=_detailed_ionic("fwo_ionic_crn", CRN_STATE)))

@@ -108,3 +108,61 @@ def stimuli_2d():
                             coords=g["area_coords"], u_max=1.2)],
                 trackers=[dict(kind="at", threshold=0.5)])
     return case, g
+
+
+TP06_VARS = ["cai", "casr", "cass", "nai", "Ki", "m", "h", "j", "xr1", "xr2",
+             "xs", "r", "s", "d", "f", "f2", "fcass", "rr", "oo"]
+CRN_VARS = ["nai", "ki", "cai", "caup", "carel", "m", "h", "j_", "d", "f",
+            "oa", "oi", "ua", "ui", "xr", "xs", "fca", "irel", "vrel", "urel",
+            "wrel"]
+MODEL_VARS["tp06"] = ["u"] + TP06_VARS
+MODEL_VARS["crn"] = ["u"] + CRN_VARS
+
+
+def tp06(dim):
+    """TP06 2D (anisotropic, fibrotic) or 3D (isotropic), current S1,
+    2000 steps, probes of u, m, cai, nai, Ki, casr every 10 steps."""
+    g = load("tp06")
+    if dim == 2:
+        case = dict(model="tp06", mesh=g["mesh2"], fibers=g["fib2"],
+                    stencil="aniso9", dt=0.01, dr=0.25, t_max=20,
+                    stims=[dict(kind="current", t=0, value=60, duration=1.0,
+                                box=[(0, 10), (0, 3)])],
+                    trackers=[dict(kind="probe", cells=[[4, 4]],
+                                   vars=["u", "m", "cai", "nai", "Ki", "casr"],
+                                   step=10)])
+    else:
+        case = dict(model="tp06", mesh=g["mesh3"], stencil="iso7", dt=0.01,
+                    dr=0.25, t_max=20,
+                    stims=[dict(kind="current", t=0, value=100, duration=1.0,
+                                box=[(0, 6), (0, 3), (0, 5)])],
+                    trackers=[dict(kind="probe", cells=[[3, 3, 2]],
+                                   vars=["u", "m", "cai", "nai", "Ki", "casr"],
+                                   step=10)])
+    gold = {v: g[f"d{dim}_{v}"] for v in MODEL_VARS["tp06"]}
+    gold.update({f"mv_{v}": g[f"d{dim}_mv_{v}"]
+                 for v in ["u", "m", "cai", "nai", "Ki", "casr"]})
+    return case, gold
+
+
+def courtemanche(dim):
+    """Courtemanche 2D (isotropic) or 3D (anisotropic), current S1, 2000
+    steps, probes of u, cai, nai, xs, xr, irel every 10 steps."""
+    g = load("courtemanche")
+    probe = dict(kind="probe", cells=[[4, 4]] if dim == 2 else [[3, 3, 2]],
+                 vars=["u", "cai", "nai", "xs", "xr", "irel"], step=10)
+    if dim == 2:
+        case = dict(model="crn", mesh=g["mesh2"], stencil="iso5", dt=0.01,
+                    dr=0.25, t_max=20,
+                    stims=[dict(kind="current", t=0, value=80, duration=1.0,
+                                box=[(0, 10), (0, 4)])],
+                    trackers=[probe])
+    else:
+        case = dict(model="crn", mesh=g["mesh3"], fibers=g["fib3"],
+                    stencil="aniso19", dt=0.01, dr=0.25, t_max=20,
+                    stims=[dict(kind="current", t=0, value=80, duration=1.0,
+                                box=[(0, 6), (0, 3), (0, 5)])],
+                    trackers=[probe])
+    gold = {v: g[f"d{dim}_{v}"] for v in MODEL_VARS["crn"]}
+    gold.update({f"mv_{v}": g[f"d{dim}_mv_{v}"] for v in probe["vars"]})
+    return case, gold

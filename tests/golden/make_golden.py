@@ -385,7 +385,7 @@ def case_tp06(fw):
             tissue.mesh = mesh3.copy()
             model = fw.TP063D()
             ss = fw.StimSequence()
-            ss.add_stim(fw.StimCurrentCoord3D(0, 60, 1.0, 0, 6, 0, 2, 0, 5))
+            ss.add_stim(fw.StimCurrentCoord3D(0, 100, 1.0, 0, 6, 0, 3, 0, 5))
         model.dt, model.dr, model.t_max = 0.01, 0.25, 20
         model.prog_bar = False
         model.cardiac_tissue = tissue
@@ -413,7 +413,8 @@ def case_tp06(fw):
 
 
 def case_courtemanche(fw):
-    """Courtemanche 2D/3D small tissues with a current S1."""
+    """Courtemanche 2D/3D small tissues with a current S1, probes of u,
+    Ca_i, Na_i and both potassium gates."""
     out = {}
     rng = np.random.default_rng(808)
     mesh2 = _fibrosis(rng, (10, 10), 0.1)
@@ -425,20 +426,31 @@ def case_courtemanche(fw):
             tissue = fw.CardiacTissue2D((10, 10))
             tissue.mesh = mesh2.copy()
             model = fw.Courtemanche2D()
-            ss.add_stim(fw.StimCurrentCoord2D(0, 40, 1.0, 0, 10, 0, 3))
+            ss.add_stim(fw.StimCurrentCoord2D(0, 80, 1.0, 0, 10, 0, 4))
         else:
             tissue = fw.CardiacTissue3D((6, 6, 5))
             tissue.mesh = mesh3.copy()
             tissue.fibers = fib3
             model = fw.Courtemanche3D()
-            ss.add_stim(fw.StimCurrentCoord3D(0, 40, 1.0, 0, 6, 0, 2, 0, 5))
+            ss.add_stim(fw.StimCurrentCoord3D(0, 80, 1.0, 0, 6, 0, 3, 0, 5))
         model.dt, model.dr, model.t_max = 0.01, 0.25, 20
         model.prog_bar = False
         model.cardiac_tissue = tissue
         model.stim_sequence = ss
+        tr = (fw.MultiVariable2DTracker() if dim == 2
+              else fw.MultiVariable3DTracker())
+        tr.cell_ind = [[4, 4]] if dim == 2 else [[3, 3, 2]]
+        tr.var_list = ["u", "cai", "nai", "xs", "xr", "irel"]
+        tr.step = 10
+        for var in tr.var_list:  # see case_tp06
+            if var not in model.__dict__:
+                setattr(model, var, None)
+        _attach(fw, model, [tr])
         model.run()
         for var in model.state_vars:
             out[f"d{dim}_{var}"] = getattr(model, var)
+        for var in tr.var_list:
+            out[f"d{dim}_mv_{var}"] = tr.output[var]
     out["mesh2"], out["mesh3"], out["fib3"] = mesh2, mesh3, fib3
     return out
 
