@@ -1,7 +1,8 @@
 """finitewave_gb300 -- Finitewave's explicit monodomain step on a GB300 GPU.
 
 Drop-in GPU versions of the reference's model classes (``AlievPanfilov2D``,
-``MitchellSchaeffer2D``, ``FentonKarma2D`` and their 3D variants) behind the
+``MitchellSchaeffer2D``, ``FentonKarma2D``, ``TP062D``,
+``Courtemanche2D`` and their 3D variants) behind the
 reference's own API: ``CardiacTissue2D/3D``, ``model.run()``,
 ``StimSequence`` with the coordinate / matrix / area stimuli,
 ``TrackerSequence`` with the activation-time, local-activation-time and
@@ -10,8 +11,9 @@ hand-written sm_103a CUDA (``libfwgpu.so``, C ABI in ``include/fwgpu.h``).
 """
 from .command import Command, CommandSequence
 from .model import (AlievPanfilov2D, AlievPanfilov3D, CardiacModel,
-                    FentonKarma2D, FentonKarma3D, MitchellSchaeffer2D,
-                    MitchellSchaeffer3D)
+                    Courtemanche2D, Courtemanche3D, FentonKarma2D,
+                    FentonKarma3D, MitchellSchaeffer2D, MitchellSchaeffer3D,
+                    TP062D, TP063D)
 from .state import StateLoader, StateSaver, StateSaverCollection
 from .stencil import (AsymmetricStencil2D, AsymmetricStencil3D,
                       IsotropicStencil2D, IsotropicStencil3D, Stencil)

@@ -7,6 +7,7 @@
 
 #include "fw_internal.cuh"
 #include "fw_model_dispatch.cuh"
+#include "fw_models_big.cuh"
 
 namespace fw {
 
@@ -41,6 +42,8 @@ Info model_info(int32_t model)
     case FW_MODEL_AP: return {ModelAP::NS, ModelAP::NP};
     case FW_MODEL_MS: return {ModelMS::NS, ModelMS::NP};
     case FW_MODEL_FK: return {ModelFK::NS, ModelFK::NP};
+    case FW_MODEL_TP06: return {ModelTP06::NS, ModelTP06::NP};
+    case FW_MODEL_CRN: return {ModelCRN::NS, ModelCRN::NP};
     }
     return {-1, -1};
 }
@@ -177,9 +180,10 @@ int fw_model_info(int32_t model, int32_t *n_state, int32_t *n_params)
 
 int fw_state_is_f64(int32_t model, int32_t precision, int32_t index)
 {
-    (void)index;
     if (precision == FW_F64) return 1;
     switch (model) {
+    case FW_MODEL_TP06: return fw::ModelTP06::is_conc(index) ? 1 : 0;
+    case FW_MODEL_CRN: return fw::ModelCRN::is_conc(index) ? 1 : 0;
     default: return 0;
     }
 }

@@ -142,4 +142,18 @@ int step_fused_ms(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 int step_fused_fk(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                   cudaStream_t stream);
 
+// Detailed models, one translation unit per model x precision
+// (fw_step_detailed_*.cu).
+#define FW_DECLARE_DETAILED(NAME)                                             \
+    int plain_##NAME(const fw_step_args *a, int64_t n_begin, int64_t n_steps, \
+                     cudaStream_t stream);                                    \
+    int ionic_##NAME(void *u_new, const void *u, void *const *state,          \
+                     const int64_t *idx, int64_t n_idx, double dt,            \
+                     const double *params, cudaStream_t stream);
+FW_DECLARE_DETAILED(tp06_f64)
+FW_DECLARE_DETAILED(tp06_f32)
+FW_DECLARE_DETAILED(crn_f64)
+FW_DECLARE_DETAILED(crn_f32)
+#undef FW_DECLARE_DETAILED
+
 }  // namespace fw

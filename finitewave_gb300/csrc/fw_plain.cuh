@@ -1,0 +1,377 @@
+// fw_plain.cuh -- kernels and host loop of the plain form of the monodomain
+// step (one launch per time step) and of the stand-alone ionic pass, as
+// templates over the model M, the stencil ST and the precision T.  Each
+// translation unit that instantiates them picks its own FMA policy: the
+// float64 path of the reference's +,-,*,/-only models is compiled with
+// --fmad=false so that it is bitwise the reference's.
+//
+// Per time step n (core/model/cardiac_model.py:164-178):
+//   1. k_stim      once per stimulus whose step window contains n, on u_cur
+//   2. k_step      all nodes: trackers read u_cur (after stimuli, before the
+//                  update, as tracker_next does after the kernels but before
+//                  the swap); myocytes get u_nxt = diffusion + ionic
+//   3. k_probe     when a probe tracker is active at n: u_cur and the state
+//                  variables (already advanced, as the reference's trackers
+//                  see them)
+//   the caller's buffers then swap roles.
+#pragma once
+
+#include "fw_internal.cuh"
+#include "fw_models.cuh"
+
+namespace fw {
+namespace {
+
+
+constexpr int kThreads = 256;
+
+template <class T>
+struct StimK {
+    const int8_t *mesh;
+    const int8_t *mask;
+    T *u;
+    int64_t lo[3], ext[3];
+    int64_t stride[3];
+    int64_t count;
+    double value, u_max;
+    int kind, has_umax;
+};
+
+// StimVoltage*/StimCurrent* .stimulate (cpuwave2D/stimulation/*.py) over the
+// stimulus box, restricted to mesh == 1 and the optional mask.
+template <class T>
+__global__ void k_stim(StimK<T> s)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+         t < s.count; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c2 = t % s.ext[2];
+        int64_t r = t / s.ext[2];
+        int64_t c1 = r % s.ext[1];
+        int64_t c0 = r / s.ext[1];
+        int64_t p = (s.lo[0] + c0) * s.stride[0] + (s.lo[1] + c1) * s.stride[1] +
+                    (s.lo[2] + c2) * s.stride[2];
+        if (s.mesh[p] != 1) continue;
+        if (s.mask && !s.mask[p]) continue;
+        if (s.kind == FW_STIM_VOLTAGE) {
+            s.u[p] = (T)s.value;
+        } else {
+            T x = s.u[p] + (T)s.value;
+            if (s.has_umax && x > (T)s.u_max) x = (T)s.u_max;
+            s.u[p] = x;
+        }
+    }
+}
+
+struct AtK {
+    double thr;
+    int32_t *act;
+};
+
+struct LatK {
+    double thr;
+    uint8_t *activated;
+    int32_t *steps;
+    int32_t *count;
+    int32_t cap;
+};
+
+template <class T>
+struct StepK {
+    const int8_t *myo;
+    const T *w;
+    const T *u;
+    T *un;
+    void *state[FW_MAX_STATE];
+    double params[FW_MAX_PARAMS];
+    double dt;
+    int64_t n, si, sj;
+    int64_t step;
+    int32_t n_at, n_lat;
+    AtK at[FW_MAX_AT];
+    LatK lat[FW_MAX_LAT];
+    int32_t *status;
+};
+
+template <class T>
+__device__ __forceinline__ void track(const StepK<T> &k, int64_t p, T uc)
+{
+    for (int a = 0; a < k.n_at; ++a) {
+        // (act_t < 0) & (u > threshold)  (activation_time_2d_tracker.py:61-63)
+        if (uc > (T)k.at[a].thr && k.at[a].act[p] < 0)
+            k.at[a].act[p] = (int32_t)k.step;
+    }
+    for (int l = 0; l < k.n_lat; ++l) {
+        // cross_threshold (local_activation_time_2d_tracker.py:71-89)
+        const LatK &L = k.lat[l];
+        uint8_t act = L.activated[p];
+        if (uc >= (T)L.thr && !act) {
+            L.activated[p] = 1;
+            int32_t c = L.count[p];
+            if (c < L.cap)
+                L.steps[(int64_t)c * k.n + p] = (int32_t)k.step;
+            else if (k.status)
+                atomicOr(k.status, FW_DEV_LAT_OVERFLOW);
+            L.count[p] = c + 1;
+        } else if (uc < (T)L.thr && act) {
+            L.activated[p] = 0;
+        }
+    }
+}
+
+template <class M, int ST, class T>
+__global__ void __launch_bounds__(kThreads) k_step(StepK<T> k)
+{
+    const Params<T, M::NP> P = load_params<T, M::NP>(k.params);
+    const T dt = (T)k.dt;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < k.n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        T uc = k.u[p];
+        if (k.n_at | k.n_lat) track(k, p, uc);
+        if (!k.myo[p]) continue;
+        T un = diffuse_node<ST, T>(k.u, k.w, p, k.n, k.si, k.sj);
+        auto st = M::template load<T>(k.state, p);
+        un = M::template update<T>(uc, un, st, P, dt);
+        M::template store<T>(k.state, p, st);
+        k.un[p] = un;
+    }
+}
+
+struct ProbeOne {
+    const int64_t *cells;
+    double *out;
+    int64_t sample;
+    int64_t capacity;
+    int32_t n_cells, n_vars;
+    int32_t var_ids[FW_MAX_PROBE_VARS];
+};
+
+template <class T>
+struct ProbeK {
+    const T *u;
+    void *state[FW_MAX_STATE];
+    uint32_t f64_mask;
+    int32_t n;
+    ProbeOne pr[FW_MAX_PROBE];
+    int32_t *status;
+};
+
+template <class T>
+__global__ void k_probe(ProbeK<T> k)
+{
+    for (int t = 0; t < k.n; ++t) {
+        const ProbeOne &P = k.pr[t];
+        if (P.sample >= P.capacity) {
+            if (threadIdx.x == 0 && k.status)
+                atomicOr(k.status, FW_DEV_PROBE_OVERFLOW);
+            continue;
+        }
+        int total = P.n_cells * P.n_vars;
+        for (int q = threadIdx.x; q < total; q += blockDim.x) {
+            int v = q / P.n_cells, c = q % P.n_cells;
+            int64_t p = P.cells[c];
+            int id = P.var_ids[v];
+            double x;
+            if (id == 0)
+                x = (double)k.u[p];
+            else if ((k.f64_mask >> (id - 1)) & 1u)
+                x = ((const double *)k.state[id - 1])[p];
+            else
+                x = (double)((const T *)k.state[id - 1])[p];
+            P.out[(P.sample * P.n_vars + v) * (int64_t)P.n_cells + c] = x;
+        }
+    }
+}
+
+template <int ST, class T>
+__global__ void k_diffuse(T *un, const T *u, const T *w, const int64_t *idx,
+                          int64_t n_idx, int64_t n, int64_t si, int64_t sj)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_idx;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p = idx[t];
+        un[p] = diffuse_node<ST, T>(u, w, p, n, si, sj);
+    }
+}
+
+template <class M, class T>
+struct IonicK {
+    T *un;
+    const T *u;
+    void *state[FW_MAX_STATE];
+    double params[FW_MAX_PARAMS];
+    double dt;
+    const int64_t *idx;
+    int64_t n_idx;
+};
+
+template <class M, class T>
+__global__ void k_ionic(IonicK<M, T> k)
+{
+    const Params<T, M::NP> P = load_params<T, M::NP>(k.params);
+    const T dt = (T)k.dt;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+         t < k.n_idx; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p = k.idx[t];
+        auto st = M::template load<T>(k.state, p);
+        k.un[p] = M::template update<T>(k.u[p], k.un[p], st, P, dt);
+        M::template store<T>(k.state, p, st);
+    }
+}
+
+bool in_window(const fw_window &w, int64_t n)
+{
+    return w.stride > 0 && n >= w.first && n <= w.last && n % w.stride == 0;
+}
+
+template <class T>
+int launch_stim(const fw_step_args *a, const fw_stim &s, T *u,
+                cudaStream_t stream)
+{
+    StimK<T> k;
+    int dim = stencil_dim(a->stencil);
+    Grid g = make_grid(a->ni, a->nj, a->nk, dim);
+    int64_t shape[3] = {g.ni, g.nj, g.nk};
+    k.mesh = a->mesh;
+    k.mask = s.mask;
+    k.u = u;
+    k.count = 1;
+    for (int d = 0; d < 3; ++d) {
+        int64_t lo = d < dim ? s.lo[d] : 0, hi = d < dim ? s.hi[d] : 1;
+        if (lo < 0) lo = 0;
+        if (hi > shape[d]) hi = shape[d];
+        if (hi <= lo) return FW_OK;
+        k.lo[d] = lo;
+        k.ext[d] = hi - lo;
+        k.count *= hi - lo;
+    }
+    k.stride[0] = g.si;
+    k.stride[1] = dim == 2 ? 1 : g.sj;
+    k.stride[2] = 1;
+    k.value = s.value;
+    k.u_max = s.u_max;
+    k.kind = s.kind;
+    k.has_umax = s.has_umax;
+    k_stim<T><<<grid_for(k.count, kThreads), kThreads, 0, stream>>>(k);
+    FW_CHECK_LAUNCH("k_stim");
+    return FW_OK;
+}
+
+template <class M, int ST, class T>
+int run_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+              cudaStream_t stream)
+{
+    int dim = stencil_dim(ST);
+    Grid g = make_grid(a->ni, a->nj, a->nk, dim);
+    StepK<T> k;
+    k.myo = a->myo;
+    k.w = (const T *)a->weights;
+    for (int i = 0; i < FW_MAX_STATE; ++i) k.state[i] = a->state[i];
+    for (int i = 0; i < FW_MAX_PARAMS; ++i) k.params[i] = a->params[i];
+    k.dt = a->dt;
+    k.n = g.n;
+    k.si = g.si;
+    k.sj = g.sj;
+    k.status = a->status;
+
+    ProbeK<T> pk;
+    pk.status = a->status;
+    for (int i = 0; i < FW_MAX_STATE; ++i) pk.state[i] = a->state[i];
+    pk.f64_mask = 0;
+    for (int i = 0; i < M::NS; ++i)
+        if (fw_state_is_f64(a->model, a->precision, i)) pk.f64_mask |= 1u << i;
+
+    const int blocks = grid_for(g.n, kThreads, 152 * 8);
+    for (int64_t s = 0; s < n_steps; ++s) {
+        const int64_t n = n_begin + s;
+        T *cur = (T *)a->u[s & 1];
+        T *nxt = (T *)a->u[(s + 1) & 1];
+        for (int i = 0; i < a->n_stims; ++i) {
+            const fw_stim &st = a->stims[i];
+            if (n >= st.first && n <= st.last) {
+                int rc = launch_stim<T>(a, st, cur, stream);
+                if (rc) return rc;
+            }
+        }
+        k.u = cur;
+        k.un = nxt;
+        k.step = n;
+        k.n_at = 0;
+        for (int i = 0; i < a->n_at; ++i)
+            if (in_window(a->at[i].win, n))
+                k.at[k.n_at++] = AtK{a->at[i].threshold, a->at[i].act_step};
+        k.n_lat = 0;
+        for (int i = 0; i < a->n_lat; ++i)
+            if (in_window(a->lat[i].win, n)) {
+                const fw_lat_tracker &L = a->lat[i];
+                k.lat[k.n_lat++] = LatK{L.threshold, L.activated,
+                                        L.cross_steps, L.cross_count,
+                                        L.capacity};
+            }
+        k_step<M, ST, T><<<blocks, kThreads, 0, stream>>>(k);
+        FW_CHECK_LAUNCH("k_step");
+        pk.n = 0;
+        for (int i = 0; i < a->n_probe; ++i) {
+            const fw_probe_tracker &P = a->probe[i];
+            if (!in_window(P.win, n)) continue;
+            ProbeOne &o = pk.pr[pk.n++];
+            o.cells = P.cells;
+            o.out = P.out;
+            o.sample = P.sample_offset + (n - P.win.first) / P.win.stride;
+            o.capacity = P.capacity;
+            o.n_cells = P.n_cells;
+            o.n_vars = P.n_vars;
+            for (int v = 0; v < FW_MAX_PROBE_VARS; ++v) o.var_ids[v] = P.var_ids[v];
+        }
+        if (pk.n) {
+            pk.u = cur;
+            k_probe<T><<<1, 128, 0, stream>>>(pk);
+            FW_CHECK_LAUNCH("k_probe");
+        }
+    }
+    return FW_OK;
+}
+
+template <class M, class T>
+int run_ionic(void *u_new, const void *u, void *const *state,
+              const int64_t *idx, int64_t n_idx, double dt,
+              const double *params, cudaStream_t stream)
+{
+    IonicK<M, T> k;
+    k.un = (T *)u_new;
+    k.u = (const T *)u;
+    for (int i = 0; i < FW_MAX_STATE; ++i) k.state[i] = i < M::NS ? state[i] : nullptr;
+    for (int i = 0; i < FW_MAX_PARAMS; ++i) k.params[i] = i < M::NP ? params[i] : 0.0;
+    k.dt = dt;
+    k.idx = idx;
+    k.n_idx = n_idx;
+    if (n_idx > 0) k_ionic<M, T><<<grid_for(n_idx, kThreads), kThreads, 0, stream>>>(k);
+    FW_CHECK_LAUNCH("k_ionic");
+    return FW_OK;
+}
+
+struct PlainDispatch {
+    const fw_step_args *a;
+    int64_t n_begin, n_steps;
+    cudaStream_t stream;
+    template <class M, int ST, class T>
+    int run() const { return run_plain<M, ST, T>(a, n_begin, n_steps, stream); }
+};
+
+struct IonicDispatch {
+    void *u_new;
+    const void *u;
+    void *const *state;
+    const int64_t *idx;
+    int64_t n_idx;
+    double dt;
+    const double *params;
+    cudaStream_t stream;
+    template <class M, class T>
+    int run() const
+    {
+        return run_ionic<M, T>(u_new, u, state, idx, n_idx, dt, params, stream);
+    }
+};
+
+}  // namespace
+}  // namespace fw

@@ -81,6 +81,7 @@ class CardiacModel:
     _state_names = ()
     _param_names = ()
     _reset_u_new = False
+    _init_names = {}   # state variable -> suffix of its init_* attribute
 
     u = _StateVar("u")
     u_new = _StateVar("u_new")
@@ -192,7 +193,8 @@ class CardiacModel:
             self._dev["u_new"].copy_(self._dev["u"])
         for i, name in enumerate(self._state_names):
             t = torch.empty(shape, dtype=self._torch_dtype(i), device=dev)
-            t.fill_(float(getattr(self, "init_" + name)))
+            t.fill_(float(getattr(
+                self, "init_" + self._init_names.get(name, name))))
             self._dev[name] = t
 
     def compute_weights(self):
@@ -600,6 +602,135 @@ class FentonKarma2D(CardiacModel):
 
 class FentonKarma3D(FentonKarma2D):
     """(cpuwave3D/model/fenton_karma_3d.py)"""
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_3d(cardiac_tissue)
+
+
+class TP062D(CardiacModel):
+    """ten Tusscher-Panfilov 2006 epicardial model (cpuwave2D/model/
+    tp06_2d.py:10-240).  Parameters in the order of ionic_kernel_2d's
+    signature (:1003-1012), defaults from :81-148, initial values :151-170.
+    Under npfloat float32 the ion concentrations (cai, casr, cass, nai, Ki)
+    stay float64; the reference's frozen Ca_i (:1098) is kept."""
+
+    _model_id = _ffi.MODEL_TP06
+    _reset_u_new = True
+    _state_names = ("cai", "casr", "cass", "nai", "Ki", "m", "h", "j", "xr1",
+                    "xr2", "xs", "r", "s", "d", "f", "f2", "fcass", "rr",
+                    "oo")
+    _param_names = ("ko", "cao", "nao", "Vc", "Vsr", "Vss", "Bufc", "Kbufc",
+                    "Bufsr", "Kbufsr", "Bufss", "Kbufss", "Vmaxup", "Kup",
+                    "Vrel", "k1_", "k2_", "k3", "k4", "EC", "maxsr", "minsr",
+                    "Vleak", "Vxfer", "R", "F", "T", "RTONF", "CAPACITANCE",
+                    "gkr", "pKNa", "gk1", "gna", "gbna", "KmK", "KmNa",
+                    "knak", "gcal", "gbca", "knaca", "KmNai", "KmCa", "ksat",
+                    "n_", "gpca", "KpCa", "gpk", "gto", "gks")
+
+    def __init__(self):
+        super().__init__()
+        self.D_model = 0.154
+        self.state_vars = ["u"] + list(self._state_names)
+        self.npfloat = "float64"
+        self.ko, self.cao, self.nao = 5.4, 2.0, 140.0
+        self.Vc, self.Vsr, self.Vss = 0.016404, 0.001094, 0.00005468
+        self.Bufc, self.Kbufc = 0.2, 0.001
+        self.Bufsr, self.Kbufsr = 10.0, 0.3
+        self.Bufss, self.Kbufss = 0.4, 0.00025
+        self.Vmaxup, self.Kup, self.Vrel = 0.006375, 0.00025, 0.102
+        self.k1_, self.k2_, self.k3, self.k4 = 0.15, 0.045, 0.060, 0.005
+        self.EC, self.maxsr, self.minsr = 1.5, 2.5, 1.0
+        self.Vleak, self.Vxfer = 0.00036, 0.0038
+        self.R, self.F, self.T = 8314.472, 96485.3415, 310.0
+        self.RTONF = 26.71376
+        self.CAPACITANCE = 0.185
+        self.gkr, self.pKNa, self.gk1, self.gna = 0.153, 0.03, 5.405, 14.838
+        self.gbna, self.KmK, self.KmNa, self.knak = 0.00029, 1.0, 40.0, 2.724
+        self.gcal, self.gbca, self.knaca = 0.00003980, 0.000592, 1000
+        self.KmNai, self.KmCa, self.ksat, self.n_ = 87.5, 1.38, 0.1, 0.35
+        self.gpca, self.KpCa, self.gpk = 0.1238, 0.0005, 0.0146
+        self.gto, self.gks = 0.294, 0.392
+        self.init_u = -84.5
+        self.init_cai, self.init_casr, self.init_cass = 0.00007, 1.3, 0.00007
+        self.init_nai, self.init_Ki = 7.67, 138.3
+        self.init_m, self.init_h, self.init_j = 0.0, 0.75, 0.75
+        self.init_xr1, self.init_xr2, self.init_xs = 0.0, 1.0, 0.0
+        self.init_r, self.init_s, self.init_d = 0.0, 1.0, 0.0
+        self.init_f, self.init_f2, self.init_fcass = 1.0, 1.0, 1.0
+        self.init_rr, self.init_oo = 1.0, 0.0
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_2d(cardiac_tissue)
+
+
+class TP063D(TP062D):
+    """(cpuwave3D/model/tp06_3d.py:36-83)"""
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_3d(cardiac_tissue)
+
+
+class Courtemanche2D(CardiacModel):
+    """Courtemanche-Ramirez-Nattel 1998 atrial model (cpuwave2D/model/
+    courtemanche_2d.py:10-178).  Parameters in the order of
+    ionic_kernel_2d's signature (:569-577), defaults :32-83, initial values
+    :85-106.  Under npfloat float32 the concentrations (nai, ki, cai, caup,
+    carel) stay float64.  As in the reference, the model's ``xs`` array
+    holds the IKr gate and ``xr`` the IKs gate (:152-160 against :581), and
+    IKr uses the fixed conductance 0.0294 (:420-422) whatever ``gkr`` is."""
+
+    _model_id = _ffi.MODEL_CRN
+    _reset_u_new = True
+    _state_names = ("nai", "ki", "cai", "caup", "carel", "m", "h", "j_", "d",
+                    "f", "oa", "oi", "ua", "ui", "xr", "xs", "fca", "irel",
+                    "vrel", "urel", "wrel")
+    _init_names = {"j_": "j"}
+    _param_names = ("gna", "gnab", "gk1", "gkr", "gks", "gto", "gcal", "gcab",
+                    "gkur_coeff", "F", "T", "R", "Vc", "Vj", "Vup", "Vrel",
+                    "ibk", "cao", "nao", "ko", "caupmax", "kup", "kmnai",
+                    "kmko", "kmnancx", "kmcancx", "ksatncx", "kmcmdn",
+                    "kmtrpn", "kmcsqn", "trpnmax", "cmdnmax", "csqnmax",
+                    "inacamax", "inakmax", "ipcamax", "krel", "iupmax",
+                    "kq10")
+
+    def __init__(self):
+        super().__init__()
+        self.D_model = 0.154
+        self.state_vars = ["u"] + list(self._state_names)
+        self.npfloat = "float64"
+        self.gna, self.gnab, self.gk1 = 7.8, 0.000674, 0.09
+        self.gkr, self.gks, self.gto = 0.0294, 0.129, 0.1652
+        self.gcal, self.gcab, self.gkur_coeff = 0.1238, 0.00113, 1
+        self.F, self.T, self.R = 96485.0, 310.0, 8314.0
+        self.Vc = 20100
+        self.Vj = self.Vc * 0.68
+        self.Vup = self.Vj * 0.06 * 0.92
+        self.Vrel = self.Vj * 0.06 * 0.08
+        self.ibk, self.cao, self.nao, self.ko = 0.0, 1.8, 140, 5.4
+        self.caupmax, self.kup = 15, 0.00092
+        self.kmnai, self.kmko = 10, 1.5
+        self.kmnancx, self.kmcancx, self.ksatncx = 87.5, 1.38, 0.1
+        self.kmcmdn, self.kmtrpn, self.kmcsqn = 0.00238, 0.0005, 0.8
+        self.trpnmax, self.cmdnmax, self.csqnmax = 0.07, 0.05, 10.0
+        self.inacamax, self.inakmax, self.ipcamax = 1600, 0.6, 0.275
+        self.krel, self.iupmax, self.kq10 = 30, 0.005, 3
+        self.init_u = -84.5
+        self.init_nai, self.init_ki, self.init_cai = 11.2, 139, 0.000102
+        self.init_caup, self.init_carel = 1.6, 1.1
+        self.init_m, self.init_h, self.init_j = 0.00291, 0.965, 0.978
+        self.init_d, self.init_f = 0.000137, 0.999837
+        self.init_oa, self.init_oi = 0.000592, 0.9992
+        self.init_ua, self.init_ui = 0.003519, 0.9987
+        self.init_xs, self.init_xr, self.init_fca = 0.0187, 0.0000329, 0.775
+        self.init_irel, self.init_vrel = 0, 1
+        self.init_urel, self.init_wrel = 0, 0.9
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_2d(cardiac_tissue)
+
+
+class Courtemanche3D(Courtemanche2D):
+    """(cpuwave3D/model/courtemanche_3d.py:40-88)"""
 
     def select_stencil(self, cardiac_tissue):
         return _stencil_3d(cardiac_tissue)

@@ -20,8 +20,10 @@ def _stream():
 
 
 def _dev_f64(a, device):
-    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64),
-                           device=device)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if not a.flags.writeable:
+        a = a.copy()
+    return torch.as_tensor(a, device=device)
 
 
 class Stencil:

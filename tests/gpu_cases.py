@@ -5,7 +5,9 @@ import finitewave_gb300 as fg
 
 _MODELS = {("ap", 2): fg.AlievPanfilov2D, ("ap", 3): fg.AlievPanfilov3D,
            ("ms", 2): fg.MitchellSchaeffer2D, ("ms", 3): fg.MitchellSchaeffer3D,
-           ("fk", 2): fg.FentonKarma2D, ("fk", 3): fg.FentonKarma3D}
+           ("fk", 2): fg.FentonKarma2D, ("fk", 3): fg.FentonKarma3D,
+           ("tp06", 2): fg.TP062D, ("tp06", 3): fg.TP063D,
+           ("crn", 2): fg.Courtemanche2D, ("crn", 3): fg.Courtemanche3D}
 
 
 def register(name, cls2d, cls3d):

@@ -43,6 +43,8 @@ def test_version_and_model_info(lib):
     assert lib.fw_version() >= 100
     assert _ffi.model_info(_ffi.MODEL_AP) == (1, 5)
     assert _ffi.model_info(_ffi.MODEL_FK) == (2, 11)
+    assert _ffi.model_info(_ffi.MODEL_TP06) == (19, 49)
+    assert _ffi.model_info(_ffi.MODEL_CRN) == (21, 39)
     with pytest.raises(_ffi.FwError) as e:
         _ffi.model_info(99)
     assert e.value.code == _ffi.FW_ERR_UNSUPPORTED
@@ -177,3 +179,22 @@ def test_lat_layer_reconstruction():
     out = tr.output
     assert out.shape == (len(act), *shape)
     assert np.array_equal(out, np.array(act).reshape(len(act), *shape))
+
+
+def test_detailed_model_layout(lib):
+    """TP06 / Courtemanche: state and parameter lists agree with the
+    library's counts, and under float32 exactly the ion concentrations are
+    float64 arrays."""
+    import finitewave_gb300 as fg
+    from finitewave_gb300 import _ffi
+    conc = {fg.TP062D: {"cai", "casr", "cass", "nai", "Ki"},
+            fg.Courtemanche2D: {"nai", "ki", "cai", "caup", "carel"}}
+    for cls, names in conc.items():
+        m = cls()
+        ns, npar = _ffi.model_info(m._model_id)
+        assert (len(m._state_names), len(m._param_names)) == (ns, npar)
+        for i, name in enumerate(m._state_names):
+            assert _ffi.state_is_f64(m._model_id, _ffi.F64, i) == 1
+            assert _ffi.state_is_f64(m._model_id, _ffi.F32, i) == \
+                (name in names), name
+        assert m.state_vars == ["u"] + list(m._state_names)
