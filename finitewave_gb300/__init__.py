@@ -9,6 +9,7 @@ reference's own API: ``CardiacTissue2D/3D``, ``model.run()``,
 probe trackers, commands and state save / load.  The per-step work runs in
 hand-written sm_103a CUDA (``libfwgpu.so``, C ABI in ``include/fwgpu.h``).
 """
+from .batch import TissueBatch
 from .command import Command, CommandSequence
 from .model import (AlievPanfilov2D, AlievPanfilov3D, CardiacModel,
                     Courtemanche2D, Courtemanche3D, FentonKarma2D,

@@ -30,6 +30,7 @@ UNITS = {
     "fw_weights.cu": ["--fmad=false"],
     "fw_step.cu": ["--fmad=false"],
     "fw_fused.cu": [],
+    "fw_batch.cu": ["--prec-div=false", "--ftz=true"],
     "fw_fused_ap.cu": ["--prec-div=false", "--ftz=true"],
     "fw_fused_ms.cu": ["--prec-div=false", "--ftz=true"],
     "fw_fused_fk.cu": ["--prec-div=false", "--ftz=true"],

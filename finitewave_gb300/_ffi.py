@@ -82,6 +82,11 @@ class StepArgs(ctypes.Structure):
                 ("fused_variant", _i32), ("weights_packed", _vp)]
 
 
+class Batch(ctypes.Structure):
+    _fields_ = [("plan", _vp), ("n_tissues", _i32), ("n_tiles", _i32),
+                ("ksteps", _i32), ("grid", _i32)]
+
+
 class FwError(RuntimeError):
     """A non-OK status from libfwgpu."""
 
@@ -109,11 +114,16 @@ _SIGS = {
                  _i32),
     "fw_step": ([ctypes.POINTER(StepArgs), _i64, _i64, _vp], _i32),
     "fw_pack_weights": ([_i32, _vp, _i64, _vp, _vp], _i32),
+    "fw_batch_plan_size": ([_vp, _i32, ctypes.POINTER(_i64)], _i32),
+    "fw_batch_plan": ([_vp, _i32, _vp, _vp, _i64, ctypes.POINTER(Batch),
+                       _vp], _i32),
+    "fw_batch_scratch_size": ([ctypes.POINTER(_i64)], _i32),
+    "fw_batch_run": ([ctypes.POINTER(Batch), _vp, _i64, _i64, _vp], _i32),
 }
 
 # symbol -> ctypes structure whose size must match the library's
 _STRUCTS = {0: StepArgs, 1: Stim, 2: AtTracker, 3: LatTracker,
-            4: ProbeTracker, 5: Window}
+            4: ProbeTracker, 5: Window, 6: Batch}
 
 
 def load(path=None):

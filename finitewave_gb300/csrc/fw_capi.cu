@@ -158,6 +158,7 @@ size_t fw_struct_size(int32_t which)
     case 3: return sizeof(fw_lat_tracker);
     case 4: return sizeof(fw_probe_tracker);
     case 5: return sizeof(fw_window);
+    case 6: return sizeof(fw_batch);
     }
     return 0;
 }
@@ -244,6 +245,37 @@ int fw_step(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     if (a->form == FW_FORM_FUSED)
         return fw::step_fused(a, n_begin, n_steps, (cudaStream_t)stream);
     return fw::step_plain(a, n_begin, n_steps, (cudaStream_t)stream);
+}
+
+int fw_batch_plan_size(const fw_step_args *const *tissues, int32_t n,
+                       int64_t *plan_bytes)
+{
+    return fw::batch_plan_size(tissues, n, plan_bytes);
+}
+
+int fw_batch_plan(const fw_step_args *const *tissues, int32_t n,
+                  const int64_t *n_begin, void *plan, int64_t plan_bytes,
+                  fw_batch *out, void *stream)
+{
+    return fw::batch_plan(tissues, n, n_begin, plan, plan_bytes, out,
+                          (cudaStream_t)stream);
+}
+
+int fw_batch_scratch_size(int64_t *bytes)
+{
+    if (!bytes) {
+        fw::set_error("fw_batch_scratch_size: NULL output");
+        return FW_ERR_ARG;
+    }
+    *bytes = fw::kBatchScratchBytes;
+    return FW_OK;
+}
+
+int fw_batch_run(const fw_batch *b, void *scratch, int64_t offset,
+                 int64_t n_steps, void *stream)
+{
+    return fw::batch_run(b, (uint32_t *)scratch, offset, n_steps,
+                         (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -142,6 +142,15 @@ int step_fused_ms(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 int step_fused_fk(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                   cudaStream_t stream);
 
+int batch_plan_size(const fw_step_args *const *tissues, int32_t n,
+                    int64_t *bytes);
+int batch_plan(const fw_step_args *const *tissues, int32_t n,
+               const int64_t *n_begin, void *plan, int64_t plan_bytes,
+               fw_batch *out, cudaStream_t stream);
+int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
+              int64_t n_steps, cudaStream_t stream);
+constexpr int64_t kBatchScratchBytes = 256;
+
 // Detailed models, one translation unit per model x precision
 // (fw_step_detailed_*.cu).
 #define FW_DECLARE_DETAILED(NAME)                                             \

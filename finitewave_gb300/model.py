@@ -381,6 +381,18 @@ class CardiacModel:
         """Advance up to `limit` steps on the device (one fw_step call);
         returns the number of steps taken.  With sync=False the device
         status word is not read back (no host synchronisation)."""
+        seg = self._prepare_segment(limit)
+        stream = torch.cuda.current_stream().cuda_stream
+        _ffi.call("fw_step", ctypes.byref(seg.args), seg.n0, seg.n_seg,
+                  stream)
+        if sync:
+            self._check_status()
+        self._finish_segment(seg)
+        return seg.n_seg
+
+    def _prepare_segment(self, limit):
+        """The fw_step_args of the next segment of at most `limit` steps
+        (stimulus and tracker windows in global step indices)."""
         ts, t_end, n_seg = self._segment_times(limit)
         n0 = int(self.step)
         self._t_hist.append(ts)
@@ -481,17 +493,27 @@ class CardiacModel:
                                     "finitewave_gb300 tracker")
         a.n_at, a.n_lat, a.n_probe = n_at, n_lat, n_pr
         a.status = self._status.data_ptr()
-        stream = torch.cuda.current_stream().cuda_stream
-        _ffi.call("fw_step", ctypes.byref(a), n0, n_seg, stream)
-        if sync:
-            self._check_status()
-        del keep
-        if n_seg % 2 == 1:
+        return _Segment(a, n0, n_seg, t_end, keep)
+
+    def _finish_segment(self, seg):
+        """Account for a segment the device has been given: swap u / u_new
+        after an odd step count, advance t and step."""
+        if seg.n_seg % 2 == 1:
             self._dev["u"], self._dev["u_new"] = (self._dev["u_new"],
                                                   self._dev["u"])
-        self.t = t_end
-        self.step = n0 + n_seg
-        return n_seg
+        self.t = seg.t_end
+        self.step = seg.n0 + seg.n_seg
+
+
+class _Segment:
+    """One segment's fw_step_args and bookkeeping (`keep` holds host-side
+    objects whose device memory the args point to)."""
+
+    __slots__ = ("args", "n0", "n_seg", "t_end", "keep")
+
+    def __init__(self, args, n0, n_seg, t_end, keep):
+        self.args, self.n0, self.n_seg = args, n0, n_seg
+        self.t_end, self.keep = t_end, keep
 
 
 # ------------------------------------------------------------------ models

@@ -197,12 +197,23 @@ typedef struct fw_step_args {
                                    when not available                       */
 } fw_step_args;
 
+/* A planned batch of tissues (fw_batch_plan).  Host-side handle; the
+ * device data lives in the caller's plan buffer. */
+typedef struct fw_batch {
+    void *plan;          /* device plan buffer given to fw_batch_plan        */
+    int32_t n_tissues;
+    int32_t n_tiles;     /* fused regions over all tissues                   */
+    int32_t ksteps;      /* time steps per launch                            */
+    int32_t grid;        /* persistent CTAs per launch                       */
+} fw_batch;
+
 /* Library version (major*10000 + minor*100 + patch). */
 FW_API int fw_version(void);
 
 /* sizeof of the ABI structs as compiled into the library, so a binding can
  * check its own layout: which = 0 fw_step_args, 1 fw_stim, 2 fw_at_tracker,
- * 3 fw_lat_tracker, 4 fw_probe_tracker, 5 fw_window.  0 for unknown. */
+ * 3 fw_lat_tracker, 4 fw_probe_tracker, 5 fw_window, 6 fw_batch.  0 for
+ * unknown. */
 FW_API size_t fw_struct_size(int32_t which);
 
 /* Number of kernels this library has launched in the process so far
@@ -266,6 +277,41 @@ FW_API int fw_pack_weights(int32_t stencil, const float *w, int64_t n,
  * step counter).  On return the current u is a->u[n_steps & 1]. */
 FW_API int fw_step(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
             void *stream);
+
+/* ---- batches of tissues (no single reference counterpart: the reference
+ * runs one CardiacModel.run loop per tissue, core/model/cardiac_model.py:
+ * 130-189; a batch advances many such runs together) -------------------- */
+
+/* Device bytes of the plan for these tissues.  Each tissue is an
+ * fw_step_args as for fw_step with: a 2D grid, FW_F32, model AP / MS / FK,
+ * stencil ISO5 / ANISO9, at most one activation tracker and one local
+ * activation tracker, no probe tracker, and u[0], u[1] equal at
+ * non-myocytes.  Tissues may differ in size, model, stencil, parameters,
+ * stimuli and trackers. */
+FW_API int fw_batch_plan_size(const fw_step_args *const *tissues, int32_t n,
+                              int64_t *plan_bytes);
+
+/* Build the device plan (descriptor table and tile list) in `plan`
+ * (16-byte aligned device memory of at least fw_batch_plan_size bytes) and
+ * fill *out.  n_begin[i] is tissue i's global step at batch offset 0 (its
+ * stimulus and tracker windows are in its own step numbering).  Copies the
+ * plan synchronously on `stream`. */
+FW_API int fw_batch_plan(const fw_step_args *const *tissues, int32_t n,
+                         const int64_t *n_begin, void *plan,
+                         int64_t plan_bytes, fw_batch *out, void *stream);
+
+/* Device bytes of the scratch a batch run needs (tile counters).  The
+ * scratch must be zero before its first use; every launch leaves it zero,
+ * so it can be reused by later runs on the same stream. */
+FW_API int fw_batch_scratch_size(int64_t *bytes);
+
+/* Advance every tissue of the batch by n_steps time steps from batch offset
+ * `offset` (tissue i at its step n_begin[i] + offset).  The current u of
+ * each tissue is its u[offset & 1] on entry and u[(offset + n_steps) & 1] on
+ * return, as after the same steps of fw_step.  Calls sharing one scratch
+ * buffer must be ordered (the same stream). */
+FW_API int fw_batch_run(const fw_batch *b, void *scratch, int64_t offset,
+                        int64_t n_steps, void *stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,109 @@
+"""GPU: a batch of tissues of different models, stencils, sizes, stimuli,
+trackers and run lengths advanced together by the persistent ragged kernel
+(TissueBatch / fw_batch_run) equals each tissue run on its own in the fused
+form with the same region shape and K (cp.async variant, K = 4): every node
+is computed by the same float32 expression on the same inputs, whichever
+tile or launch computes it, so the comparison is exact."""
+import copy
+
+import numpy as np
+import pytest
+import torch
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gc():
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    from finitewave_gb300 import _ffi
+    _ffi.load()
+    import gpu_cases
+    return gpu_cases
+
+
+def _no_probes(case, keep_at=1):
+    c = copy.copy(case)
+    out, n_at = [], 0
+    for t in case.get("trackers", []):
+        if t["kind"] == "at":
+            if n_at >= keep_at:
+                continue
+            n_at += 1
+        elif t["kind"] != "lat":
+            continue
+        out.append(t)
+    c["trackers"] = out
+    return c
+
+
+def _batch_cases():
+    """Tissues of every batched kind: AP / MS / FK, iso5 / aniso9, sizes
+    from 34 to 102 nodes a side and a 3 x 200 cable, 600 to 10000 steps."""
+    out = [_no_probes(cases.ap2d_cfg1()[0]),
+           _no_probes(cases.ap2d_aniso_spiral()[0])]
+    for name in ("ms", "fk"):
+        for aniso in (False, True):
+            out.append(_no_probes(cases.models_2d(name, aniso)[0]))
+    cable = _no_probes(cases.trackers_cable()[0])
+    out.append(cable)
+    st = _no_probes(cases.stimuli_2d()[0])
+    out.append(st)
+    return out
+
+
+def _outputs(model, objs):
+    r = {"u": model.u, "step": model.step, "t": model.t}
+    for name in model._state_names:
+        r[name] = getattr(model, name)
+    r["trackers"] = [o.output for o in objs]
+    return r
+
+
+def _same(a, b, where):
+    if isinstance(a, list):
+        assert len(a) == len(b), where
+        for i, (x, y) in enumerate(zip(a, b)):
+            _same(x, y, f"{where}[{i}]")
+    elif isinstance(a, dict):
+        assert a.keys() == b.keys(), where
+        for k in a:
+            _same(a[k], b[k], f"{where}.{k}")
+    else:
+        assert np.array_equal(np.asarray(a), np.asarray(b)), where
+
+
+def test_batch_equals_single_fused(gc):
+    import finitewave_gb300 as fg
+    cs = _batch_cases()
+    single = []
+    for c in cs:
+        m, objs = gc.build(c, npfloat="float32", form="fused", fused_k=4,
+                           fused_variant=1)
+        m.run()
+        single.append(_outputs(m, objs))
+    built = [gc.build(c, npfloat="float32") for c in cs]
+    batch = fg.TissueBatch([m for m, _ in built])
+    launches0 = fg._ffi.load().fw_launch_count()
+    batch.run()
+    torch.cuda.synchronize()
+    assert fg._ffi.load().fw_launch_count() > launches0
+    for i, ((m, objs), ref) in enumerate(zip(built, single)):
+        got = _outputs(m, objs)
+        assert got["step"] == ref["step"] and got["t"] == ref["t"], i
+        _same(got, ref, f"tissue {i}")
+
+
+def test_batch_rejects_unsupported(gc):
+    import finitewave_gb300 as fg
+    case, _ = cases.ap2d_aniso_spiral()   # has probe trackers
+    m, _ = gc.build(case, npfloat="float32")
+    with pytest.raises(ValueError, match="probe"):
+        fg.TissueBatch([m]).run()
+    case, _ = cases.ap2d_cfg1()
+    m, _ = gc.build(case, npfloat="float64")
+    with pytest.raises(ValueError, match="float32"):
+        fg.TissueBatch([m]).run()

@@ -198,3 +198,41 @@ def test_detailed_model_layout(lib):
             assert _ffi.state_is_f64(m._model_id, _ffi.F32, i) == \
                 (name in names), name
         assert m.state_vars == ["u"] + list(m._state_names)
+
+
+def test_batch_plan_checks(lib):
+    """fw_batch_plan_size validates each tissue on the host (no device
+    work): supported models / precision / trackers, and sizes the plan by
+    the tissues' tile counts."""
+    from finitewave_gb300 import _ffi
+
+    def tissue(ni, nj, model=_ffi.MODEL_AP, prec=_ffi.F32, n_probe=0):
+        a = _ffi.StepArgs()
+        a.model, a.stencil, a.precision = model, _ffi.ISO5, prec
+        a.ni, a.nj, a.nk = ni, nj, 1
+        a.weights = a.myo = a.u[0] = a.u[1] = 0x1000
+        a.state[0] = a.state[1] = 0x1000
+        a.n_probe = n_probe
+        return a
+
+    def size(ts):
+        arr = (ctypes.c_void_p * len(ts))(*[ctypes.addressof(t) for t in ts])
+        out = ctypes.c_int64()
+        rc = lib.fw_batch_plan_size(arr, len(ts), ctypes.byref(out))
+        return rc, out.value
+
+    rc, one = size([tissue(100, 100)])
+    assert rc == _ffi.FW_OK and one > 0
+    rc, two = size([tissue(100, 100), tissue(100, 100)])
+    assert rc == _ffi.FW_OK and two > one
+    rc, big = size([tissue(1000, 1000)])
+    assert rc == _ffi.FW_OK and big > one
+    assert size([tissue(64, 64, model=_ffi.MODEL_TP06)])[0] == \
+        _ffi.FW_ERR_UNSUPPORTED
+    assert size([tissue(64, 64, prec=_ffi.F64)])[0] == \
+        _ffi.FW_ERR_UNSUPPORTED
+    assert size([tissue(64, 64, n_probe=1)])[0] == _ffi.FW_ERR_UNSUPPORTED
+    assert size([tissue(2, 64)])[0] == _ffi.FW_ERR_ARG
+    nb = ctypes.c_int64()
+    assert lib.fw_batch_scratch_size(ctypes.byref(nb)) == _ffi.FW_OK
+    assert nb.value >= 8
