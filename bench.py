@@ -19,6 +19,14 @@ public model API with the state uploaded from pinned host memory and the
 potential and activation map read back every bench step.  The float64 plain
 form is timed beside it (``fp64_plain``).
 
+``batched``: the many-tissue configuration -- 256 independent 2D tissues
+of uneven sizes (side log-uniform in [64, 1024]), models drawn from
+Aliev-Panfilov / Mitchell-Schaeffer / Fenton-Karma, isotropic or anisotropic,
+fibrosis p uniform in [0, 0.3], S1-S2 protocol, a local activation tracker
+each -- advanced together by TissueBatch (one persistent float32 launch per
+4 steps over a ragged tile list), next to the same tissues in the float64
+plain form.
+
 ``--impl reference`` times the reference's algorithm on the host cores: the
 C restatement of its numba kernels (oracle/fw_oracle.c, OpenMP over all
 cores, float64, precomputed weights) on the same workload, a bounded number
@@ -28,6 +36,7 @@ Multi-GPU: the path is replicated, not sharded -- each rank advances its own
 copy of the tissue (``scaling: weak``); rank 0 prints the line.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -61,6 +70,162 @@ def workload_inputs(n=N, seed=SEED):
     theta = (np.pi / 4) * g / np.abs(g).max()
     fibers = np.stack([np.cos(theta), np.sin(theta)], -1).astype(np.float64)
     return mesh, fibers
+
+
+# batched workload: 256 independent 2D tissues (see batched_specs)
+N_TISSUES = 256
+BCL = {"ap": 60.0, "ms": 1000.0, "fk": 1000.0}
+B_ALG_BATCH = {("ap", "iso5"): 17, ("ap", "aniso9"): 25,
+               ("ms", "iso5"): 17, ("ms", "aniso9"): 25,
+               ("fk", "iso5"): 25, ("fk", "aniso9"): 33}
+
+
+def batched_specs(n_tissues=N_TISSUES, seed=SEED):
+    """The batched configuration: side lengths log-uniform in [64, 1024],
+    model uniform over Aliev-Panfilov / Mitchell-Schaeffer / Fenton-Karma,
+    isotropic or 9-point anisotropic (smooth random fibers, sigma = side/64
+    nodes), diffuse fibrosis with p uniform in [0, 0.3]; S1-S2 protocol: 8
+    S1 beats from the left edge at the model's basic cycle length, then an
+    S2 on the lower-left quadrant after a coupling interval uniform in
+    [0.5, 1] x BCL.  Seeded; all randomness from default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_tissues):
+        side = int(round(np.exp(rng.uniform(np.log(64), np.log(1024)))))
+        model = ("ap", "ms", "fk")[int(rng.integers(3))]
+        aniso = bool(rng.integers(2))
+        p = float(rng.uniform(0.0, 0.3))
+        ci = float(rng.uniform(0.5, 1.0)) * BCL[model]
+        specs.append(dict(side=side, model=model, aniso=aniso, p=p, ci=ci,
+                          seed=int(rng.integers(1 << 31))))
+    return specs
+
+
+def batched_tissue(fg, spec, npfloat):
+    import scipy.ndimage as nd
+    n = spec["side"]
+    r = np.random.default_rng(spec["seed"])
+    mesh = (1 + (r.random((n, n)) <= spec["p"])).astype(np.int8)
+    mesh[0, :] = mesh[-1, :] = mesh[:, 0] = mesh[:, -1] = 0
+    tissue = fg.CardiacTissue2D((n, n))
+    tissue.mesh = mesh
+    cls = {"ap": fg.AlievPanfilov2D, "ms": fg.MitchellSchaeffer2D,
+           "fk": fg.FentonKarma2D}[spec["model"]]
+    model = cls()
+    if spec["aniso"]:
+        g = nd.gaussian_filter(r.standard_normal((n, n)), n / 64.0)
+        theta = (np.pi / 4) * g / max(np.abs(g).max(), 1e-30)
+        tissue.fibers = np.stack([np.cos(theta), np.sin(theta)], -1)
+        st = fg.AsymmetricStencil2D()
+        st.D_al, st.D_ac = 1.0, 0.111
+        model.stencil = st
+    model.dt, model.dr = 0.01, 0.25
+    bcl = BCL[spec["model"]]
+    model.t_max = 7 * bcl + spec["ci"] + bcl
+    model.npfloat = npfloat
+    model.cardiac_tissue = tissue
+    seq = fg.StimSequence()
+    for b in range(8):
+        seq.add_stim(fg.StimVoltageCoord2D(b * bcl, 1.0, 0, n, 1, 6))
+    seq.add_stim(fg.StimVoltageCoord2D(7 * bcl + spec["ci"], 1.0, n // 2, n,
+                                       0, n // 2))
+    model.stim_sequence = seq
+    lat = fg.LocalActivationTime2DTracker()
+    lat.threshold = 0.5
+    trs = fg.TrackerSequence()
+    trs.add_tracker(lat)
+    model.tracker_sequence = trs
+    return model
+
+
+def run_batched(args, fg, torch):
+    """Batched float32 throughput through TissueBatch.run (one persistent
+    launch per 4 steps over all tissues), the same tissues in the float64
+    plain form one after another, and the myocyte-weighted algorithmic
+    bytes."""
+    specs = batched_specs(args.batched_tissues)
+    models = [batched_tissue(fg, s, "float32") for s in specs]
+    for m in models:
+        m.initialize()
+    myo = [int(m._myo_d.sum().item()) for m in models]
+    b_alg = sum(B_ALG_BATCH[(s["model"], "aniso9" if s["aniso"] else "iso5")]
+                * k for s, k in zip(specs, myo)) / sum(myo)
+    batch = fg.TissueBatch(models)
+    chunk = args.chunk
+
+    def advance(steps):
+        steps0 = [m.step for m in models]
+        for m in models:
+            m.t_max = m.t + steps * m.dt
+        batch.run(initialize=False)
+        return sum(k * (m.step - s0) for k, m, s0 in zip(myo, models, steps0))
+
+    for _ in range(args.warmup):
+        advance(chunk)
+    torch.cuda.synchronize()
+    L = fg._ffi.load()
+    # public API: one TissueBatch.run over k_b bench steps (one plan)
+    k_b = max(3, args.steps // 4)
+    l0 = L.fw_launch_count()
+    t0 = time.perf_counter()
+    work = advance(k_b * chunk)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    launches = L.fw_launch_count() - l0
+    value = work / el
+    # the kernel alone: fw_batch_run on the last plan, CUDA events (the
+    # models' host-side step counters are not advanced; discarded below)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    kl0 = L.fw_launch_count()
+    e0.record(stream)
+    fg._ffi.call("fw_batch_run", ctypes.byref(batch._batch),
+                 batch._scratch.data_ptr(), 0, chunk, stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    kms = e0.elapsed_time(e1)
+    kl = L.fw_launch_count() - kl0
+    kernel_value = sum(myo) * chunk / (kms / 1e3)
+    del batch, models
+    torch.cuda.empty_cache()
+
+    # the same tissues, float64 plain form, one tissue after the other
+    s64 = 20
+    work64, t64 = 0, 0.0
+    for s in specs:
+        m = batched_tissue(fg, s, "float64")
+        m.form = "plain"
+        m.initialize()
+        k = int(m._myo_d.sum().item())
+        m._run_segment(s64, sync=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m._run_segment(s64, sync=False)
+        torch.cuda.synchronize()
+        t64 += time.perf_counter() - t0
+        work64 += k * s64
+        del m
+    torch.cuda.empty_cache()
+    peak, _ = peaks()
+    achieved = b_alg * kernel_value / 1e9
+    return {"value": value, "unit": UNIT, "tissues": len(specs),
+            "myocytes": sum(myo), "time_steps_per_bench_step": chunk,
+            "bench_steps": k_b, "launches": int(launches),
+            "ms_per_step": 1e3 * el / k_b,
+            "kernel": {"name": "k_batch", "value": kernel_value,
+                       "ms_per_launch": kms / max(1, kl),
+                       "time_steps_per_launch": chunk / max(1, kl)},
+            "fp64_plain": {"value": work64 / t64, "unit": UNIT,
+                           "time_steps": s64},
+            "speedup_fp32_batched_over_fp64_plain": value / (work64 / t64),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "alg_bytes_per_myocyte_step": b_alg},
+            "timing": "value: wall clock over one TissueBatch.run of "
+                      "bench_steps x time_steps_per_bench_step steps (host "
+                      "planning included), state resident; kernel: CUDA "
+                      "events over fw_batch_run; roofline on the kernel"}
 
 
 def peaks():
@@ -279,6 +444,10 @@ def run_gb300(args):
     del m64
     torch.cuda.empty_cache()
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args, fg, torch)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(mesh, fibers, args.cpu_seconds)
@@ -309,6 +478,7 @@ def run_gb300(args):
                          "kernel": kernel_name,
                          "alg_bytes_per_myocyte_step": B_ALG["float32"],
                          "time_steps_per_launch": steps_per_launch},
+            "batched": batched,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks,
@@ -367,8 +537,6 @@ def run_reference(args):
     if rank != 0:
         return
     mesh, fibers = workload_inputs()
-    total = 0.0
-    steps_done = 0
     per = None
     for _ in range(args.warmup + args.steps):
         per = cpu_baseline(mesh, fibers, args.cpu_seconds / max(1, args.steps))
@@ -387,7 +555,6 @@ def run_reference(args):
         "e2e": {"value": cpu["value"], "unit": UNIT,
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    del total, steps_done
     print(json.dumps(line), flush=True)
 
 
@@ -407,6 +574,9 @@ def main():
                     help="time only the float32 form (profiling)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched many-tissue measurement")
+    ap.add_argument("--batched-tissues", type=int, default=N_TISSUES)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

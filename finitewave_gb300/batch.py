@@ -32,6 +32,7 @@ class TissueBatch:
         self.models = list(models)
         self._plan = None
         self._scratch = None
+        self._batch = None   # the last plan's fw_batch handle
 
     def add(self, model):
         self.models.append(model)
@@ -116,6 +117,7 @@ class TissueBatch:
                       plan.numel(), ctypes.byref(b), stream)
             _ffi.call("fw_batch_run", ctypes.byref(b), scratch.data_ptr(),
                       0, n, stream)
+            self._batch = b
             still = []
             for i, seg in zip(active, segs):
                 m = ms[i]

@@ -49,7 +49,10 @@ struct BWin {
     int64_t first, last, stride;
 };
 
-struct BTissue {
+// Per-tissue scalars and pointers, staged into shared memory at the start
+// of each tile (so that the sub-step loops read them without reloading
+// from global memory around their own global stores).
+struct BHead {
     const float *w;
     const int8_t *myo;
     float *u[2];
@@ -60,7 +63,6 @@ struct BTissue {
     int32_t ni, nj, tiles_j;
     int32_t n_stims, has_at, has_lat;
     int64_t n, step_base;
-    BStim stims[FW_MAX_STIMS];
     BWin at_win;
     float at_thr;
     int32_t *at_act;
@@ -73,6 +75,11 @@ struct BTissue {
     int32_t *status;
 };
 
+struct BTissue {
+    BHead h;
+    BStim stims[FW_MAX_STIMS];
+};
+
 struct BTile {
     int32_t tissue, tile;
 };
@@ -80,10 +87,12 @@ struct BTile {
 struct BSmem {
     float4 w[2][LH][LW];
     float u[2][LH + 2][LW + 2];
+    BHead h;
     uint32_t stim_on[FW_MAX_STIMS];
     uint32_t any_stim, at_on, lat_on;
     int next;
 };
+static_assert(sizeof(BHead) % 4 == 0, "BHead is staged in 4-byte words");
 
 // Sub-steps s < ks of a launch starting at tissue step n0 that fall inside
 // [first, last] and on a multiple of stride.
@@ -100,7 +109,7 @@ __device__ __forceinline__ uint32_t window_bits(int64_t n0, int ks,
     return m;
 }
 
-__device__ __noinline__ void lat_append(const BTissue &T, int64_t p, int64_t n)
+__device__ __noinline__ void lat_append(const BHead &T, int64_t p, int64_t n)
 {
     const int32_t c = T.lat_count[p];
     if (c < T.lat_cap)
@@ -110,13 +119,16 @@ __device__ __noinline__ void lat_append(const BTissue &T, int64_t p, int64_t n)
     T.lat_count[p] = c + 1;
 }
 
-// One tile of tissue T: K sub-steps from tissue step n0, input buffer
-// u[in_buf].  The per-sub-step event bits are in S (set before the call).
+// One tile of a tissue: K sub-steps from tissue step n0, input buffer
+// u[in_buf].  The tissue's head and the per-sub-step event bits are in S
+// (staged before the call, visible after the staging barrier below); its
+// stimuli are read from `stims` in global memory.
 template <class M, int ST>
-__device__ __forceinline__ void run_tile(const BTissue &T, int tile,
+__device__ __forceinline__ void run_tile(const BStim *stims, int tile,
                                          int64_t n0, int ks, int in_buf,
                                          BSmem &S)
 {
+    const BHead &T = S.h;
     constexpr int NWO = fused::Stencil2D<ST>::NWO;
     constexpr int CEN = fused::Stencil2D<ST>::CENTRE;
     const int tid = threadIdx.x;
@@ -209,7 +221,7 @@ __device__ __forceinline__ void run_tile(const BTissue &T, int tile,
         if ((any_stim >> s) & 1u) {
             for (int i = 0; i < T.n_stims; ++i) {
                 if (!((S.stim_on[i] >> s) & 1u)) continue;
-                const BStim &F = T.stims[i];
+                const BStim &F = stims[i];
                 if (gj < F.lo1 || gj >= F.hi1) continue;
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
@@ -324,13 +336,23 @@ __global__ void __launch_bounds__(NT, 2)
         const int t = S.next;
         if (t >= n_tiles) break;
         const BTile bt = tiles[t];
-        const BTissue &T = tissues[bt.tissue];
+        const BTissue *Tg = tissues + bt.tissue;
+        {
+            // stage the tissue's head into shared memory
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(&Tg->h);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&S.h);
+            for (int i = tid; i < (int)(sizeof(BHead) / 4); i += NT)
+                dst[i] = src[i];
+        }
+        __syncthreads();
+        const BHead &T = S.h;
         const int64_t n0 = T.step_base + offset;
         // event bits of this launch for the tissue (uniform per CTA)
         if (tid < FW_MAX_STIMS) {
             uint32_t b = 0;
             if (tid < T.n_stims)
-                b = window_bits(n0, ks, T.stims[tid].first, T.stims[tid].last, 1);
+                b = window_bits(n0, ks, Tg->stims[tid].first,
+                                Tg->stims[tid].last, 1);
             S.stim_on[tid] = b;
         } else if (tid == FW_MAX_STIMS) {
             S.at_on = T.has_at ? window_bits(n0, ks, T.at_win.first,
@@ -349,24 +371,25 @@ __global__ void __launch_bounds__(NT, 2)
         }
         // S.any_stim is read after the staging barrier inside run_tile
         const int key = T.model * 8 + T.stencil;
+        const BStim *stims = Tg->stims;
         switch (key) {
         case FW_MODEL_AP * 8 + FW_STENCIL_ISO5:
-            run_tile<ModelAP, FW_STENCIL_ISO5>(T, bt.tile, n0, ks, in_buf, S);
+            run_tile<ModelAP, FW_STENCIL_ISO5>(stims, bt.tile, n0, ks, in_buf, S);
             break;
         case FW_MODEL_AP * 8 + FW_STENCIL_ANISO9:
-            run_tile<ModelAP, FW_STENCIL_ANISO9>(T, bt.tile, n0, ks, in_buf, S);
+            run_tile<ModelAP, FW_STENCIL_ANISO9>(stims, bt.tile, n0, ks, in_buf, S);
             break;
         case FW_MODEL_MS * 8 + FW_STENCIL_ISO5:
-            run_tile<ModelMS, FW_STENCIL_ISO5>(T, bt.tile, n0, ks, in_buf, S);
+            run_tile<ModelMS, FW_STENCIL_ISO5>(stims, bt.tile, n0, ks, in_buf, S);
             break;
         case FW_MODEL_MS * 8 + FW_STENCIL_ANISO9:
-            run_tile<ModelMS, FW_STENCIL_ANISO9>(T, bt.tile, n0, ks, in_buf, S);
+            run_tile<ModelMS, FW_STENCIL_ANISO9>(stims, bt.tile, n0, ks, in_buf, S);
             break;
         case FW_MODEL_FK * 8 + FW_STENCIL_ISO5:
-            run_tile<ModelFK, FW_STENCIL_ISO5>(T, bt.tile, n0, ks, in_buf, S);
+            run_tile<ModelFK, FW_STENCIL_ISO5>(stims, bt.tile, n0, ks, in_buf, S);
             break;
         case FW_MODEL_FK * 8 + FW_STENCIL_ANISO9:
-            run_tile<ModelFK, FW_STENCIL_ANISO9>(T, bt.tile, n0, ks, in_buf, S);
+            run_tile<ModelFK, FW_STENCIL_ANISO9>(stims, bt.tile, n0, ks, in_buf, S);
             break;
         default:
             break;  // rejected by the plan
@@ -504,7 +527,7 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     int32_t t_count = 0;
     for (int i = 0; i < n; ++i) {
         const fw_step_args *a = tissues[i];
-        BTissue &T = desc[i];
+        BHead &T = desc[i].h;
         T.w = (const float *)a->weights;
         T.myo = a->myo;
         T.u[0] = (float *)a->u[0];
@@ -524,7 +547,7 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
         T.n_stims = a->n_stims;
         for (int s = 0; s < a->n_stims; ++s) {
             const fw_stim &S = a->stims[s];
-            BStim &B = T.stims[s];
+            BStim &B = desc[i].stims[s];
             B.first = S.first;
             B.last = S.last;
             B.kind = S.kind;
