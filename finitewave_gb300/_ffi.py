@@ -119,6 +119,7 @@ _SIGS = {
                        _vp], _i32),
     "fw_batch_scratch_size": ([ctypes.POINTER(_i64)], _i32),
     "fw_batch_run": ([ctypes.POINTER(Batch), _vp, _i64, _i64, _vp], _i32),
+    "fw_batch_run_noalloc": ([ctypes.POINTER(Batch), _i64, _i64, _vp], _i32),
 }
 
 # symbol -> ctypes structure whose size must match the library's

@@ -23,6 +23,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "fw_fused_kernel.cuh"
@@ -640,6 +641,65 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
         done += ks;
     }
     return FW_OK;
+}
+
+// ---- fw_batch_run_noalloc ----------------------------------------------------
+// The same launches as batch_run with the tile counters in the library's own
+// device memory: a file-scope array, one per device, so the call takes no
+// scratch buffer from its caller.  Only the counters live here (the plan
+// stays in the caller's buffer); they must start at zero, which the set-up
+// below ensures, and every launch leaves them at zero.  All calls on a device
+// share this one array, so calls whose launches overlap in time (other
+// streams, other host threads) race on it and must be ordered by the caller.
+
+namespace {
+
+constexpr int kNoallocScratchBytes = 256;  // the stated maximum
+constexpr int kNoallocMaxDevices = 64;
+
+static __device__ __align__(256) uint32_t
+    g_noalloc_scratch[kNoallocScratchBytes / sizeof(uint32_t)];
+
+std::mutex g_noalloc_mu;
+uint32_t *g_noalloc_ptr[kNoallocMaxDevices];  // device address, per device
+
+}  // namespace
+
+int batch_run_noalloc(const fw_batch *b, int64_t offset, int64_t n_steps,
+                      cudaStream_t stream)
+{
+    if (kBatchScratchBytes > kNoallocScratchBytes) {
+        set_error("fw_batch_run_noalloc: the batch needs %lld bytes of "
+                  "scratch, the library's fixed scratch holds %d",
+                  (long long)kBatchScratchBytes, kNoallocScratchBytes);
+        return FW_ERR_ARG;
+    }
+    int dev = 0;
+    FW_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoallocMaxDevices) {
+        set_error("fw_batch_run_noalloc: device %d beyond the %d supported",
+                  dev, kNoallocMaxDevices);
+        return FW_ERR_ARG;
+    }
+    uint32_t *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        scratch = g_noalloc_ptr[dev];
+        if (!scratch) {
+            // set-up, once per device, with that device current: the
+            // address of this device's copy of the array, then zero it
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess)
+                return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            e = cudaMemsetAsync(p, 0, kNoallocScratchBytes, stream);
+            if (e != cudaSuccess)
+                return cuda_error(e, "cudaMemsetAsync(g_noalloc_scratch)");
+            scratch = static_cast<uint32_t *>(p);
+            g_noalloc_ptr[dev] = scratch;
+        }
+    }
+    return batch_run(b, scratch, offset, n_steps, stream);
 }
 
 }  // namespace fw

@@ -278,4 +278,10 @@ int fw_batch_run(const fw_batch *b, void *scratch, int64_t offset,
                          (cudaStream_t)stream);
 }
 
+int fw_batch_run_noalloc(const fw_batch *b, int64_t offset, int64_t n_steps,
+                         void *stream)
+{
+    return fw::batch_run_noalloc(b, offset, n_steps, (cudaStream_t)stream);
+}
+
 }  // extern "C"

@@ -150,6 +150,8 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
 int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
               int64_t n_steps, cudaStream_t stream);
 constexpr int64_t kBatchScratchBytes = 256;
+int batch_run_noalloc(const fw_batch *b, int64_t offset, int64_t n_steps,
+                      cudaStream_t stream);
 
 // Detailed models, one translation unit per model x precision
 // (fw_step_detailed_*.cu).

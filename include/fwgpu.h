@@ -313,6 +313,23 @@ FW_API int fw_batch_scratch_size(int64_t *bytes);
 FW_API int fw_batch_run(const fw_batch *b, void *scratch, int64_t offset,
                         int64_t n_steps, void *stream);
 
+/* fw_batch_run without a scratch argument; no counterpart in the reference
+ * (the reference runs on the CPU and has no device scratch).  For callers
+ * that cannot hand the library a scratch buffer: code that may not allocate
+ * device memory itself -- for instance a binding that receives the tissues'
+ * arrays and the plan buffer from another runtime and has no allocator of
+ * its own for the device, or a program that fixes its device memory at
+ * set-up.  The tile counters then live in a fixed array inside the library
+ * (256 bytes per device; a batch needing more scratch is rejected with
+ * FW_ERR_ARG).  The call allocates nothing.  The first call on a device does
+ * a one-time set-up (looks up the array's device address and zeroes it on
+ * `stream`), so make that first call before any stream capture.  All calls
+ * on one device share the array: calls whose launches may overlap (other
+ * streams, other host threads) race and must be ordered by the caller.
+ * Otherwise identical to fw_batch_run. */
+FW_API int fw_batch_run_noalloc(const fw_batch *b, int64_t offset,
+                                int64_t n_steps, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
