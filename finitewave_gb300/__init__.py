@@ -11,6 +11,7 @@ hand-written sm_103a CUDA (``libfwgpu.so``, C ABI in ``include/fwgpu.h``).
 """
 from .batch import TissueBatch
 from .command import Command, CommandSequence
+from .fibrosis import Diffuse2DPattern, Diffuse3DPattern, FibrosisPattern
 from .model import (AlievPanfilov2D, AlievPanfilov3D, CardiacModel,
                     Courtemanche2D, Courtemanche3D, FentonKarma2D,
                     FentonKarma3D, MitchellSchaeffer2D, MitchellSchaeffer3D,

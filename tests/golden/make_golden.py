@@ -455,6 +455,28 @@ def case_courtemanche(fw):
     return out
 
 
+def case_fibrosis(fw):
+    """Seeded diffuse fibrosis patterns, 2D and 3D, whole mesh and boxes."""
+    out = {}
+    np.random.seed(2024)
+    out["d2_full"] = fw.Diffuse2DPattern(0.3).generate(shape=(20, 30))
+    np.random.seed(2025)
+    out["d2_box"] = fw.Diffuse2DPattern(0.5, 3, 15, 4, 22).generate(
+        shape=(20, 30))
+    np.random.seed(2026)
+    mesh = np.ones((20, 30), dtype=np.int8)
+    mesh[0, :] = 0
+    out["d2_mesh_in"] = mesh.copy()
+    out["d2_mesh"] = fw.Diffuse2DPattern(0.2).generate(mesh=mesh)
+    np.random.seed(2027)
+    out["d3_box"] = fw.Diffuse3DPattern(2, 10, 1, 8, 0, 5, 0.25).generate(
+        (12, 9, 6))
+    np.random.seed(2028)
+    out["d3_full"] = fw.Diffuse3DPattern(None, None, None, None, None, None,
+                                         0.1).generate((8, 7, 6))
+    return out
+
+
 CASES = {
     "weights_2d": case_weights_2d,
     "weights_3d": case_weights_3d,
@@ -466,6 +488,7 @@ CASES = {
     "stimuli": case_stimuli,
     "tp06": case_tp06,
     "courtemanche": case_courtemanche,
+    "fibrosis": case_fibrosis,
 }
 
 

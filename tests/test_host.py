@@ -236,3 +236,34 @@ def test_batch_plan_checks(lib):
     nb = ctypes.c_int64()
     assert lib.fw_batch_scratch_size(ctypes.byref(nb)) == _ffi.FW_OK
     assert nb.value >= 8
+
+
+def test_diffuse_patterns_match_reference():
+    """Diffuse2DPattern / Diffuse3DPattern draw the reference's random
+    numbers: same seed, same mesh (tests/golden/fibrosis.npz)."""
+    import finitewave_gb300 as fg
+    g = np.load(os.path.join(ROOT, "tests", "golden", "fibrosis.npz"))
+    np.random.seed(2024)
+    assert np.array_equal(fg.Diffuse2DPattern(0.3).generate(shape=(20, 30)),
+                          g["d2_full"])
+    np.random.seed(2025)
+    assert np.array_equal(
+        fg.Diffuse2DPattern(0.5, 3, 15, 4, 22).generate(shape=(20, 30)),
+        g["d2_box"])
+    np.random.seed(2026)
+    got = fg.Diffuse2DPattern(0.2).generate(mesh=g["d2_mesh_in"].copy())
+    assert np.array_equal(got, g["d2_mesh"])
+    np.random.seed(2027)
+    assert np.array_equal(
+        fg.Diffuse3DPattern(2, 10, 1, 8, 0, 5, 0.25).generate((12, 9, 6)),
+        g["d3_box"])
+    np.random.seed(2028)
+    assert np.array_equal(
+        fg.Diffuse3DPattern(None, None, None, None, None, None,
+                            0.1).generate((8, 7, 6)), g["d3_full"])
+    t = fg.CardiacTissue2D((20, 30))
+    np.random.seed(2024)
+    fg.Diffuse2DPattern(0.3).apply(t)
+    ref = g["d2_full"].copy()
+    ref[0, :] = ref[-1, :] = ref[:, 0] = ref[:, -1] = 0
+    assert np.array_equal(np.asarray(t.mesh), ref)
