@@ -138,7 +138,7 @@ def batched_tissue(fg, spec, npfloat):
     return model
 
 
-def run_batched(args, fg, torch):
+def run_batched(args, fg, torch, reps):
     """Batched float32 throughput through TissueBatch.run (one persistent
     launch per 4 steps over all tissues), the same tissues in the float64
     plain form one after another, and the myocyte-weighted algorithmic
@@ -162,7 +162,7 @@ def run_batched(args, fg, torch):
 
     for _ in range(args.warmup):
         advance(chunk)
-    torch.cuda.synchronize()
+    reps.barrier()
     L = fg._ffi.load()
     # public API: one TissueBatch.run over k_b bench steps (one plan)
     k_b = max(3, args.steps // 4)
@@ -171,8 +171,10 @@ def run_batched(args, fg, torch):
     work = advance(k_b * chunk)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
+    reps.barrier()
     launches = L.fw_launch_count() - l0
-    value = work / el
+    value = reps.whole_job(work, el)
+    el = reps.max(el)
     # the kernel alone: fw_batch_run on the last plan, CUDA events (the
     # models' host-side step counters are not advanced; discarded below)
     stream = torch.cuda.current_stream()
@@ -186,7 +188,7 @@ def run_batched(args, fg, torch):
     torch.cuda.synchronize()
     kms = e0.elapsed_time(e1)
     kl = L.fw_launch_count() - kl0
-    kernel_value = sum(myo) * chunk / (kms / 1e3)
+    kernel_value = reps.whole_job(sum(myo) * chunk, kms / 1e3)
     del batch, models
     torch.cuda.empty_cache()
 
@@ -208,7 +210,8 @@ def run_batched(args, fg, torch):
         del m
     torch.cuda.empty_cache()
     peak, _ = peaks()
-    achieved = b_alg * kernel_value / 1e9
+    achieved = b_alg * kernel_value / reps.world / 1e9   # per GPU
+    fp64_value = reps.whole_job(work64, t64)
     return {"value": value, "unit": UNIT, "tissues": len(specs),
             "myocytes": sum(myo), "time_steps_per_bench_step": chunk,
             "bench_steps": k_b, "launches": int(launches),
@@ -216,9 +219,9 @@ def run_batched(args, fg, torch):
             "kernel": {"name": "k_batch", "value": kernel_value,
                        "ms_per_launch": kms / max(1, kl),
                        "time_steps_per_launch": chunk / max(1, kl)},
-            "fp64_plain": {"value": work64 / t64, "unit": UNIT,
+            "fp64_plain": {"value": fp64_value, "unit": UNIT,
                            "time_steps": s64},
-            "speedup_fp32_batched_over_fp64_plain": value / (work64 / t64),
+            "speedup_fp32_batched_over_fp64_plain": value / fp64_value,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "alg_bytes_per_myocyte_step": b_alg},
@@ -330,15 +333,56 @@ def device_steps(model, chunk, iters, torch):
     return e0.elapsed_time(e1), L.fw_launch_count() - l0
 
 
+class Replicas:
+    """The N > 1 path: one process per GPU, each advancing its own replica
+    of the workload with no data exchange (the path is not sharded); the
+    only collectives are the barriers around timed regions and the maximum
+    of the per-rank times.  Whole-job throughput = world x per-rank units /
+    max time.  `backend` / `device` are "nccl" / "cuda" on GPUs and "gloo" /
+    "cpu" in the host-only tests."""
+
+    def __init__(self, backend="nccl", device="cuda"):
+        import torch
+        import torch.distributed as dist
+        self.torch, self.dist = torch, dist
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.device = device
+        self.owned = False
+        if self.world > 1 and not dist.is_initialized():
+            dist.init_process_group(backend)
+            self.owned = True
+
+    def barrier(self):
+        if self.device == "cuda":
+            self.torch.cuda.synchronize()
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64,
+                              device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def whole_job(self, units_per_rank, seconds_per_rank):
+        """Units all ranks processed / the slowest rank's time."""
+        return self.world * units_per_rank / self.max(seconds_per_rank)
+
+    def close(self):
+        if self.owned:
+            self.dist.destroy_process_group()
+            self.owned = False
+
+
 def run_gb300(args):
     import torch
-    import torch.distributed as dist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl")
+    reps = Replicas("nccl", "cuda")
+    world, rank, local = reps.world, reps.rank, reps.local
     torch.cuda.set_device(local)
     import finitewave_gb300 as fg
     from finitewave_gb300 import _ffi
@@ -348,18 +392,7 @@ def run_gb300(args):
     myo = int((mesh == 1).sum())
     chunk, K, W = args.chunk, args.steps, args.warmup
     form32 = args.form
-
-    def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = reps.barrier, reps.max
 
     # --- float32 form, state resident -------------------------------------
     model, at = build_model(fg, mesh, fibers, "float32", form32)
@@ -446,7 +479,7 @@ def run_gb300(args):
 
     batched = None
     if not args.no_batched:
-        batched = run_batched(args, fg, torch)
+        batched = run_batched(args, fg, torch, reps)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -484,8 +517,7 @@ def run_gb300(args):
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    reps.close()
 
 
 def traffic_from_profiles(myo, steps_per_launch):
