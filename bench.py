@@ -27,6 +27,11 @@ each -- advanced together by TissueBatch (one persistent float32 launch per
 4 steps over a ragged tile list), next to the same tissues in the float64
 plain form.
 
+``tp06_slab``: TP06 on a 512 x 512 x 64 slab (10 % fibrosis, fibers
+rotating -60..+60 degrees through the depth, AsymmetricStencil3D, S1-S2,
+16 probes), plain form, float32 with float64 ion concentrations next to
+float64.
+
 ``--impl reference`` times the reference's algorithm on the host cores: the
 C restatement of its numba kernels (oracle/fw_oracle.c, OpenMP over all
 cores, float64, precomputed weights) on the same workload, a bounded number
@@ -231,6 +236,99 @@ def run_batched(args, fg, torch, reps):
                       "events over fw_batch_run; roofline on the kernel"}
 
 
+# TP06 slab: 512 x 512 x 64, float32 state with float64 concentrations
+SLAB = (512, 512, 64)
+# algorithmic bytes per myocyte-step: 14 float32 arrays (u, 13 gates / the
+# derived oo) + 5 float64 concentrations, read and written; 1 B mesh code;
+# 3 float32 fiber components
+B_ALG_TP06 = 2 * (15 * 4 + 5 * 8) + 1 + 3 * 4
+
+
+def tp06_slab(fg, npfloat, shape=SLAB, seed=SEED):
+    """The TP06 slab configuration: 10 % diffuse fibrosis (seeded
+    Diffuse3DPattern), fibers (cos phi, sin phi, 0) with phi linear from -60
+    to +60 degrees over the interior layers k, AsymmetricStencil3D with
+    D_al = 1, D_ac = 0.25 (D_model 0.154: D_long 0.154, D_trans 0.0385
+    mm^2/ms), dr = 0.25 mm, dt = 0.01 ms; S1 current on the first interior
+    layers at 0 ms, S2 on a corner quarter at 310 ms; u probed at 16 seeded
+    myocytes every 10 steps."""
+    ni, nj, nk = shape
+    np.random.seed(seed)
+    mesh = fg.Diffuse3DPattern(None, None, None, None, None, None,
+                               0.1).generate(shape)
+    tissue = fg.CardiacTissue3D(shape)
+    tissue.mesh = mesh
+    phi = np.zeros(nk)
+    phi[1:-1] = np.deg2rad(np.linspace(-60.0, 60.0, nk - 2))
+    fib = np.zeros(shape + (3,))
+    fib[..., 0] = np.cos(phi)[None, None, :]
+    fib[..., 1] = np.sin(phi)[None, None, :]
+    tissue.fibers = fib
+    model = fg.TP063D()
+    st = fg.AsymmetricStencil3D()
+    st.D_al, st.D_ac = 1.0, 0.25
+    model.stencil = st
+    model.dt, model.dr = 0.01, 0.25
+    model.t_max = 1000.0
+    model.npfloat = npfloat
+    model.cardiac_tissue = tissue
+    seq = fg.StimSequence()
+    seq.add_stim(fg.StimCurrentCoord3D(0, 100, 1.0, 0, ni, 0, nj, 1, 4))
+    seq.add_stim(fg.StimCurrentCoord3D(310, 100, 1.0, ni // 2, ni, nj // 2,
+                                       nj, 1, nk - 1))
+    model.stim_sequence = seq
+    myo = np.argwhere(np.asarray(tissue.mesh) == 1)
+    pick = np.random.default_rng(seed).choice(len(myo), 16, replace=False)
+    pr = fg.MultiVariable3DTracker()
+    pr.cell_ind = myo[pick].tolist()
+    pr.var_list = ["u"]
+    pr.step = 10
+    trs = fg.TrackerSequence()
+    trs.add_tracker(pr)
+    model.tracker_sequence = trs
+    return model
+
+
+def run_tp06_slab(args, fg, torch, reps):
+    """TP06 slab throughput, float32 (float64 concentrations) and float64,
+    plain form, state resident (~3 GB, larger than L2)."""
+    chunk = args.chunk
+    out = {}
+    shape = tuple(args.slab)
+    for prec, k in (("float32", max(3, args.steps // 10)),
+                    ("float64", 2)):
+        m = tp06_slab(fg, prec, shape)
+        m.initialize()
+        myo = int(m._myo_d.sum().item())
+        for _ in range(2):
+            m._run_segment(chunk, sync=False)
+        reps.barrier()
+        ms, launches = device_steps(m, chunk, k, torch)
+        reps.barrier()
+        out[prec] = dict(value=reps.whole_job(myo * chunk * k, ms / 1e3),
+                         ms_per_step=reps.max(ms) / k, launches=int(launches),
+                         myocytes=myo, bench_steps=k)
+        del m
+        torch.cuda.empty_cache()
+    peak, _ = peaks()
+    v32 = out["float32"]["value"]
+    achieved = B_ALG_TP06 * v32 / reps.world / 1e9
+    return {"value": v32, "unit": UNIT, "grid": list(shape),
+            "myocytes": out["float32"]["myocytes"],
+            "time_steps_per_bench_step": chunk,
+            "ms_per_step": out["float32"]["ms_per_step"],
+            "bench_steps": out["float32"]["bench_steps"],
+            "launches": out["float32"]["launches"],
+            "form": "plain", "dtype": "f32 (f64 ion concentrations)",
+            "fp64_plain": {"value": out["float64"]["value"], "unit": UNIT},
+            "speedup_fp32_over_fp64": v32 / out["float64"]["value"],
+            "roofline": {"bound": "fp32+sfu (compute); HBM fraction shown",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak,
+                         "alg_bytes_per_myocyte_step": B_ALG_TP06,
+                         "kernel": "k_step<ModelTP06, ANISO19, float>"}}
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -388,6 +486,15 @@ def run_gb300(args):
     from finitewave_gb300 import _ffi
     _ffi.load()
 
+    if args.only in ("tp06", "batched"):
+        # one sub-measurement alone (profiling runs); not the bench line
+        fn = run_tp06_slab if args.only == "tp06" else run_batched
+        r = fn(args, fg, torch, reps)
+        if rank == 0:
+            print(json.dumps({"only": args.only, **r}), flush=True)
+        reps.close()
+        return
+
     mesh, fibers = workload_inputs(args.grid)
     myo = int((mesh == 1).sum())
     chunk, K, W = args.chunk, args.steps, args.warmup
@@ -481,6 +588,10 @@ def run_gb300(args):
     if not args.no_batched:
         batched = run_batched(args, fg, torch, reps)
 
+    tp06 = None
+    if not args.no_tp06:
+        tp06 = run_tp06_slab(args, fg, torch, reps)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(mesh, fibers, args.cpu_seconds)
@@ -512,6 +623,7 @@ def run_gb300(args):
                          "alg_bytes_per_myocyte_step": B_ALG["float32"],
                          "time_steps_per_launch": steps_per_launch},
             "batched": batched,
+            "tp06_slab": tp06,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks,
@@ -609,6 +721,12 @@ def main():
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched many-tissue measurement")
     ap.add_argument("--batched-tissues", type=int, default=N_TISSUES)
+    ap.add_argument("--no-tp06", action="store_true",
+                    help="skip the TP06 slab measurement")
+    ap.add_argument("--only", default=None, choices=[None, "tp06", "batched"],
+                    help="run one sub-measurement alone (profiling)")
+    ap.add_argument("--slab", type=int, nargs=3, default=list(SLAB),
+                    help="TP06 slab shape (profiling runs use a smaller one)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

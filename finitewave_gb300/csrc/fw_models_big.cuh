@@ -1,15 +1,17 @@
 // fw_models_big.cuh -- the detailed ionic models: ten Tusscher-Panfilov 2006
 // (TP06) and Courtemanche 1998, in the interface of fw_models.cuh.
 //
-// Template parameter T is the type of the potential, the gates and the
-// currents; the ion-concentration state (TP06: Ca_i, Ca_SR, Ca_ss, Na_i,
-// K_i; Courtemanche: Na_i, K_i, Ca_i, Ca_up, Ca_rel) is always float64 and
-// its update is done in float64, so that under FW_F32 only the
-// concentration accumulators carry the extra precision.  Under FW_F64 every
-// quantity is float64 and the expressions follow the reference's evaluation
-// order, with CUDA's exp/log/sqrt/pow (a few ulp from the C library's).
-// Under FW_F32 the Nernst logarithms take the float64 concentration ratio
-// rounded to float.
+// Template parameter T is the type of the potential, the gates, the
+// currents and the concentration rates; the ion-concentration state (TP06:
+// Ca_i, Ca_SR, Ca_ss, Na_i, K_i; Courtemanche: Na_i, K_i, Ca_i, Ca_up,
+// Ca_rel) is always stored as float64.  Under FW_F64 every quantity is
+// float64 and the expressions follow the reference's evaluation order, with
+// CUDA's exp/log/sqrt/pow (a few ulp from the C library's).  Under FW_F32
+// everything is computed in float32 from the concentrations rounded to
+// float, and only the accumulation `c += dt * rate` runs in float64 -- the
+// increments are ~1e-6 of the value, below float32's resolution -- which
+// keeps the float64 pipe (a small fraction of GB300's float32 rate) out of
+// the per-node work.
 //
 // Reference quirks kept: TP06 never updates Ca_i (tp06_2d.py:1098 assigns the
 // new value and then the old one); Courtemanche's IKr conductance is fixed
@@ -25,8 +27,36 @@
 
 namespace fw {
 
-__device__ __forceinline__ float fpow(float x, float y) { return powf(x, y); }
-__device__ __forceinline__ double fpow(double x, double y) { return pow(x, y); }
+// Transcendentals of the two precisions.  float64: CUDA's exp / log / pow
+// (the reference's expressions, within a few ulp of the C library).
+// float32: the SFU forms (__expf, __logf: a few ulp, growing by about one
+// ulp per unit of |x| for exp, CUDA's documented bound) and the integer and
+// half-integer powers as products -- the float32 form is compared with
+// float64 by tolerance, and these calls are most of its instructions.
+__device__ __forceinline__ float mexp(float x) { return __expf(x); }
+__device__ __forceinline__ double mexp(double x) { return exp(x); }
+__device__ __forceinline__ float mlog(float x) { return __logf(x); }
+__device__ __forceinline__ double mlog(double x) { return log(x); }
+__device__ __forceinline__ float pow3(float x) { return x * x * x; }
+__device__ __forceinline__ double pow3(double x) { return pow(x, 3.0); }
+__device__ __forceinline__ float pow15(float x) { return x * sqrtf(x); }
+__device__ __forceinline__ double pow15(double x) { return pow(x, 1.5); }
+
+// Instantaneous buffering (Rapid buffer approximation): the free
+// concentration c after adding d to the total c + B c / (c + K) solves
+// c^2 + (B - T + K) c - K T = 0 with T = c0 + B c0 / (c0 + K) + d
+// (tp06_2d.py:793-873).  With c = c0 + delta the constant term becomes
+// -(c0 + K) d, so delta solves delta^2 + p delta - (c0 + K) d = 0 with
+// p = c0 + K + B K / (c0 + K) - d; its root near zero, in the form without
+// cancellation, is 2 (c0 + K) d / (p + sqrt(p^2 + 4 (c0 + K) d)).
+__device__ __forceinline__ float buffered_step(float c0, float B, float K,
+                                               float d)
+{
+    const float kc = c0 + K;
+    const float p = kc + B * K / kc - d;
+    const float q = kc * d;
+    return 2.f * q / (p + sqrtf(fmaxf(p * p + 4.f * q, 0.f)));
+}
 
 // ---------------------------------------------------------------- TP06
 // Parameters in the order of tp06_2d.py's ionic_kernel_2d signature
@@ -129,132 +159,127 @@ struct ModelTP06 {
                                                const Params<T, NP> &P, T dt)
     {
         const T c1 = (T)1.0;
-        const double dtd = (double)dt;
-        // concentration-dependent constants in float64
-        const double Fd = (double)P.v[F], Vcd = (double)P.v[Vc],
-                     Vssd = (double)P.v[Vss], CAPd = (double)P.v[CAPACITANCE];
-        const double inverseVcF = 1.0 / (Vcd * Fd);
-        const double inversevssF2 = 1.0 / (2 * Vssd * Fd);
-
-        const T Ek = P.v[RTONF] * fw_log((T)((double)P.v[ko] / x.Ki));
-        const T Ena = P.v[RTONF] * fw_log((T)((double)P.v[nao] / x.nai));
-        const T Eks = P.v[RTONF] *
-                      fw_log((T)(((double)P.v[ko] + (double)P.v[pKNa] * (double)P.v[nao]) /
-                                  (x.Ki + (double)P.v[pKNa] * x.nai)));
-        const T Eca = (T)0.5 * P.v[RTONF] * fw_log((T)((double)P.v[cao] / x.cai));
         const T cass = (T)x.cass, cai = (T)x.cai, casr = (T)x.casr;
-        const T nai = (T)x.nai;
+        const T nai = (T)x.nai, Ki = (T)x.Ki;
+        const T inverseVcF = c1 / (P.v[Vc] * P.v[F]);
+        const T inversevssF2 = c1 / ((T)2 * P.v[Vss] * P.v[F]);
+
+        const T Ek = P.v[RTONF] * mlog(P.v[ko] / Ki);
+        const T Ena = P.v[RTONF] * mlog(P.v[nao] / nai);
+        const T Eks = P.v[RTONF] * mlog((P.v[ko] + P.v[pKNa] * P.v[nao]) /
+                                          (Ki + P.v[pKNa] * nai));
+        const T Eca = (T)0.5 * P.v[RTONF] * mlog(P.v[cao] / cai);
 
         // calc_ina
         T ina;
         {
-            const T am = c1 / (c1 + fw_exp(((T)(-60.0) - u) / (T)5.0));
-            const T beta_m = (T)0.1 / (c1 + fw_exp((u + (T)35.0) / (T)5.0)) +
-                             (T)0.1 / (c1 + fw_exp((u - (T)50.0) / (T)200.0));
+            const T am = c1 / (c1 + mexp(((T)(-60.0) - u) / (T)5.0));
+            const T beta_m = (T)0.1 / (c1 + mexp((u + (T)35.0) / (T)5.0)) +
+                             (T)0.1 / (c1 + mexp((u - (T)50.0) / (T)200.0));
             const T tau_m = am * beta_m;
-            const T e_m = fw_exp(((T)(-56.86) - u) / (T)9.03);
+            const T e_m = mexp(((T)(-56.86) - u) / (T)9.03);
             const T m_inf = c1 / ((c1 + e_m) * (c1 + e_m));
             T alpha_h, beta_h, alpha_j, beta_j;
             if (u >= (T)(-40.0)) {
                 alpha_h = (T)0;
-                beta_h = (T)0.77 / ((T)0.13 * (c1 + fw_exp(-(u + (T)10.66) / (T)11.1)));
+                beta_h = (T)0.77 / ((T)0.13 * (c1 + mexp(-(u + (T)10.66) / (T)11.1)));
                 alpha_j = (T)0;
-                beta_j = (T)0.6 * fw_exp((T)0.057 * u) /
-                         (c1 + fw_exp((T)(-0.1) * (u + (T)32.0)));
+                beta_j = (T)0.6 * mexp((T)0.057 * u) /
+                         (c1 + mexp((T)(-0.1) * (u + (T)32.0)));
             } else {
-                alpha_h = (T)0.057 * fw_exp(-(u + (T)80.0) / (T)6.8);
-                beta_h = (T)2.7 * fw_exp((T)0.079 * u) +
-                         (T)310000.0 * fw_exp((T)0.3485 * u);
-                alpha_j = ((T)(-25428.0) * fw_exp((T)0.2444 * u) -
-                           (T)6.948e-06 * fw_exp((T)(-0.04391) * u)) *
-                          (u + (T)37.78) / (c1 + fw_exp((T)0.311 * (u + (T)79.23)));
-                beta_j = (T)0.02424 * fw_exp((T)(-0.01052) * u) /
-                         (c1 + fw_exp((T)(-0.1378) * (u + (T)40.14)));
+                alpha_h = (T)0.057 * mexp(-(u + (T)80.0) / (T)6.8);
+                beta_h = (T)2.7 * mexp((T)0.079 * u) +
+                         (T)310000.0 * mexp((T)0.3485 * u);
+                alpha_j = ((T)(-25428.0) * mexp((T)0.2444 * u) -
+                           (T)6.948e-06 * mexp((T)(-0.04391) * u)) *
+                          (u + (T)37.78) / (c1 + mexp((T)0.311 * (u + (T)79.23)));
+                beta_j = (T)0.02424 * mexp((T)(-0.01052) * u) /
+                         (c1 + mexp((T)(-0.1378) * (u + (T)40.14)));
             }
             const T tau_h = c1 / (alpha_h + beta_h);
-            const T e_h = fw_exp((u + (T)71.55) / (T)7.43);
+            const T e_h = mexp((u + (T)71.55) / (T)7.43);
             const T h_inf = c1 / ((c1 + e_h) * (c1 + e_h));
             const T tau_j = c1 / (alpha_j + beta_j);
             const T j_inf = h_inf;
-            x.m = m_inf - (m_inf - x.m) * fw_exp(-dt / tau_m);
-            x.h = h_inf - (h_inf - x.h) * fw_exp(-dt / tau_h);
-            x.j = j_inf - (j_inf - x.j) * fw_exp(-dt / tau_j);
+            x.m = m_inf - (m_inf - x.m) * mexp(-dt / tau_m);
+            x.h = h_inf - (h_inf - x.h) * mexp(-dt / tau_h);
+            x.j = j_inf - (j_inf - x.j) * mexp(-dt / tau_j);
             ina = P.v[gna] * x.m * x.m * x.m * x.h * x.j * (u - Ena);
         }
         // calc_ical
         T ical;
         {
             const T FF = P.v[F], RT = P.v[R] * P.v[T_];
-            const T d_inf = c1 / (c1 + fw_exp(((T)(-8) - u) / (T)7.5));
-            const T Ad = (T)1.4 / (c1 + fw_exp(((T)(-35) - u) / (T)13)) + (T)0.25;
-            const T Bd = (T)1.4 / (c1 + fw_exp((u + (T)5) / (T)5));
-            const T Cd = c1 / (c1 + fw_exp(((T)50 - u) / (T)20));
+            const T d_inf = c1 / (c1 + mexp(((T)(-8) - u) / (T)7.5));
+            const T Ad = (T)1.4 / (c1 + mexp(((T)(-35) - u) / (T)13)) + (T)0.25;
+            const T Bd = (T)1.4 / (c1 + mexp((u + (T)5) / (T)5));
+            const T Cd = c1 / (c1 + mexp(((T)50 - u) / (T)20));
             const T tau_d = Ad * Bd + Cd;
-            const T f_inf = c1 / (c1 + fw_exp((u + (T)20) / (T)7));
-            const T Af = (T)1102.5 * fw_exp(-(u + (T)27) * (u + (T)27) / (T)225);
-            const T Bf = (T)200.0 / (c1 + fw_exp(((T)13 - u) / (T)10.0));
-            const T Cf = (T)180.0 / (c1 + fw_exp((u + (T)30) / (T)10)) + (T)20;
+            const T f_inf = c1 / (c1 + mexp((u + (T)20) / (T)7));
+            const T Af = (T)1102.5 * mexp(-(u + (T)27) * (u + (T)27) / (T)225);
+            const T Bf = (T)200.0 / (c1 + mexp(((T)13 - u) / (T)10.0));
+            const T Cf = (T)180.0 / (c1 + mexp((u + (T)30) / (T)10)) + (T)20;
             const T tau_f = Af + Bf + Cf;
-            const T f2_inf = (T)0.67 / (c1 + fw_exp((u + (T)35) / (T)7)) + (T)0.33;
-            const T Af2 = (T)600 * fw_exp(-(u + (T)25) * (u + (T)25) / (T)170);
-            const T Bf2 = (T)31 / (c1 + fw_exp(((T)25 - u) / (T)10));
-            const T Cf2 = (T)16 / (c1 + fw_exp((u + (T)30) / (T)10));
+            const T f2_inf = (T)0.67 / (c1 + mexp((u + (T)35) / (T)7)) + (T)0.33;
+            const T Af2 = (T)600 * mexp(-(u + (T)25) * (u + (T)25) / (T)170);
+            const T Bf2 = (T)31 / (c1 + mexp(((T)25 - u) / (T)10));
+            const T Cf2 = (T)16 / (c1 + mexp((u + (T)30) / (T)10));
             const T tau_f2 = Af2 + Bf2 + Cf2;
             const T q = cass / (T)0.05 * (cass / (T)0.05);
             const T fcass_inf = (T)0.6 / (c1 + q) + (T)0.4;
             const T tau_fcass = (T)80.0 / (c1 + q) + (T)2.0;
-            x.d = d_inf - (d_inf - x.d) * fw_exp(-dt / tau_d);
-            x.f = f_inf - (f_inf - x.f) * fw_exp(-dt / tau_f);
-            x.f2 = f2_inf - (f2_inf - x.f2) * fw_exp(-dt / tau_f2);
-            x.fcass = fcass_inf - (fcass_inf - x.fcass) * fw_exp(-dt / tau_fcass);
-            const T e2 = fw_exp((T)2 * (u - (T)15) * FF / RT);
+            x.d = d_inf - (d_inf - x.d) * mexp(-dt / tau_d);
+            x.f = f_inf - (f_inf - x.f) * mexp(-dt / tau_f);
+            x.f2 = f2_inf - (f2_inf - x.f2) * mexp(-dt / tau_f2);
+            x.fcass = fcass_inf - (fcass_inf - x.fcass) * mexp(-dt / tau_fcass);
+            const T e2 = mexp((T)2 * (u - (T)15) * FF / RT);
             ical = P.v[gcal] * x.d * x.f * x.f2 * x.fcass * (T)4 * (u - (T)15) *
                    (FF * FF / RT) * ((T)0.25 * e2 * cass - P.v[cao]) / (e2 - c1);
         }
         // calc_ito
         T ito;
         {
-            const T r_inf = c1 / (c1 + fw_exp(((T)20 - u) / (T)6.0));
-            const T s_inf = c1 / (c1 + fw_exp((u + (T)20) / (T)5.0));
+            const T r_inf = c1 / (c1 + mexp(((T)20 - u) / (T)6.0));
+            const T s_inf = c1 / (c1 + mexp((u + (T)20) / (T)5.0));
             const T tau_r =
-                (T)9.5 * fw_exp(-(u + (T)40.0) * (u + (T)40.0) / (T)1800.0) + (T)0.8;
+                (T)9.5 * mexp(-(u + (T)40.0) * (u + (T)40.0) / (T)1800.0) + (T)0.8;
             const T tau_s =
-                (T)85.0 * fw_exp(-(u + (T)45.0) * (u + (T)45.0) / (T)320.0) +
-                (T)5.0 / (c1 + fw_exp((u - (T)20.0) / (T)5.0)) + (T)3.0;
-            x.s = s_inf - (s_inf - x.s) * fw_exp(-dt / tau_s);
-            x.r = r_inf - (r_inf - x.r) * fw_exp(-dt / tau_r);
+                (T)85.0 * mexp(-(u + (T)45.0) * (u + (T)45.0) / (T)320.0) +
+                (T)5.0 / (c1 + mexp((u - (T)20.0) / (T)5.0)) + (T)3.0;
+            x.s = s_inf - (s_inf - x.s) * mexp(-dt / tau_s);
+            x.r = r_inf - (r_inf - x.r) * mexp(-dt / tau_r);
             ito = P.v[gto] * x.r * x.s * (u - Ek);
         }
         // calc_ikr
         T ikr;
         {
-            const T xr1_inf = c1 / (c1 + fw_exp(((T)(-26.0) - u) / (T)7.0));
-            const T axr1 = (T)450.0 / (c1 + fw_exp(((T)(-45.0) - u) / (T)10.0));
-            const T bxr1 = (T)6.0 / (c1 + fw_exp((u - (T)(-30.0)) / (T)11.5));
+            const T xr1_inf = c1 / (c1 + mexp(((T)(-26.0) - u) / (T)7.0));
+            const T axr1 = (T)450.0 / (c1 + mexp(((T)(-45.0) - u) / (T)10.0));
+            const T bxr1 = (T)6.0 / (c1 + mexp((u - (T)(-30.0)) / (T)11.5));
             const T tau_xr1 = axr1 * bxr1;
-            const T xr2_inf = c1 / (c1 + fw_exp((u - (T)(-88.0)) / (T)24.0));
-            const T axr2 = (T)3.0 / (c1 + fw_exp(((T)(-60.0) - u) / (T)20.0));
-            const T bxr2 = (T)1.12 / (c1 + fw_exp((u - (T)60.0) / (T)20.0));
+            const T xr2_inf = c1 / (c1 + mexp((u - (T)(-88.0)) / (T)24.0));
+            const T axr2 = (T)3.0 / (c1 + mexp(((T)(-60.0) - u) / (T)20.0));
+            const T bxr2 = (T)1.12 / (c1 + mexp((u - (T)60.0) / (T)20.0));
             const T tau_xr2 = axr2 * bxr2;
-            x.xr1 = xr1_inf - (xr1_inf - x.xr1) * fw_exp(-dt / tau_xr1);
-            x.xr2 = xr2_inf - (xr2_inf - x.xr2) * fw_exp(-dt / tau_xr2);
+            x.xr1 = xr1_inf - (xr1_inf - x.xr1) * mexp(-dt / tau_xr1);
+            x.xr2 = xr2_inf - (xr2_inf - x.xr2) * mexp(-dt / tau_xr2);
             ikr = P.v[gkr] * fw_sqrt(P.v[ko] / (T)5.4) * x.xr1 * x.xr2 * (u - Ek);
         }
         // calc_iks
         T iks;
         {
-            const T Axs = (T)1400.0 / fw_sqrt(c1 + fw_exp(((T)5.0 - u) / (T)6));
-            const T Bxs = c1 / (c1 + fw_exp((u - (T)35.0) / (T)15.0));
+            const T Axs = (T)1400.0 / fw_sqrt(c1 + mexp(((T)5.0 - u) / (T)6));
+            const T Bxs = c1 / (c1 + mexp((u - (T)35.0) / (T)15.0));
             const T tau_xs = Axs * Bxs + (T)80;
-            const T xs_inf = c1 / (c1 + fw_exp(((T)(-5.0) - u) / (T)14.0));
-            x.xs = xs_inf - (xs_inf - x.xs) * fw_exp(-dt / tau_xs);
+            const T xs_inf = c1 / (c1 + mexp(((T)(-5.0) - u) / (T)14.0));
+            x.xs = xs_inf - (xs_inf - x.xs) * mexp(-dt / tau_xs);
             iks = P.v[gks] * x.xs * x.xs * (u - Eks);
         }
         // calc_ik1
-        const T ak1 = (T)0.1 / (c1 + fw_exp((T)0.06 * (u - Ek - (T)200)));
-        const T bk1 = ((T)3.0 * fw_exp((T)0.0002 * (u - Ek + (T)100)) +
-                       fw_exp((T)0.1 * (u - Ek - (T)10))) /
-                      (c1 + fw_exp((T)(-0.5) * (u - Ek)));
+        const T ak1 = (T)0.1 / (c1 + mexp((T)0.06 * (u - Ek - (T)200)));
+        const T bk1 = ((T)3.0 * mexp((T)0.0002 * (u - Ek + (T)100)) +
+                       mexp((T)0.1 * (u - Ek - (T)10))) /
+                      (c1 + mexp((T)(-0.5) * (u - Ek)));
         const T ik1 = P.v[gk1] * (ak1 / (ak1 + bk1)) * (u - Ek);
         // calc_inaca, calc_inak
         const T RT = P.v[R] * P.v[T_];
@@ -263,16 +288,16 @@ struct ModelTP06 {
             (c1 / (P.v[KmNai] * P.v[KmNai] * P.v[KmNai] +
                    P.v[nao] * P.v[nao] * P.v[nao])) *
             (c1 / (P.v[KmCa] + P.v[cao])) *
-            (c1 / (c1 + P.v[ksat] * fw_exp((P.v[n_] - c1) * u * P.v[F] / RT))) *
-            (fw_exp(P.v[n_] * u * P.v[F] / RT) * nai * nai * nai * P.v[cao] -
-             fw_exp((P.v[n_] - c1) * u * P.v[F] / RT) * P.v[nao] * P.v[nao] *
+            (c1 / (c1 + P.v[ksat] * mexp((P.v[n_] - c1) * u * P.v[F] / RT))) *
+            (mexp(P.v[n_] * u * P.v[F] / RT) * nai * nai * nai * P.v[cao] -
+             mexp((P.v[n_] - c1) * u * P.v[F] / RT) * P.v[nao] * P.v[nao] *
                  P.v[nao] * cai * (T)2.5);
-        const T rec_iNaK = c1 / (c1 + (T)0.1245 * fw_exp((T)(-0.1) * u * P.v[F] / RT) +
-                                 (T)0.0353 * fw_exp(-u * P.v[F] / RT));
+        const T rec_iNaK = c1 / (c1 + (T)0.1245 * mexp((T)(-0.1) * u * P.v[F] / RT) +
+                                 (T)0.0353 * mexp(-u * P.v[F] / RT));
         const T inak = P.v[knak] * (P.v[ko] / (P.v[ko] + P.v[KmK])) *
                        (nai / (nai + P.v[KmNa])) * rec_iNaK;
         const T ipca = P.v[gpca] * cai / (P.v[KpCa] + cai);
-        const T ipk = P.v[gpk] * (c1 / (c1 + fw_exp(((T)25 - u) / (T)5.98))) * (u - Ek);
+        const T ipk = P.v[gpk] * (c1 / (c1 + mexp(((T)25 - u) / (T)5.98))) * (u - Ek);
         const T ibna = P.v[gbna] * (u - Ena);
         const T ibca = P.v[gbca] * (u - Eca);
         // calc_irel
@@ -287,29 +312,38 @@ struct ModelTP06 {
         const T ileak = P.v[Vleak] * (casr - cai);
         const T iup = P.v[Vmaxup] / (c1 + P.v[Kup] * P.v[Kup] / (cai * cai));
         const T ixfer = P.v[Vxfer] * (cass - cai);
-        // calc_casr, calc_cass in float64 (concentrations)
-        {
-            const double Bsr = (double)P.v[Bufsr], Ksr = (double)P.v[Kbufsr];
-            const double CaCSQN = Bsr * x.casr / (x.casr + Ksr);
-            const double dCaSR = dtd * ((double)iup - (double)irel - (double)ileak);
-            const double bjsr = Bsr - CaCSQN - dCaSR - x.casr + Ksr;
-            const double cjsr = Ksr * (CaCSQN + dCaSR + x.casr);
-            const double Bss = (double)P.v[Bufss], Kss = (double)P.v[Kbufss];
-            const double CaSSBuf = Bss * x.cass / (x.cass + Kss);
-            const double dCaSS =
-                dtd * (-(double)ixfer * (Vcd / Vssd) +
-                       (double)irel * ((double)P.v[Vsr] / Vssd) +
-                       -(double)ical * inversevssF2 * CAPd);
-            const double bcss = Bss - CaSSBuf - dCaSS - x.cass + Kss;
-            const double ccss = Kss * (CaSSBuf + dCaSS + x.cass);
-            x.casr = (sqrt(bjsr * bjsr + 4 * cjsr) - bjsr) / 2;
-            x.cass = (sqrt(bcss * bcss + 4 * ccss) - bcss) / 2;
+        // calc_casr, calc_cass (tp06_2d.py:793-873), calc_nai, calc_ki
+        // (:924-966); calc_cai is discarded by the reference
+        const T dCaSR = dt * (iup - irel - ileak);
+        const T dCaSS = dt * (-ixfer * (P.v[Vc] / P.v[Vss]) +
+                              irel * (P.v[Vsr] / P.v[Vss]) +
+                              -ical * inversevssF2 * P.v[CAPACITANCE]);
+        const T dNai = dt * (-(ina + ibna + (T)3 * inak + (T)3 * inaca) *
+                             inverseVcF * P.v[CAPACITANCE]);
+        const T dKi = dt * (-(ik1 + ito + ikr + iks - (T)2 * inak + ipk) *
+                            inverseVcF * P.v[CAPACITANCE]);
+        if constexpr (sizeof(T) == 8) {
+            // the reference's quadratic for the free SR / subspace calcium
+            const T CaCSQN = P.v[Bufsr] * casr / (casr + P.v[Kbufsr]);
+            const T bjsr = P.v[Bufsr] - CaCSQN - dCaSR - casr + P.v[Kbufsr];
+            const T cjsr = P.v[Kbufsr] * (CaCSQN + dCaSR + casr);
+            const T CaSSBuf = P.v[Bufss] * cass / (cass + P.v[Kbufss]);
+            const T bcss = P.v[Bufss] - CaSSBuf - dCaSS - cass + P.v[Kbufss];
+            const T ccss = P.v[Kbufss] * (CaSSBuf + dCaSS + cass);
+            x.casr = (fw_sqrt(bjsr * bjsr + 4 * cjsr) - bjsr) / 2;
+            x.cass = (fw_sqrt(bcss * bcss + 4 * ccss) - bcss) / 2;
+            x.nai += dNai;
+            x.Ki += dKi;
+        } else {
+            // float32 rates, float64 accumulation: the new free calcium is
+            // c0 + delta, delta the root near zero of the same quadratic
+            // shifted to c0 (see buffered_step), so only the addition needs
+            // the float64 state
+            x.casr += (double)buffered_step(casr, P.v[Bufsr], P.v[Kbufsr], dCaSR);
+            x.cass += (double)buffered_step(cass, P.v[Bufss], P.v[Kbufss], dCaSS);
+            x.nai += (double)dNai;
+            x.Ki += (double)dKi;
         }
-        // calc_cai is discarded by the reference; calc_nai, calc_ki
-        x.nai += dtd * (-((double)ina + (double)ibna + 3 * (double)inak +
-                          3 * (double)inaca) * inverseVcF * CAPd);
-        x.Ki += dtd * (-((double)ik1 + (double)ito + (double)ikr + (double)iks -
-                         2 * (double)inak + (double)ipk) * inverseVcF * CAPd);
         return un - dt * (ikr + iks + ik1 + ito + ina + ibna + ical + ibca + inak +
                           inaca + ipca + ipk);
     }
@@ -418,7 +452,7 @@ struct ModelCRN {
     template <class T>
     __device__ static __forceinline__ T gate(T x, T x_inf, T tau, T dt)
     {
-        return x_inf - (x_inf - x) * fw_exp(-dt / tau);
+        return x_inf - (x_inf - x) * mexp(-dt / tau);
     }
 
     // ionic_kernel_2d and its helpers (courtemanche_2d.py:180-641)
@@ -427,14 +461,12 @@ struct ModelCRN {
                                                const Params<T, NP> &P, T dt)
     {
         const T c1 = (T)1;
-        const double dtd = (double)dt;
-        const T RTF = P.v[R] * P.v[T_] / P.v[F];
-        const T ena = RTF * fw_log((T)((double)P.v[nao] / x.nai));
-        const T ek = RTF * fw_log((T)((double)P.v[ko] / x.ki));
-        const T eca = P.v[R] * P.v[T_] / ((T)2 * P.v[F]) *
-                      fw_log((T)((double)P.v[cao] / x.cai));
         const T cai = (T)x.cai, nai = (T)x.nai, carel = (T)x.carel;
-        const T caup = (T)x.caup;
+        const T caup = (T)x.caup, ki = (T)x.ki;
+        const T RTF = P.v[R] * P.v[T_] / P.v[F];
+        const T ena = RTF * mlog(P.v[nao] / nai);
+        const T ek = RTF * mlog(P.v[ko] / ki);
+        const T eca = P.v[R] * P.v[T_] / ((T)2 * P.v[F]) * mlog(P.v[cao] / cai);
         // calc_gating_m, calc_gating_h, calc_gating_j
         {
             T am;
@@ -442,84 +474,84 @@ struct ModelCRN {
                 am = (T)3.2;
             else
                 am = (T)0.32 * (u + (T)47.13) /
-                     (c1 - fw_exp((T)(-0.1) * (u + (T)47.13)));
-            const T bm = (T)0.08 * fw_exp(-u / (T)11);
+                     (c1 - mexp((T)(-0.1) * (u + (T)47.13)));
+            const T bm = (T)0.08 * mexp(-u / (T)11);
             x.m = gate(x.m, am / (am + bm), c1 / (am + bm), dt);
-            T ah = (T)0.135 * fw_exp(-((T)80 + u) / (T)6.8);
-            T bh = (T)3.56 * fw_exp((T)0.079 * u) + (T)310000 * fw_exp((T)0.35 * u);
-            T aj = ((T)(-127140) * fw_exp((T)0.2444 * u) -
-                    (T)3.474e-05 * fw_exp((T)(-0.04391) * u)) *
-                   (u + (T)37.78) / (c1 + fw_exp((T)0.311 * (u + (T)79.23)));
-            T bj = (T)0.1212 * fw_exp((T)(-0.01052) * u) /
-                   (c1 + fw_exp((T)(-0.1378) * (u + (T)40.14)));
+            T ah = (T)0.135 * mexp(-((T)80 + u) / (T)6.8);
+            T bh = (T)3.56 * mexp((T)0.079 * u) + (T)310000 * mexp((T)0.35 * u);
+            T aj = ((T)(-127140) * mexp((T)0.2444 * u) -
+                    (T)3.474e-05 * mexp((T)(-0.04391) * u)) *
+                   (u + (T)37.78) / (c1 + mexp((T)0.311 * (u + (T)79.23)));
+            T bj = (T)0.1212 * mexp((T)(-0.01052) * u) /
+                   (c1 + mexp((T)(-0.1378) * (u + (T)40.14)));
             if (u >= (T)(-40)) {
                 ah = (T)0;
-                bh = c1 / ((T)0.13 * (c1 + fw_exp(-(u + (T)10.66) / (T)11.1)));
+                bh = c1 / ((T)0.13 * (c1 + mexp(-(u + (T)10.66) / (T)11.1)));
                 aj = (T)0;
-                bj = (T)0.3 * fw_exp((T)(-2.535e-07) * u) /
-                     (c1 + fw_exp((T)(-0.1) * (u + (T)32)));
+                bj = (T)0.3 * mexp((T)(-2.535e-07) * u) /
+                     (c1 + mexp((T)(-0.1) * (u + (T)32)));
             }
             x.h = gate(x.h, ah / (ah + bh), c1 / (ah + bh), dt);
             const T j_inf = aj / (aj + bj);
             const T tau_j = c1 / (aj + bj);
-            x.j = j_inf - (j_inf - x.j) * fw_exp(-dt / tau_j);
+            x.j = j_inf - (j_inf - x.j) * mexp(-dt / tau_j);
         }
-        const T ina = P.v[gna] * fpow(x.m, (T)3) * x.h * x.j * (u - ena);
-        const T ik1 = P.v[gk1] * (u - ek) / (c1 + fw_exp((T)0.07 * (u + (T)80)));
+        const T ina = P.v[gna] * pow3(x.m) * x.h * x.j * (u - ena);
+        const T ik1 = P.v[gk1] * (u - ek) / (c1 + mexp((T)0.07 * (u + (T)80)));
         T ito, ikur;
         {
-            const T ao = (T)0.65 / (fw_exp(-(u + (T)10) / (T)8.5) +
-                                    fw_exp(-(u - (T)30) / (T)59.0));
-            const T bo = (T)0.65 / ((T)2.5 + fw_exp((u + (T)82) / (T)17.0));
+            const T ao = (T)0.65 / (mexp(-(u + (T)10) / (T)8.5) +
+                                    mexp(-(u - (T)30) / (T)59.0));
+            const T bo = (T)0.65 / ((T)2.5 + mexp((u + (T)82) / (T)17.0));
             const T tau_o = c1 / (P.v[kq10] * (ao + bo));
-            const T o_inf = c1 / (c1 + fw_exp(-(u + (T)20.47) / (T)17.54));
-            const T aoi = c1 / ((T)18.53 + fw_exp((u + (T)113.7) / (T)10.95));
-            const T boi = c1 / ((T)35.56 + fw_exp(-(u + (T)1.26) / (T)7.44));
+            const T o_inf = c1 / (c1 + mexp(-(u + (T)20.47) / (T)17.54));
+            const T aoi = c1 / ((T)18.53 + mexp((u + (T)113.7) / (T)10.95));
+            const T boi = c1 / ((T)35.56 + mexp(-(u + (T)1.26) / (T)7.44));
             const T tau_oi = c1 / (P.v[kq10] * (aoi + boi));
-            const T oi_inf = c1 / (c1 + fw_exp((u + (T)43.1) / (T)5.3));
+            const T oi_inf = c1 / (c1 + mexp((u + (T)43.1) / (T)5.3));
             x.oa = gate(x.oa, o_inf, tau_o, dt);
             x.oi = gate(x.oi, oi_inf, tau_oi, dt);
-            ito = P.v[gto] * fpow(x.oa, (T)3) * x.oi * (u - ek);
-            const T gkur = (T)0.005 + (T)0.05 / (c1 + fw_exp(-(u - (T)15) / (T)13.0));
+            ito = P.v[gto] * pow3(x.oa) * x.oi * (u - ek);
+            const T gkur = (T)0.005 + (T)0.05 / (c1 + mexp(-(u - (T)15) / (T)13.0));
             const T tau_ua = c1 / (P.v[kq10] * (ao + bo));
-            const T ua_inf = c1 / (c1 + fw_exp(-(u + (T)30.3) / (T)9.6));
-            const T aui = c1 / ((T)21 + fw_exp(-(u - (T)185) / (T)28.0));
-            const T bui = fw_exp((u - (T)158) / (T)16.0);
+            const T ua_inf = c1 / (c1 + mexp(-(u + (T)30.3) / (T)9.6));
+            const T aui = c1 / ((T)21 + mexp(-(u - (T)185) / (T)28.0));
+            const T bui = mexp((u - (T)158) / (T)16.0);
             const T tau_ui = c1 / (P.v[kq10] * (aui + bui));
-            const T ui_inf = c1 / (c1 + fw_exp((u - (T)99.45) / (T)27.48));
+            const T ui_inf = c1 / (c1 + mexp((u - (T)99.45) / (T)27.48));
             x.ua = gate(x.ua, ua_inf, tau_ua, dt);
             x.ui = gate(x.ui, ui_inf, tau_ui, dt);
-            ikur = P.v[gkur_coeff] * gkur * fpow(x.ua, (T)3) * x.ui * (u - ek);
+            ikur = P.v[gkur_coeff] * gkur * pow3(x.ua) * x.ui * (u - ek);
         }
         T ikr, iks;
         {
             // the model's xs holds the IKr gate, xr the IKs gate
             const T axr = (T)0.0003 * (u + (T)14.1) /
-                          (c1 - fw_exp(-(u + (T)14.1) / (T)5));
+                          (c1 - mexp(-(u + (T)14.1) / (T)5));
             const T bxr = (T)7.3898e-05 * (u - (T)3.3328) /
-                          (fw_exp((u - (T)3.3328) / (T)5.1237) - c1);
+                          (mexp((u - (T)3.3328) / (T)5.1237) - c1);
             const T tau_xr = c1 / (axr + bxr);
-            const T xr_inf = c1 / (c1 + fw_exp(-(u + (T)14.1) / (T)6.5));
+            const T xr_inf = c1 / (c1 + mexp(-(u + (T)14.1) / (T)6.5));
             x.xs = gate(x.xs, xr_inf, tau_xr, dt);
-            ikr = (T)0.0294 * x.xs * (u - ek) / (c1 + fw_exp((u + (T)15) / (T)22.4));
+            ikr = (T)0.0294 * x.xs * (u - ek) / (c1 + mexp((u + (T)15) / (T)22.4));
             const T axs = (T)4e-05 * (u - (T)19.9) /
-                          (c1 - fw_exp(-(u - (T)19.9) / (T)17));
+                          (c1 - mexp(-(u - (T)19.9) / (T)17));
             const T bxs = (T)3.5e-05 * (u - (T)19.9) /
-                          (fw_exp((u - (T)19.9) / (T)9) - c1);
+                          (mexp((u - (T)19.9) / (T)9) - c1);
             const T tau_xs = c1 / ((T)2 * (axs + bxs));
-            const T xs_inf = c1 / fw_sqrt(c1 + fw_exp(-(u - (T)19.9) / (T)12.7));
+            const T xs_inf = c1 / fw_sqrt(c1 + mexp(-(u - (T)19.9) / (T)12.7));
             x.xr = gate(x.xr, xs_inf, tau_xs, dt);
             iks = P.v[gks] * (x.xr * x.xr) * (u - ek);
         }
         T ical;
         {
-            const T e = fw_exp(-(u + (T)10) / (T)6.24);
+            const T e = mexp(-(u + (T)10) / (T)6.24);
             const T tau_d = (c1 - e) / ((T)0.035 * (u + (T)10) * (c1 + e));
-            const T d_inf = c1 / (c1 + fw_exp(-(u + (T)10) / (T)8.0));
-            const T tau_f = (T)9 / ((T)0.0197 * fw_exp(-((T)0.0337 * (T)0.0337) *
+            const T d_inf = c1 / (c1 + mexp(-(u + (T)10) / (T)8.0));
+            const T tau_f = (T)9 / ((T)0.0197 * mexp(-((T)0.0337 * (T)0.0337) *
                                                       ((u + (T)10) * (u + (T)10))) +
                                     (T)0.02);
-            const T f_inf = c1 / (c1 + fw_exp((u + (T)28) / (T)6.9));
+            const T f_inf = c1 / (c1 + mexp((u + (T)28) / (T)6.9));
             const T fca_inf = c1 / (c1 + cai / (T)0.00035);
             x.d = gate(x.d, d_inf, tau_d, dt);
             x.f = gate(x.f, f_inf, tau_f, dt);
@@ -529,18 +561,18 @@ struct ModelCRN {
         const T RT = P.v[R] * P.v[T_];
         T inak, inaca;
         {
-            const T s = c1 / (T)7.0 * (fw_exp(P.v[nao] / (T)67.3) - c1);
-            const T fnak = c1 / (c1 + (T)0.1245 * fw_exp((T)(-0.1) * (P.v[F] * u) / RT) +
-                                 (T)0.0365 * s * fw_exp(-(P.v[F] * u) / RT));
-            inak = P.v[inakmax] * fnak * (c1 / (c1 + fpow(P.v[kmnai] / nai, (T)1.5))) *
+            const T s = c1 / (T)7.0 * (mexp(P.v[nao] / (T)67.3) - c1);
+            const T fnak = c1 / (c1 + (T)0.1245 * mexp((T)(-0.1) * (P.v[F] * u) / RT) +
+                                 (T)0.0365 * s * mexp(-(P.v[F] * u) / RT));
+            inak = P.v[inakmax] * fnak * (c1 / (c1 + pow15(P.v[kmnai] / nai))) *
                    (P.v[ko] / (P.v[ko] + P.v[kmko]));
             const T gamma = (T)0.35;
-            const T exp_term = fw_exp(gamma * (P.v[F] * u) / RT);
-            const T exp_rev_term = fw_exp((gamma - c1) * (P.v[F] * u) / RT);
+            const T exp_term = mexp(gamma * (P.v[F] * u) / RT);
+            const T exp_rev_term = mexp((gamma - c1) * (P.v[F] * u) / RT);
             const T numerator = P.v[inacamax] *
-                                (exp_term * fpow(nai, (T)3) * P.v[cao] -
-                                 exp_rev_term * fpow(P.v[nao], (T)3) * cai);
-            const T term1 = fpow(P.v[kmnancx], (T)3) + fpow(P.v[nao], (T)3);
+                                (exp_term * pow3(nai) * P.v[cao] -
+                                 exp_rev_term * pow3(P.v[nao]) * cai);
+            const T term1 = pow3(P.v[kmnancx]) + pow3(P.v[nao]);
             const T term2 = P.v[kmcancx] + P.v[cao];
             const T term3 = c1 + P.v[ksatncx] * exp_rev_term;
             inaca = numerator / (term1 * term2 * term3);
@@ -551,13 +583,13 @@ struct ModelCRN {
         {
             const T Fn = (T)1e-12 * P.v[Vrel] * x.irel -
                          (T)5 * (T)1e-13 / P.v[F] * ((T)0.5 * ical - (T)0.2 * inaca);
-            const T u_inf = c1 / (c1 + fw_exp(-(Fn - (T)3.4175e-13) / (T)1.367e-15));
-            const T tau_v = (T)1.91 + (T)2.09 / (c1 + fw_exp(-(Fn - (T)3.4175e-13) /
+            const T u_inf = c1 / (c1 + mexp(-(Fn - (T)3.4175e-13) / (T)1.367e-15));
+            const T tau_v = (T)1.91 + (T)2.09 / (c1 + mexp(-(Fn - (T)3.4175e-13) /
                                                            (T)1.367e-15));
-            const T v_inf = c1 - c1 / (c1 + fw_exp(-(Fn - (T)6.835e-14) / (T)1.367e-15));
-            const T ew = fw_exp(-(u - (T)7.9) / (T)5.0);
+            const T v_inf = c1 - c1 / (c1 + mexp(-(Fn - (T)6.835e-14) / (T)1.367e-15));
+            const T ew = mexp(-(u - (T)7.9) / (T)5.0);
             const T tau_w = (T)6 * (c1 - ew) / ((c1 + (T)0.3 * ew) * (u - (T)7.9));
-            const T w_inf = c1 - c1 / (c1 + fw_exp(-(u - (T)40) / (T)17.0));
+            const T w_inf = c1 - c1 / (c1 + mexp(-(u - (T)40) / (T)17.0));
             x.urel = gate(x.urel, u_inf, (T)8, dt);
             x.vrel = gate(x.vrel, v_inf, tau_v, dt);
             x.wrel = gate(x.wrel, w_inf, tau_w, dt);
@@ -566,31 +598,29 @@ struct ModelCRN {
         const T itr = (caup - carel) / (T)180;
         const T iup = P.v[iupmax] / (c1 + P.v[kup] / cai);
         const T iupleak = caup / P.v[caupmax] * P.v[iupmax];
-        // concentrations in float64
-        const double Fd = (double)P.v[F], Vjd = (double)P.v[Vj],
-                     Vupd = (double)P.v[Vup], Vreld = (double)P.v[Vrel];
-        x.caup += dtd * ((double)iup - (double)iupleak - (double)itr * (Vreld / Vupd));
-        x.nai += dtd * ((-3 * (double)inak - 3 * (double)inaca - (double)ibna -
-                         (double)ina) / (Fd * Vjd));
-        x.ki += dtd * ((2 * (double)inak - (double)ik1 - (double)ito - (double)ikur -
-                        (double)ikr - (double)iks - (double)P.v[ibk]) / (Fd * Vjd));
-        {
-            const double ci = x.cai;
-            const double ktr = (double)P.v[kmtrpn], kcm = (double)P.v[kmcmdn];
-            const double B1 = (2 * (double)inaca - (double)ipca - (double)ical -
-                               (double)ibca) / (2 * Fd * Vjd) +
-                              (Vupd * ((double)iupleak - (double)iup) +
-                               (double)x.irel * Vreld) / Vjd;
-            const double B2 = 1 + (double)P.v[trpnmax] * ktr / ((ci + ktr) * (ci + ktr)) +
-                              (double)P.v[cmdnmax] * kcm / ((ci + kcm) * (ci + kcm));
-            x.cai += dtd * (B1 / B2);
-        }
-        {
-            const double kcs = (double)P.v[kmcsqn];
-            x.carel += dtd * (((double)itr - (double)x.irel) /
-                              (1 + (double)P.v[csqnmax] * kcs /
-                                       ((x.carel + kcs) * (x.carel + kcs))));
-        }
+        // calc_caup, calc_nai, calc_ki, calc_cai, calc_carel
+        // (courtemanche_2d.py:219-253); under float32 the rates are float32
+        // and only the accumulation is float64
+        const T FVj = P.v[F] * P.v[Vj];
+        const T dCaup = dt * (iup - iupleak - itr * (P.v[Vrel] / P.v[Vup]));
+        const T dNai = dt * (((T)(-3) * inak - (T)3 * inaca - ibna - ina) / FVj);
+        const T dKi = dt * (((T)2 * inak - ik1 - ito - ikur - ikr - iks -
+                             P.v[ibk]) / FVj);
+        const T ktr = P.v[kmtrpn], kcm = P.v[kmcmdn];
+        const T B1 = ((T)2 * inaca - ipca - ical - ibca) / ((T)2 * FVj) +
+                     (P.v[Vup] * (iupleak - iup) + x.irel * P.v[Vrel]) / P.v[Vj];
+        const T B2 = c1 + P.v[trpnmax] * ktr / ((cai + ktr) * (cai + ktr)) +
+                     P.v[cmdnmax] * kcm / ((cai + kcm) * (cai + kcm));
+        const T dCai = dt * (B1 / B2);
+        const T kcs = P.v[kmcsqn];
+        const T dCarel = dt * ((itr - x.irel) /
+                               (c1 + P.v[csqnmax] * kcs /
+                                         ((carel + kcs) * (carel + kcs))));
+        x.caup += dCaup;
+        x.nai += dNai;
+        x.ki += dKi;
+        x.cai += dCai;
+        x.carel += dCarel;
         return un - dt * (ina + ik1 + ito + ikur + ikr + iks + ical + ipca + inak +
                           inaca + ibna + ibca);
     }
