@@ -38,8 +38,8 @@ __device__ __forceinline__ double fw_log(double x) { return log(x); }
 __device__ __forceinline__ float fw_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double fw_sqrt(double x) { return sqrt(x); }
 
-template <class T, int N>
-__device__ __forceinline__ Params<T, N> load_params(const double *p)
+template <class T, int N, class S>
+__device__ __forceinline__ Params<T, N> load_params(const S *p)
 {
     Params<T, N> r;
 #pragma unroll

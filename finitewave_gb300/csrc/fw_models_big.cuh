@@ -63,6 +63,7 @@ __device__ __forceinline__ float buffered_step(float c0, float B, float K,
 // (:1003-1012); state in TP062D.state_vars order minus u (:77-79).
 struct ModelTP06 {
     static constexpr int NS = 19, NP = 49;
+    static constexpr int kMinBlocksF32 = 4;  // 64 registers, no spills
     enum {
         ko, cao, nao, Vc, Vsr, Vss, Bufc, Kbufc, Bufsr, Kbufsr, Bufss, Kbufss,
         Vmaxup, Kup, Vrel, k1_, k2_, k3, k4, EC, maxsr, minsr, Vleak, Vxfer, R,
@@ -354,6 +355,7 @@ struct ModelTP06 {
 // (:569-577); state in Courtemanche2D.state_vars order minus u (:118-120).
 struct ModelCRN {
     static constexpr int NS = 21, NP = 39;
+    static constexpr int kMinBlocksF32 = 3;  // 4 would spill
     enum {
         gna, gnab, gk1, gkr, gks, gto, gcal, gcab, gkur_coeff, F, T_, R, Vc, Vj,
         Vup, Vrel, ibk, cao, nao, ko, caupmax, kup, kmnai, kmko, kmnancx,

@@ -62,13 +62,18 @@ __global__ void k_stim(StimK<T> s)
     }
 }
 
+// Thresholds, parameters and dt are held in the kernel's precision T,
+// rounded on the host: a float32 kernel then does no float64 conversions
+// (GB300's float64 pipe is a small fraction of its float32 rate).
+template <class T>
 struct AtK {
-    double thr;
+    T thr;
     int32_t *act;
 };
 
+template <class T>
 struct LatK {
-    double thr;
+    T thr;
     uint8_t *activated;
     int32_t *steps;
     int32_t *count;
@@ -82,13 +87,13 @@ struct StepK {
     const T *u;
     T *un;
     void *state[FW_MAX_STATE];
-    double params[FW_MAX_PARAMS];
-    double dt;
+    T params[FW_MAX_PARAMS];
+    T dt;
     int64_t n, si, sj;
     int64_t step;
     int32_t n_at, n_lat;
-    AtK at[FW_MAX_AT];
-    LatK lat[FW_MAX_LAT];
+    AtK<T> at[FW_MAX_AT];
+    LatK<T> lat[FW_MAX_LAT];
     int32_t *status;
 };
 
@@ -97,14 +102,14 @@ __device__ __forceinline__ void track(const StepK<T> &k, int64_t p, T uc)
 {
     for (int a = 0; a < k.n_at; ++a) {
         // (act_t < 0) & (u > threshold)  (activation_time_2d_tracker.py:61-63)
-        if (uc > (T)k.at[a].thr && k.at[a].act[p] < 0)
+        if (uc > k.at[a].thr && k.at[a].act[p] < 0)
             k.at[a].act[p] = (int32_t)k.step;
     }
     for (int l = 0; l < k.n_lat; ++l) {
         // cross_threshold (local_activation_time_2d_tracker.py:71-89)
-        const LatK &L = k.lat[l];
+        const LatK<T> &L = k.lat[l];
         uint8_t act = L.activated[p];
-        if (uc >= (T)L.thr && !act) {
+        if (uc >= L.thr && !act) {
             L.activated[p] = 1;
             int32_t c = L.count[p];
             if (c < L.cap)
@@ -112,17 +117,30 @@ __device__ __forceinline__ void track(const StepK<T> &k, int64_t p, T uc)
             else if (k.status)
                 atomicOr(k.status, FW_DEV_LAT_OVERFLOW);
             L.count[p] = c + 1;
-        } else if (uc < (T)L.thr && act) {
+        } else if (uc < L.thr && act) {
             L.activated[p] = 0;
         }
     }
 }
 
+// Minimum resident CTAs per SM asked of the compiler for the float32
+// k_step: models may set M::kMinBlocksF32 (the detailed models trade
+// registers for the occupancy their memory latency needs); 1 otherwise.
+template <class M, class T, class = void>
+struct MinBlocks {
+    static constexpr int value = 1;
+};
+template <class M>
+struct MinBlocks<M, float, decltype(void(M::kMinBlocksF32))> {
+    static constexpr int value = M::kMinBlocksF32;
+};
+
 template <class M, int ST, class T>
-__global__ void __launch_bounds__(kThreads) k_step(StepK<T> k)
+__global__ void __launch_bounds__(kThreads, (MinBlocks<M, T>::value))
+    k_step(StepK<T> k)
 {
     const Params<T, M::NP> P = load_params<T, M::NP>(k.params);
-    const T dt = (T)k.dt;
+    const T dt = k.dt;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < k.n;
          p += (int64_t)gridDim.x * blockDim.x) {
         T uc = k.u[p];
@@ -198,8 +216,8 @@ struct IonicK {
     T *un;
     const T *u;
     void *state[FW_MAX_STATE];
-    double params[FW_MAX_PARAMS];
-    double dt;
+    T params[FW_MAX_PARAMS];
+    T dt;
     const int64_t *idx;
     int64_t n_idx;
 };
@@ -208,7 +226,7 @@ template <class M, class T>
 __global__ void k_ionic(IonicK<M, T> k)
 {
     const Params<T, M::NP> P = load_params<T, M::NP>(k.params);
-    const T dt = (T)k.dt;
+    const T dt = k.dt;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
          t < k.n_idx; t += (int64_t)gridDim.x * blockDim.x) {
         int64_t p = k.idx[t];
@@ -266,8 +284,8 @@ int run_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     k.myo = a->myo;
     k.w = (const T *)a->weights;
     for (int i = 0; i < FW_MAX_STATE; ++i) k.state[i] = a->state[i];
-    for (int i = 0; i < FW_MAX_PARAMS; ++i) k.params[i] = a->params[i];
-    k.dt = a->dt;
+    for (int i = 0; i < FW_MAX_PARAMS; ++i) k.params[i] = (T)a->params[i];
+    k.dt = (T)a->dt;
     k.n = g.n;
     k.si = g.si;
     k.sj = g.sj;
@@ -298,12 +316,13 @@ int run_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         k.n_at = 0;
         for (int i = 0; i < a->n_at; ++i)
             if (in_window(a->at[i].win, n))
-                k.at[k.n_at++] = AtK{a->at[i].threshold, a->at[i].act_step};
+                k.at[k.n_at++] = AtK<T>{(T)a->at[i].threshold,
+                                        a->at[i].act_step};
         k.n_lat = 0;
         for (int i = 0; i < a->n_lat; ++i)
             if (in_window(a->lat[i].win, n)) {
                 const fw_lat_tracker &L = a->lat[i];
-                k.lat[k.n_lat++] = LatK{L.threshold, L.activated,
+                k.lat[k.n_lat++] = LatK<T>{(T)L.threshold, L.activated,
                                         L.cross_steps, L.cross_count,
                                         L.capacity};
             }
@@ -340,8 +359,9 @@ int run_ionic(void *u_new, const void *u, void *const *state,
     k.un = (T *)u_new;
     k.u = (const T *)u;
     for (int i = 0; i < FW_MAX_STATE; ++i) k.state[i] = i < M::NS ? state[i] : nullptr;
-    for (int i = 0; i < FW_MAX_PARAMS; ++i) k.params[i] = i < M::NP ? params[i] : 0.0;
-    k.dt = dt;
+    for (int i = 0; i < FW_MAX_PARAMS; ++i)
+        k.params[i] = i < M::NP ? (T)params[i] : (T)0;
+    k.dt = (T)dt;
     k.idx = idx;
     k.n_idx = n_idx;
     if (n_idx > 0) k_ionic<M, T><<<grid_for(n_idx, kThreads), kThreads, 0, stream>>>(k);
