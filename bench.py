@@ -32,6 +32,11 @@ rotating -60..+60 degrees through the depth, AsymmetricStencil3D, S1-S2,
 16 probes), plain form, float32 with float64 ion concentrations next to
 float64.
 
+``serving``: a trace of simulation requests (Poisson arrivals at 50/s;
+TP06 / Courtemanche; 2D tissues and 3D left-ventricle shells; float32 with
+float64 concentrations) served in real time by SimulationServer under an HBM
+budget: p50 / p99 latency, queueing and service times, myocyte-steps/s.
+
 ``--impl reference`` times the reference's algorithm on the host cores: the
 C restatement of its numba kernels (oracle/fw_oracle.c, OpenMP over all
 cores, float64, precomputed weights) on the same workload, a bounded number
@@ -329,6 +334,110 @@ def run_tp06_slab(args, fg, torch, reps):
                          "kernel": "k_step<ModelTP06, ANISO19, float>"}}
 
 
+# serving trace: Poisson arrivals of TP06 / Courtemanche requests
+SERVE_RATE = 50.0          # requests per second
+SERVE_REQUESTS = 40
+SERVE_MS = (5.0, 20.0)     # simulated time per request (ms), scaled down
+
+
+def lv_shell(n, wall, rng):
+    """A truncated ellipsoidal shell on an n^3 grid (left-ventricle-like):
+    outer semi-axes 0.45 n, 0.45 n, 0.7 n around (n/2, n/2, 0.75 n), wall
+    `wall` nodes thick, cut at the centre plane; fibers in the wall's
+    tangent plane at an angle rotating linearly from +60 deg (endocardium)
+    to -60 deg (epicardium) with the normalised wall depth."""
+    c = np.array([n / 2, n / 2, 0.75 * n])
+    ax = np.array([0.45 * n, 0.45 * n, 0.7 * n])
+    g = np.stack(np.meshgrid(*[np.arange(n) + 0.5] * 3, indexing="ij"), -1) - c
+    rho = np.sqrt(((g / ax) ** 2).sum(-1))
+    rho_i = np.sqrt(((g / (ax - wall)) ** 2).sum(-1))
+    shell = (rho <= 1.0) & (rho_i > 1.0) & (g[..., 2] <= 0)
+    mesh = shell.astype(np.int8)
+    depth = np.clip((rho_i - 1.0) / np.maximum(rho_i - rho, 1e-9), 0.0, 1.0)
+    alpha = np.deg2rad(60.0 - 120.0 * depth)
+    normal = g / ax ** 2
+    normal /= np.maximum(np.linalg.norm(normal, axis=-1, keepdims=True), 1e-12)
+    e_c = np.cross(np.array([0.0, 0.0, 1.0]), g)
+    nc = np.linalg.norm(e_c, axis=-1, keepdims=True)
+    e_c = np.where(nc > 1e-9, e_c / np.maximum(nc, 1e-12),
+                   np.array([1.0, 0.0, 0.0]))
+    e_l = np.cross(normal, e_c)
+    e_l /= np.maximum(np.linalg.norm(e_l, axis=-1, keepdims=True), 1e-12)
+    fib = np.cos(alpha)[..., None] * e_c + np.sin(alpha)[..., None] * e_l
+    del rng
+    return mesh, fib
+
+
+def serving_trace(fg, n_requests=SERVE_REQUESTS, seed=SEED):
+    """The serving configuration, scaled to finish in seconds: Poisson
+    arrivals at 50 requests/s; 70 % 2D tissues with side U[256, 2048], 30 %
+    3D left-ventricle shells on 64^3..128^3 grids (wall 8-16 nodes, fibers
+    rotating +-60 deg transmurally); model TP06 or Courtemanche; 5-20 ms of
+    simulated time each (the full configuration's 500-2000 ms is two orders
+    of magnitude more work than one GPU serves in minutes); float32 state
+    with float64 concentrations; a current stimulus at t = 0 and an
+    activation-time tracker (threshold -20 mV)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    reqs = []
+    for i in range(n_requests):
+        t += rng.exponential(1.0 / SERVE_RATE)
+        tp06 = bool(rng.integers(2))
+        dur = float(rng.uniform(*SERVE_MS))
+        if rng.random() < 0.7:
+            side = int(rng.integers(256, 2049))
+            tissue = fg.CardiacTissue2D((side, side))
+            model = fg.TP062D() if tp06 else fg.Courtemanche2D()
+            stim = fg.StimCurrentCoord2D(0, 100, 1.0, 0, side, 1, 6)
+        else:
+            n = int(rng.integers(64, 129))
+            wall = int(rng.integers(8, 17))
+            mesh, fib = lv_shell(n, wall, rng)
+            tissue = fg.CardiacTissue3D((n, n, n))
+            tissue.mesh = mesh
+            tissue.fibers = fib
+            model = fg.TP063D() if tp06 else fg.Courtemanche3D()
+            st = fg.AsymmetricStencil3D()
+            st.D_al, st.D_ac = 1.0, 0.25
+            model.stencil = st
+            zs = np.flatnonzero(mesh.any(axis=(0, 1)))
+            z0 = int(zs[0]) if zs.size else 1
+            stim = fg.StimCurrentCoord3D(0, 100, 1.0, 0, n, 0, n, z0, z0 + 4)
+        model.dt, model.dr, model.t_max = 0.01, 0.25, dur
+        model.npfloat = "float32"
+        model.cardiac_tissue = tissue
+        seq = fg.StimSequence()
+        seq.add_stim(stim)
+        model.stim_sequence = seq
+        at = fg.ActivationTime2DTracker()
+        at.threshold = -20.0
+        trs = fg.TrackerSequence()
+        trs.add_tracker(at)
+        model.tracker_sequence = trs
+        reqs.append(fg.Request(model, arrival=t, name=f"r{i}"))
+    return reqs
+
+
+def run_serving(args, fg, torch, reps):
+    """The serving trace through SimulationServer in real time."""
+    reqs = serving_trace(fg, args.serving_requests)
+    server = fg.SimulationServer(chunk=args.serving_chunk)
+    server.serve(reqs, realtime=True)
+    torch.cuda.synchronize()
+    st = server.stats()
+    n2 = sum(isinstance(r.model.cardiac_tissue, fg.CardiacTissue2D)
+             for r in reqs)
+    st.update({"unit": UNIT, "requests": len(reqs), "requests_2d": n2,
+               "arrival_rate_per_s": SERVE_RATE,
+               "simulated_ms_per_request": list(SERVE_MS),
+               "chunk_steps": args.serving_chunk,
+               "value_note": "myocyte-steps of the completed requests / "
+                             "(last finish - first arrival)"})
+    if reps.world > 1:
+        st["value"] = reps.whole_job(st["myocyte_steps"], st["makespan_s"])
+    return st
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -486,9 +595,10 @@ def run_gb300(args):
     from finitewave_gb300 import _ffi
     _ffi.load()
 
-    if args.only in ("tp06", "batched"):
+    if args.only in ("tp06", "batched", "serving"):
         # one sub-measurement alone (profiling runs); not the bench line
-        fn = run_tp06_slab if args.only == "tp06" else run_batched
+        fn = {"tp06": run_tp06_slab, "batched": run_batched,
+              "serving": run_serving}[args.only]
         r = fn(args, fg, torch, reps)
         if rank == 0:
             print(json.dumps({"only": args.only, **r}), flush=True)
@@ -592,6 +702,10 @@ def run_gb300(args):
     if not args.no_tp06:
         tp06 = run_tp06_slab(args, fg, torch, reps)
 
+    serving = None
+    if not args.no_serving:
+        serving = run_serving(args, fg, torch, reps)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(mesh, fibers, args.cpu_seconds)
@@ -624,6 +738,7 @@ def run_gb300(args):
                          "time_steps_per_launch": steps_per_launch},
             "batched": batched,
             "tp06_slab": tp06,
+            "serving": serving,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks,
@@ -723,7 +838,12 @@ def main():
     ap.add_argument("--batched-tissues", type=int, default=N_TISSUES)
     ap.add_argument("--no-tp06", action="store_true",
                     help="skip the TP06 slab measurement")
-    ap.add_argument("--only", default=None, choices=[None, "tp06", "batched"],
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the serving trace")
+    ap.add_argument("--serving-requests", type=int, default=SERVE_REQUESTS)
+    ap.add_argument("--serving-chunk", type=int, default=500)
+    ap.add_argument("--only", default=None,
+                    choices=[None, "tp06", "batched", "serving"],
                     help="run one sub-measurement alone (profiling)")
     ap.add_argument("--slab", type=int, nargs=3, default=list(SLAB),
                     help="TP06 slab shape (profiling runs use a smaller one)")

@@ -16,6 +16,7 @@ from .model import (AlievPanfilov2D, AlievPanfilov3D, CardiacModel,
                     Courtemanche2D, Courtemanche3D, FentonKarma2D,
                     FentonKarma3D, MitchellSchaeffer2D, MitchellSchaeffer3D,
                     TP062D, TP063D)
+from .serving import Request, SimulationServer, device_footprint
 from .state import StateLoader, StateSaver, StateSaverCollection
 from .stencil import (AsymmetricStencil2D, AsymmetricStencil3D,
                       IsotropicStencil2D, IsotropicStencil3D, Stencil)

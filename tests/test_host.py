@@ -267,3 +267,27 @@ def test_diffuse_patterns_match_reference():
     ref = g["d2_full"].copy()
     ref[0, :] = ref[-1, :] = ref[:, 0] = ref[:, -1] = 0
     assert np.array_equal(np.asarray(t.mesh), ref)
+
+
+def test_device_footprint():
+    """The admission estimate of the request loop: bytes per node of u,
+    u_new, mesh, myo, state (float64 concentrations under float32 for the
+    detailed models), weights, packed weights and trackers."""
+    import finitewave_gb300 as fg
+    t = fg.CardiacTissue2D((50, 40))
+    t.fibers = np.zeros((50, 40, 2))
+    t.fibers[..., 0] = 1
+    m = fg.AlievPanfilov2D()
+    m.npfloat = "float32"
+    m.cardiac_tissue = t
+    trs = fg.TrackerSequence()
+    trs.add_tracker(fg.ActivationTime2DTracker())
+    m.tracker_sequence = trs
+    assert fg.device_footprint(m) == 50 * 40 * (2 * 4 + 2 + 4 + 9 * 4 +
+                                                8 * 4 + 4)
+    t3 = fg.CardiacTissue3D((10, 12, 14))
+    m3 = fg.TP063D()
+    m3.npfloat = "float32"
+    m3.cardiac_tissue = t3
+    assert fg.device_footprint(m3) == 10 * 12 * 14 * (
+        2 * 4 + 2 + 5 * 8 + 14 * 4 + 7 * 4)
