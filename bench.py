@@ -37,6 +37,12 @@ TP06 / Courtemanche; 2D tissues and 3D left-ventricle shells; float32 with
 float64 concentrations) served in real time by SimulationServer under an HBM
 budget: p50 / p99 latency, queueing and service times, myocyte-steps/s.
 
+``accuracy_f32_vs_f64``: the float32 forms against the float64 plain form
+on an Aliev-Panfilov 1024^2 S1-S2 run (the 4096^2 generator, t = 120) and a
+TP06 192^2 run through one action potential (350 ms): max |dV|, activation
+and local-activation time errors in steps, APD90 error at 16 probes,
+conduction-velocity error in percent.
+
 ``--impl reference`` times the reference's algorithm on the host cores: the
 C restatement of its numba kernels (oracle/fw_oracle.c, OpenMP over all
 cores, float64, precomputed weights) on the same workload, a bounded number
@@ -70,13 +76,13 @@ SEED = 1234
 B_ALG = {"float32": 2 * (4 + 4) + 1 + 2 * 4, "float64": 2 * (8 + 8) + 1 + 2 * 8}
 
 
-def workload_inputs(n=N, seed=SEED):
+def workload_inputs(n=N, seed=SEED, sigma=64.0):
     import scipy.ndimage as nd
     np.random.seed(seed)
     mesh = (1 + (np.random.random((n, n)) <= 0.2)).astype(np.int8)
     mesh[0, :] = mesh[-1, :] = mesh[:, 0] = mesh[:, -1] = 0
     g = np.random.default_rng(seed).standard_normal((n, n)).astype(np.float32)
-    g = nd.gaussian_filter(g, 64.0)
+    g = nd.gaussian_filter(g, sigma)
     theta = (np.pi / 4) * g / np.abs(g).max()
     fibers = np.stack([np.cos(theta), np.sin(theta)], -1).astype(np.float64)
     return mesh, fibers
@@ -438,6 +444,130 @@ def run_serving(args, fg, torch, reps):
     return st
 
 
+def _accuracy_pair(fg, build, probes_at):
+    """Run one configuration in float64 (plain) and float32 (default form)
+    and compare them with finitewave_gb300.metrics."""
+    from finitewave_gb300 import metrics
+    import torch
+    out = {}
+    runs = {}
+    for prec in ("float64", "float32"):
+        model, at, lat, pr = build(prec)
+        t0 = time.perf_counter()
+        model.run()
+        torch.cuda.synchronize()
+        runs[prec] = dict(u=model.u.astype(np.float64), at=at.act_t,
+                          lat_count=lat._count.cpu().numpy(),
+                          lat_steps=lat._steps.cpu().numpy(),
+                          probes=np.asarray(pr.output["u"], np.float64),
+                          seconds=time.perf_counter() - t0,
+                          dt=model.dt, dr=model.dr,
+                          myo=model._myo_d.cpu().numpy().astype(bool),
+                          form=("fused" if model._form() == 1 else "plain"))
+        del model
+        torch.cuda.empty_cache()
+    a, b = runs["float32"], runs["float64"]
+    myo = b["myo"]
+    within, worst, one = metrics.activation_error_steps(a["at"], b["at"],
+                                                        b["dt"], myo)
+    lw, lworst, ldiff = metrics.lat_error_steps(
+        a["lat_count"], a["lat_steps"], b["lat_count"], b["lat_steps"], myo)
+    apd_a = [metrics.apd90(a["probes"][:, c], b["dt"])
+             for c in range(b["probes"].shape[1])]
+    apd_b = [metrics.apd90(b["probes"][:, c], b["dt"])
+             for c in range(b["probes"].shape[1])]
+    d_apd = [abs(x - y) for x, y in zip(apd_a, apd_b)
+             if x is not None and y is not None]
+    out.update({
+        "max_abs_dV_field": float(np.abs(a["u"] - b["u"])[myo].max()),
+        "max_abs_dV_probes": float(np.abs(a["probes"] - b["probes"]).max()),
+        "at_within_1_step": within, "at_max_err_steps": worst,
+        "at_nodes_activated_in_one_only": one,
+        "lat_within_1_step": lw, "lat_max_err_steps": lworst,
+        "lat_nodes_count_differs": ldiff,
+        "apd90_max_err": max(d_apd) if d_apd else None,
+        "apd90_probes": len(d_apd),
+        "cv_err_percent": metrics.cv_error_percent(a["at"], b["at"], b["dr"],
+                                                   myo),
+        "form_f32": a["form"],
+        "seconds": {"float64": b["seconds"], "float32": a["seconds"]}})
+    return out
+
+
+def accuracy_ap(fg, n=1024, t_max=120.0):
+    """Aliev-Panfilov 2D n x n, the 4096^2 configuration's generator
+    (fibrosis 0.2, fibers smoothed with sigma = n / 64), S1-S2, to t_max."""
+    mesh, fibers = workload_inputs(n, sigma=n / 64.0)
+
+    def build(prec):
+        model, at = build_model(fg, mesh, fibers, prec, None, init=False)
+        model.t_max = t_max
+        lat = fg.LocalActivationTime2DTracker()
+        lat.threshold, lat.capacity = 0.5, 8
+        model.tracker_sequence.add_tracker(lat)
+        pr = fg.MultiVariable2DTracker()
+        cells = np.argwhere(mesh == 1)
+        pr.cell_ind = cells[np.random.default_rng(SEED).choice(
+            len(cells), 16, replace=False)].tolist()
+        pr.var_list = ["u"]
+        model.tracker_sequence.add_tracker(pr)
+        return model, at, lat, pr
+    return build
+
+
+def accuracy_tp06(fg, n=192, t_max=350.0):
+    """TP06 2D n x n, 10 % fibrosis, smooth fibers, S1 from the left edge,
+    to t_max (one full action potential)."""
+    import scipy.ndimage as nd
+    rng = np.random.default_rng(SEED)
+    mesh = (1 + (rng.random((n, n)) <= 0.1)).astype(np.int8)
+    g = nd.gaussian_filter(rng.standard_normal((n, n)), n / 32.0)
+    theta = (np.pi / 4) * g / np.abs(g).max()
+    fibers = np.stack([np.cos(theta), np.sin(theta)], -1)
+
+    def build(prec):
+        tissue = fg.CardiacTissue2D((n, n))
+        tissue.mesh = mesh.copy()
+        tissue.fibers = fibers
+        model = fg.TP062D()
+        st = fg.AsymmetricStencil2D()
+        st.D_al, st.D_ac = 1.0, 0.25
+        model.stencil = st
+        model.dt, model.dr, model.t_max = 0.01, 0.25, t_max
+        model.npfloat = prec
+        model.cardiac_tissue = tissue
+        seq = fg.StimSequence()
+        seq.add_stim(fg.StimCurrentCoord2D(0, 100, 1.0, 0, n, 1, 6))
+        model.stim_sequence = seq
+        at = fg.ActivationTime2DTracker()
+        at.threshold = -20.0
+        lat = fg.LocalActivationTime2DTracker()
+        lat.threshold, lat.capacity = -20.0, 4
+        pr = fg.MultiVariable2DTracker()
+        cells = np.argwhere(np.asarray(tissue.mesh) == 1)
+        pr.cell_ind = cells[rng.choice(len(cells), 16,
+                                       replace=False)].tolist()
+        pr.var_list = ["u"]
+        trs = fg.TrackerSequence()
+        for t in (at, lat, pr):
+            trs.add_tracker(t)
+        model.tracker_sequence = trs
+        return model, at, lat, pr
+    return build
+
+
+def run_accuracy(args, fg, torch, reps):
+    """Float32 against float64 on two configurations: max |dV|, activation
+    and local activation time errors in steps, APD90 error at 16 probes,
+    conduction-velocity error in percent."""
+    return {"aliev_panfilov_2d_1024": dict(
+                units="normalised u; time in model units",
+                **_accuracy_pair(fg, accuracy_ap(fg), None)),
+            "tp06_2d_192": dict(
+                units="mV; ms",
+                **_accuracy_pair(fg, accuracy_tp06(fg), None))}
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -496,7 +626,7 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def build_model(fg, mesh, fibers, npfloat, form):
+def build_model(fg, mesh, fibers, npfloat, form, init=True):
     n = mesh.shape[0]
     tissue = fg.CardiacTissue2D(mesh.shape)
     tissue.mesh = mesh.copy()
@@ -519,7 +649,8 @@ def build_model(fg, mesh, fibers, npfloat, form):
     trs = fg.TrackerSequence()
     trs.add_tracker(at)
     model.tracker_sequence = trs
-    model.initialize()
+    if init:
+        model.initialize()
     return model, at
 
 
@@ -595,10 +726,10 @@ def run_gb300(args):
     from finitewave_gb300 import _ffi
     _ffi.load()
 
-    if args.only in ("tp06", "batched", "serving"):
+    if args.only in ("tp06", "batched", "serving", "accuracy"):
         # one sub-measurement alone (profiling runs); not the bench line
         fn = {"tp06": run_tp06_slab, "batched": run_batched,
-              "serving": run_serving}[args.only]
+              "serving": run_serving, "accuracy": run_accuracy}[args.only]
         r = fn(args, fg, torch, reps)
         if rank == 0:
             print(json.dumps({"only": args.only, **r}), flush=True)
@@ -702,6 +833,10 @@ def run_gb300(args):
     if not args.no_tp06:
         tp06 = run_tp06_slab(args, fg, torch, reps)
 
+    accuracy = None
+    if not args.no_accuracy:
+        accuracy = run_accuracy(args, fg, torch, reps)
+
     serving = None
     if not args.no_serving:
         serving = run_serving(args, fg, torch, reps)
@@ -739,6 +874,7 @@ def run_gb300(args):
             "batched": batched,
             "tp06_slab": tp06,
             "serving": serving,
+            "accuracy_f32_vs_f64": accuracy,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks,
@@ -838,12 +974,15 @@ def main():
     ap.add_argument("--batched-tissues", type=int, default=N_TISSUES)
     ap.add_argument("--no-tp06", action="store_true",
                     help="skip the TP06 slab measurement")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the float32 vs float64 accuracy runs")
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the serving trace")
     ap.add_argument("--serving-requests", type=int, default=SERVE_REQUESTS)
     ap.add_argument("--serving-chunk", type=int, default=500)
     ap.add_argument("--only", default=None,
-                    choices=[None, "tp06", "batched", "serving"],
+                    choices=[None, "tp06", "batched", "serving",
+                             "accuracy"],
                     help="run one sub-measurement alone (profiling)")
     ap.add_argument("--slab", type=int, nargs=3, default=list(SLAB),
                     help="TP06 slab shape (profiling runs use a smaller one)")

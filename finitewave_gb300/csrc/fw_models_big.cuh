@@ -37,6 +37,18 @@ __device__ __forceinline__ float mexp(float x) { return __expf(x); }
 __device__ __forceinline__ double mexp(double x) { return exp(x); }
 __device__ __forceinline__ float mlog(float x) { return __logf(x); }
 __device__ __forceinline__ double mlog(double x) { return log(x); }
+// x / (e^x - 1), continuous through x = 0 where it is 1.  Several rates are
+// written in the reference as a difference quotient such as
+// (u - u0) / (exp(k (u - u0)) - 1), which is 0 / 0 at u = u0; in float64
+// that point is never met in practice, but in float32 the exponential
+// rounds to exactly 1 within ~1e-6 mV of u0 and the quotient becomes
+// inf or NaN.  The float32 forms use this function instead (series
+// 1 - x / 2 for |x| < 1e-4, where the next term is below 1e-9).
+__device__ __forceinline__ float x_expm1(float x)
+{
+    return fabsf(x) < 1e-4f ? 1.f - 0.5f * x : x / expm1f(x);
+}
+
 __device__ __forceinline__ float pow3(float x) { return x * x * x; }
 __device__ __forceinline__ double pow3(double x) { return pow(x, 3.0); }
 __device__ __forceinline__ float pow15(float x) { return x * sqrtf(x); }
@@ -233,9 +245,17 @@ struct ModelTP06 {
             x.f = f_inf - (f_inf - x.f) * mexp(-dt / tau_f);
             x.f2 = f2_inf - (f2_inf - x.f2) * mexp(-dt / tau_f2);
             x.fcass = fcass_inf - (fcass_inf - x.fcass) * mexp(-dt / tau_fcass);
-            const T e2 = mexp((T)2 * (u - (T)15) * FF / RT);
-            ical = P.v[gcal] * x.d * x.f * x.f2 * x.fcass * (T)4 * (u - (T)15) *
-                   (FF * FF / RT) * ((T)0.25 * e2 * cass - P.v[cao]) / (e2 - c1);
+            const T z = (T)2 * (u - (T)15) * FF / RT;
+            const T e2 = mexp(z);
+            if constexpr (sizeof(T) == 8) {
+                ical = P.v[gcal] * x.d * x.f * x.f2 * x.fcass * (T)4 *
+                       (u - (T)15) * (FF * FF / RT) *
+                       ((T)0.25 * e2 * cass - P.v[cao]) / (e2 - c1);
+            } else {
+                // 4 (u - 15) F^2 / RT / (e2 - 1) = 2 F z / (e^z - 1)
+                ical = P.v[gcal] * x.d * x.f * x.f2 * x.fcass * (T)2 * FF *
+                       x_expm1(z) * ((T)0.25 * e2 * cass - P.v[cao]);
+            }
         }
         // calc_ito
         T ito;
@@ -472,11 +492,15 @@ struct ModelCRN {
         // calc_gating_m, calc_gating_h, calc_gating_j
         {
             T am;
-            if (u == (T)(-47.13))
-                am = (T)3.2;
-            else
-                am = (T)0.32 * (u + (T)47.13) /
-                     (c1 - mexp((T)(-0.1) * (u + (T)47.13)));
+            if constexpr (sizeof(T) == 8) {
+                if (u == (T)(-47.13))
+                    am = (T)3.2;
+                else
+                    am = (T)0.32 * (u + (T)47.13) /
+                         (c1 - mexp((T)(-0.1) * (u + (T)47.13)));
+            } else {
+                am = (T)3.2 * x_expm1((T)(-0.1) * (u + (T)47.13));
+            }
             const T bm = (T)0.08 * mexp(-u / (T)11);
             x.m = gate(x.m, am / (am + bm), c1 / (am + bm), dt);
             T ah = (T)0.135 * mexp(-((T)80 + u) / (T)6.8);
@@ -528,18 +552,31 @@ struct ModelCRN {
         T ikr, iks;
         {
             // the model's xs holds the IKr gate, xr the IKs gate
-            const T axr = (T)0.0003 * (u + (T)14.1) /
-                          (c1 - mexp(-(u + (T)14.1) / (T)5));
-            const T bxr = (T)7.3898e-05 * (u - (T)3.3328) /
-                          (mexp((u - (T)3.3328) / (T)5.1237) - c1);
+            T axr, bxr;
+            if constexpr (sizeof(T) == 8) {
+                axr = (T)0.0003 * (u + (T)14.1) /
+                      (c1 - mexp(-(u + (T)14.1) / (T)5));
+                bxr = (T)7.3898e-05 * (u - (T)3.3328) /
+                      (mexp((u - (T)3.3328) / (T)5.1237) - c1);
+            } else {
+                axr = (T)(0.0003 * 5) * x_expm1(-(u + (T)14.1) / (T)5);
+                bxr = (T)(7.3898e-05 * 5.1237) *
+                      x_expm1((u - (T)3.3328) / (T)5.1237);
+            }
             const T tau_xr = c1 / (axr + bxr);
             const T xr_inf = c1 / (c1 + mexp(-(u + (T)14.1) / (T)6.5));
             x.xs = gate(x.xs, xr_inf, tau_xr, dt);
             ikr = (T)0.0294 * x.xs * (u - ek) / (c1 + mexp((u + (T)15) / (T)22.4));
-            const T axs = (T)4e-05 * (u - (T)19.9) /
-                          (c1 - mexp(-(u - (T)19.9) / (T)17));
-            const T bxs = (T)3.5e-05 * (u - (T)19.9) /
-                          (mexp((u - (T)19.9) / (T)9) - c1);
+            T axs, bxs;
+            if constexpr (sizeof(T) == 8) {
+                axs = (T)4e-05 * (u - (T)19.9) /
+                      (c1 - mexp(-(u - (T)19.9) / (T)17));
+                bxs = (T)3.5e-05 * (u - (T)19.9) /
+                      (mexp((u - (T)19.9) / (T)9) - c1);
+            } else {
+                axs = (T)(4e-05 * 17) * x_expm1(-(u - (T)19.9) / (T)17);
+                bxs = (T)(3.5e-05 * 9) * x_expm1((u - (T)19.9) / (T)9);
+            }
             const T tau_xs = c1 / ((T)2 * (axs + bxs));
             const T xs_inf = c1 / fw_sqrt(c1 + mexp(-(u - (T)19.9) / (T)12.7));
             x.xr = gate(x.xr, xs_inf, tau_xs, dt);
@@ -548,7 +585,14 @@ struct ModelCRN {
         T ical;
         {
             const T e = mexp(-(u + (T)10) / (T)6.24);
-            const T tau_d = (c1 - e) / ((T)0.035 * (u + (T)10) * (c1 + e));
+            T tau_d;
+            if constexpr (sizeof(T) == 8) {
+                tau_d = (c1 - e) / ((T)0.035 * (u + (T)10) * (c1 + e));
+            } else {
+                // (1 - e^-v) / v = 1 / x_expm1(-v), v = (u + 10) / 6.24
+                tau_d = c1 / ((T)(0.035 * 6.24) *
+                              x_expm1(-(u + (T)10) / (T)6.24) * (c1 + e));
+            }
             const T d_inf = c1 / (c1 + mexp(-(u + (T)10) / (T)8.0));
             const T tau_f = (T)9 / ((T)0.0197 * mexp(-((T)0.0337 * (T)0.0337) *
                                                       ((u + (T)10) * (u + (T)10))) +
@@ -590,7 +634,13 @@ struct ModelCRN {
                                                            (T)1.367e-15));
             const T v_inf = c1 - c1 / (c1 + mexp(-(Fn - (T)6.835e-14) / (T)1.367e-15));
             const T ew = mexp(-(u - (T)7.9) / (T)5.0);
-            const T tau_w = (T)6 * (c1 - ew) / ((c1 + (T)0.3 * ew) * (u - (T)7.9));
+            T tau_w;
+            if constexpr (sizeof(T) == 8) {
+                tau_w = (T)6 * (c1 - ew) / ((c1 + (T)0.3 * ew) * (u - (T)7.9));
+            } else {
+                tau_w = (T)(6.0 / 5.0) /
+                        ((c1 + (T)0.3 * ew) * x_expm1(-(u - (T)7.9) / (T)5.0));
+            }
             const T w_inf = c1 - c1 / (c1 + mexp(-(u - (T)40) / (T)17.0));
             x.urel = gate(x.urel, u_inf, (T)8, dt);
             x.vrel = gate(x.vrel, v_inf, tau_v, dt);
