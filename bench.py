@@ -524,6 +524,10 @@ def accuracy_tp06(fg, n=192, t_max=350.0):
     g = nd.gaussian_filter(rng.standard_normal((n, n)), n / 32.0)
     theta = (np.pi / 4) * g / np.abs(g).max()
     fibers = np.stack([np.cos(theta), np.sin(theta)], -1)
+    interior = np.zeros((n, n), bool)
+    interior[1:-1, 1:-1] = True
+    cells = np.argwhere((mesh == 1) & interior)
+    probe_cells = cells[rng.choice(len(cells), 16, replace=False)].tolist()
 
     def build(prec):
         tissue = fg.CardiacTissue2D((n, n))
@@ -544,9 +548,7 @@ def accuracy_tp06(fg, n=192, t_max=350.0):
         lat = fg.LocalActivationTime2DTracker()
         lat.threshold, lat.capacity = -20.0, 4
         pr = fg.MultiVariable2DTracker()
-        cells = np.argwhere(np.asarray(tissue.mesh) == 1)
-        pr.cell_ind = cells[rng.choice(len(cells), 16,
-                                       replace=False)].tolist()
+        pr.cell_ind = probe_cells
         pr.var_list = ["u"]
         trs = fg.TrackerSequence()
         for t in (at, lat, pr):
