@@ -128,13 +128,15 @@ _STRUCTS = {0: StepArgs, 1: Stim, 2: AtTracker, 3: LatTracker,
 
 
 def load(path=None):
-    """Load (building first if needed) libfwgpu.so and return the handle."""
+    """Load (building first if needed) libfwgpu.so and return the handle.
+    The environment variable FWGPU_LIBRARY names a prebuilt library to load
+    instead."""
     global _lib
     with _lock:
         if _lib is not None:
             return _lib
         if path is None:
-            path = _build.build()
+            path = os.environ.get("FWGPU_LIBRARY") or _build.build()
         if not os.path.exists(path):
             raise OSError(f"libfwgpu not found at {path}")
         L = ctypes.CDLL(path)
