@@ -9,7 +9,11 @@
 //   * two stages: while the CTA computes tile i from one stage, the TMA
 //     fills the other with tile i + 1, so HBM traffic overlaps compute.
 // Every wait on an mbarrier is bounded; a timeout sets FW_DEV_TIMEOUT in the
-// status word and the CTA returns.
+// status word and the CTA returns.  Unlike the cp.async kernel, the sub-steps
+// form the diffusion sum as  w_c u + sum_k w_k u_k  in one FMA chain, with
+// the centre weight w_c = 1 - sum_k w_k computed once per tile from the
+// staged off-centre weights (9 FMA per node and sub-step instead of 17
+// operations for  u + sum_k w_k (u_k - u)).
 //
 // Layout requirements (checked by the host): nj % 16 == 0 (TMA row strides
 // and the int8 myocyte rows) and the packed weight array of fw_pack_weights.
@@ -242,6 +246,20 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             st[r] = M::template from_array<float>(sv);
         }
         upd &= myo_bits;
+        // centre weights of the strip: every stencil row sums to one, so
+        // w_c = 1 - sum of the off-centre weights; the sub-steps then form
+        // the reference's sum  w_c u + sum_k w_k u_k  as one FMA chain
+        float wcen[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float4 wa = G.wa[r0 + r][col];
+            float sw = wa.x + wa.y + wa.z + wa.w;
+            if constexpr (NWO == 8) {
+                const float4 wb = G.wb[r0 + r][col];
+                sw += wb.x + wb.y + wb.z + wb.w;
+            }
+            wcen[r] = 1.f - sw;
+        }
 
         // probe cells of this tile
         uint32_t probe_mine = 0;
@@ -371,19 +389,25 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             for (int r = 0; r < R; ++r) {
                 const float b1 = wc[r + 1];
                 const int lr = r0 + r;
-                float d;
+                float un = wcen[r] * b1;
                 const float4 wa = G.wa[lr][col];
                 if constexpr (ST == FW_STENCIL_ISO5) {
-                    d = wa.x * (wc[r] - b1) + wa.y * (wl[r + 1] - b1) +
-                        wa.z * (wr[r + 1] - b1) + wa.w * (wc[r + 2] - b1);
+                    un = fmaf(wa.x, wc[r], un);
+                    un = fmaf(wa.y, wl[r + 1], un);
+                    un = fmaf(wa.z, wr[r + 1], un);
+                    un = fmaf(wa.w, wc[r + 2], un);
                 } else {
                     const float4 wb = G.wb[lr][col];
-                    d = wa.x * (wl[r] - b1) + wa.y * (wc[r] - b1) +
-                        wa.z * (wr[r] - b1) + wa.w * (wl[r + 1] - b1) +
-                        wb.x * (wr[r + 1] - b1) + wb.y * (wl[r + 2] - b1) +
-                        wb.z * (wc[r + 2] - b1) + wb.w * (wr[r + 2] - b1);
+                    un = fmaf(wa.x, wl[r], un);
+                    un = fmaf(wa.y, wc[r], un);
+                    un = fmaf(wa.z, wr[r], un);
+                    un = fmaf(wa.w, wl[r + 1], un);
+                    un = fmaf(wb.x, wr[r + 1], un);
+                    un = fmaf(wb.y, wl[r + 2], un);
+                    un = fmaf(wb.z, wc[r + 2], un);
+                    un = fmaf(wb.w, wr[r + 2], un);
                 }
-                const float uu = M::template update<float>(b1, b1 + d, st[r], P, dt);
+                const float uu = M::template update<float>(b1, un, st[r], P, dt);
                 nxt[lr + 1][col + xo] = ((upd >> r) & 1u) ? uu : b1;
                 if (probes_now && ((probe_mine >> r) & 1u))
                     write_probes<M>(f, S.probe_list, S.probe_count, lr, col, s, b1,
