@@ -30,6 +30,7 @@ from .stimulation import (Stim, StimCurrent, StimCurrentArea2D,
 from .tissue import CardiacTissue, CardiacTissue2D, CardiacTissue3D
 from .tracker import (ActionPotential2DTracker, ActionPotential3DTracker,
                       ActivationTime2DTracker, ActivationTime3DTracker,
+                      ECG2DTracker, ECG3DTracker,
                       LocalActivationTime2DTracker,
                       LocalActivationTime3DTracker, MultiVariable2DTracker,
                       MultiVariable3DTracker, Tracker, TrackerSequence,

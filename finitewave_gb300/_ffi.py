@@ -34,6 +34,8 @@ MAX_AT = 4
 MAX_LAT = 2
 MAX_PROBE = 4
 MAX_PROBE_VARS = 8
+MAX_ECG = 2
+MAX_ECG_LEADS = 8
 
 STENCIL_NW = {ISO5: 5, ANISO9: 9, ISO7: 7, ANISO19: 19}
 
@@ -67,6 +69,12 @@ class ProbeTracker(ctypes.Structure):
                 ("out", _vp), ("sample_offset", _i64), ("capacity", _i64)]
 
 
+class EcgTracker(ctypes.Structure):
+    _fields_ = [("win", Window), ("n_leads", _i32), ("reserved", _i32),
+                ("coords", (_f64 * 3) * MAX_ECG_LEADS), ("dr", _f64),
+                ("out", _vp), ("sample_offset", _i64), ("capacity", _i64)]
+
+
 class StepArgs(ctypes.Structure):
     _fields_ = [("model", _i32), ("stencil", _i32), ("precision", _i32),
                 ("form", _i32), ("ni", _i64), ("nj", _i64), ("nk", _i64),
@@ -79,7 +87,9 @@ class StepArgs(ctypes.Structure):
                 ("lat", LatTracker * MAX_LAT),
                 ("probe", ProbeTracker * MAX_PROBE),
                 ("status", _vp), ("fused_k", _i32),
-                ("fused_variant", _i32), ("weights_packed", _vp)]
+                ("fused_variant", _i32), ("weights_packed", _vp),
+                ("n_ecg", _i32), ("reserved", _i32),
+                ("ecg", EcgTracker * MAX_ECG)]
 
 
 class Batch(ctypes.Structure):
@@ -114,6 +124,8 @@ _SIGS = {
                  _i32),
     "fw_step": ([ctypes.POINTER(StepArgs), _i64, _i64, _vp], _i32),
     "fw_pack_weights": ([_i32, _vp, _i64, _vp, _vp], _i32),
+    "fw_ecg": ([_i32, _i32, _vp, _vp, _vp, _i64, _i64, _i64, _vp, _i32, _f64,
+                _vp, _vp], _i32),
     "fw_batch_plan_size": ([_vp, _i32, ctypes.POINTER(_i64)], _i32),
     "fw_batch_plan": ([_vp, _i32, _vp, _vp, _i64, ctypes.POINTER(Batch),
                        _vp], _i32),
@@ -124,7 +136,7 @@ _SIGS = {
 
 # symbol -> ctypes structure whose size must match the library's
 _STRUCTS = {0: StepArgs, 1: Stim, 2: AtTracker, 3: LatTracker,
-            4: ProbeTracker, 5: Window, 6: Batch}
+            4: ProbeTracker, 5: Window, 6: Batch, 7: EcgTracker}
 
 
 def load(path=None):

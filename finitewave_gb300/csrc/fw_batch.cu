@@ -436,9 +436,9 @@ int check_tissue(const fw_step_args *a, int i)
                   (long long)a->ni, (long long)a->nj, (long long)a->nk);
         return FW_ERR_ARG;
     }
-    if (a->n_at > 1 || a->n_lat > 1 || a->n_probe != 0) {
+    if (a->n_at > 1 || a->n_lat > 1 || a->n_probe != 0 || a->n_ecg != 0) {
         set_error("fw_batch: tissue %d: at most one activation and one local "
-                  "activation tracker, no probes", i);
+                  "activation tracker, no probes or ECG", i);
         return FW_ERR_UNSUPPORTED;
     }
     if (a->n_stims < 0 || a->n_stims > FW_MAX_STIMS) {

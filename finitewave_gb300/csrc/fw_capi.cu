@@ -139,6 +139,24 @@ int check_step_args(const fw_step_args *a, int64_t n_steps)
                 return FW_ERR_ARG;
             }
     }
+    if (a->n_ecg < 0 || a->n_ecg > FW_MAX_ECG) {
+        set_error("fw_step: n_ecg %d out of range (0..%d)", a->n_ecg,
+                  FW_MAX_ECG);
+        return FW_ERR_ARG;
+    }
+    for (int i = 0; i < a->n_ecg; ++i) {
+        const fw_ecg_tracker &E = a->ecg[i];
+        if (!valid_window(E.win) || E.n_leads < 1 ||
+            E.n_leads > FW_MAX_ECG_LEADS || !E.out || E.capacity < 0 ||
+            E.sample_offset < 0) {
+            set_error("fw_step: ECG tracker %d invalid", i);
+            return FW_ERR_ARG;
+        }
+    }
+    if (a->n_ecg > 0 && a->form == FW_FORM_FUSED) {
+        set_error("fw_step: ECG trackers run in the plain form only");
+        return FW_ERR_UNSUPPORTED;
+    }
     return FW_OK;
 }
 
@@ -159,6 +177,7 @@ size_t fw_struct_size(int32_t which)
     case 4: return sizeof(fw_probe_tracker);
     case 5: return sizeof(fw_window);
     case 6: return sizeof(fw_batch);
+    case 7: return sizeof(fw_ecg_tracker);
     }
     return 0;
 }
@@ -245,6 +264,15 @@ int fw_step(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     if (a->form == FW_FORM_FUSED)
         return fw::step_fused(a, n_begin, n_steps, (cudaStream_t)stream);
     return fw::step_plain(a, n_begin, n_steps, (cudaStream_t)stream);
+}
+
+int fw_ecg(int32_t stencil, int32_t precision, const void *u, const void *w,
+           const int8_t *myo, int64_t ni, int64_t nj, int64_t nk,
+           const double *coords, int32_t n_leads, double dr, double *out,
+           void *stream)
+{
+    return fw::ecg(stencil, precision, u, w, myo, ni, nj, nk, coords, n_leads,
+                   dr, out, (cudaStream_t)stream);
 }
 
 int fw_batch_plan_size(const fw_step_args *const *tissues, int32_t n,

@@ -131,6 +131,10 @@ int ionic(int32_t model, int32_t precision, void *u_new, const void *u,
           const double *params, cudaStream_t stream);
 int step_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                cudaStream_t stream);
+int ecg(int32_t stencil, int32_t precision, const void *u, const void *w,
+        const int8_t *myo, int64_t ni, int64_t nj, int64_t nk,
+        const double *coords, int32_t n_leads, double dr, double *out,
+        cudaStream_t stream);
 int step_fused(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                cudaStream_t stream);
 int pack_weights(int32_t stencil, const float *w, int64_t n, float *out,

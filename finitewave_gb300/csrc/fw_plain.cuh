@@ -200,6 +200,98 @@ __global__ void k_probe(ProbeK<T> k)
     }
 }
 
+// ECG leads (ecg_2d_tracker.py:114-153, ecg_3d_tracker.py:99-140): per
+// myocyte the diffusion increment diffuse(u) - u weighted by 1 / (d dr),
+// d the squared distance to the lead; per-thread partial sums in T, a block
+// reduction in float64, one float64 atomic add per block and lead.
+template <class T>
+struct EcgK {
+    const T *u;
+    const T *w;
+    const int8_t *myo;
+    int64_t n, si, sj, nj, nk;
+    int32_t dim, n_leads;
+    T xyz[FW_MAX_ECG_LEADS][3];
+    T dr;
+    double *out;
+};
+
+template <int ST, class T>
+__global__ void __launch_bounds__(kThreads) k_ecg(EcgK<T> k)
+{
+    T acc[FW_MAX_ECG_LEADS];
+#pragma unroll
+    for (int c = 0; c < FW_MAX_ECG_LEADS; ++c) acc[c] = (T)0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < k.n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        if (!k.myo[p]) continue;
+        const T diff = diffuse_node<ST, T>(k.u, k.w, p, k.n, k.si, k.sj) - k.u[p];
+        T fi, fj, fk;
+        if (k.dim == 2) {
+            fi = (T)(p / k.nj);
+            fj = (T)(p % k.nj);
+            fk = (T)0;
+        } else {
+            const int64_t plane = k.nj * k.nk, r = p % plane;
+            fi = (T)(p / plane);
+            fj = (T)(r / k.nk);
+            fk = (T)(r % k.nk);
+        }
+#pragma unroll
+        for (int c = 0; c < FW_MAX_ECG_LEADS; ++c) {
+            if (c >= k.n_leads) break;
+            const T dx = k.xyz[c][0] - fi, dy = k.xyz[c][1] - fj,
+                    dz = k.xyz[c][2] - fk;
+            const T d = dx * dx + dy * dy + dz * dz;
+            if (d > (T)0) acc[c] += diff / (d * k.dr);
+        }
+    }
+    __shared__ double red[FW_MAX_ECG_LEADS][kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < FW_MAX_ECG_LEADS; ++c) {
+        double v = (double)acc[c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[c][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < FW_MAX_ECG_LEADS && (int)threadIdx.x < k.n_leads) {
+        double v = 0.0;
+        for (int q = 0; q < kThreads / 32; ++q) v += red[threadIdx.x][q];
+        atomicAdd(&k.out[threadIdx.x], v);
+    }
+}
+
+template <int ST, class T>
+int launch_ecg(const T *u, const T *w, const int8_t *myo, const Grid &g,
+               int dim, const double (*coords)[3], int n_leads, double dr,
+               double *out, cudaStream_t stream)
+{
+    if (n_leads < 1 || n_leads > FW_MAX_ECG_LEADS) {
+        set_error("ECG: %d leads (1..%d)", n_leads, FW_MAX_ECG_LEADS);
+        return FW_ERR_ARG;
+    }
+    EcgK<T> k;
+    k.u = u;
+    k.w = w;
+    k.myo = myo;
+    k.n = g.n;
+    k.si = g.si;
+    k.sj = g.sj;
+    k.nj = g.nj;
+    k.nk = g.nk;
+    k.dim = dim;
+    k.n_leads = n_leads;
+    for (int c = 0; c < FW_MAX_ECG_LEADS; ++c)
+        for (int a = 0; a < 3; ++a)
+            k.xyz[c][a] = c < n_leads ? (T)coords[c][a] : (T)0;
+    k.dr = (T)dr;
+    k.out = out;
+    k_ecg<ST, T><<<grid_for(g.n, kThreads, 152 * 8), kThreads, 0, stream>>>(k);
+    FW_CHECK_LAUNCH("k_ecg");
+    return FW_OK;
+}
+
 template <int ST, class T>
 __global__ void k_diffuse(T *un, const T *u, const T *w, const int64_t *idx,
                           int64_t n_idx, int64_t n, int64_t si, int64_t sj)
@@ -345,6 +437,20 @@ int run_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
             pk.u = cur;
             k_probe<T><<<1, 128, 0, stream>>>(pk);
             FW_CHECK_LAUNCH("k_probe");
+        }
+        for (int i = 0; i < a->n_ecg; ++i) {
+            const fw_ecg_tracker &E = a->ecg[i];
+            if (!in_window(E.win, n)) continue;
+            const int64_t smp = E.sample_offset + (n - E.win.first) / E.win.stride;
+            if (smp < 0 || smp >= E.capacity) {
+                set_error("fw_step: ECG sample %lld outside its capacity %lld",
+                          (long long)smp, (long long)E.capacity);
+                return FW_ERR_ARG;
+            }
+            int rc = launch_ecg<ST, T>(cur, k.w, a->myo, g, dim, E.coords,
+                                       E.n_leads, E.dr,
+                                       E.out + smp * E.n_leads, stream);
+            if (rc) return rc;
         }
     }
     return FW_OK;

@@ -47,6 +47,51 @@ int ionic(int32_t model, int32_t precision, void *u_new, const void *u,
     return dispatch_model(model, precision, d);
 }
 
+int ecg(int32_t stencil, int32_t precision, const void *u, const void *w,
+        const int8_t *myo, int64_t ni, int64_t nj, int64_t nk,
+        const double *coords, int32_t n_leads, double dr, double *out,
+        cudaStream_t stream)
+{
+    if (!stencil_nw(stencil) || !u || !w || !myo || !coords || !out) {
+        set_error("fw_ecg: bad stencil or null pointer");
+        return FW_ERR_ARG;
+    }
+    if (precision != FW_F64 && precision != FW_F32) {
+        set_error("fw_ecg: unknown precision %d", precision);
+        return FW_ERR_ARG;
+    }
+    {
+        // the lead coordinates are read on the host: refuse device memory
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, coords) == cudaSuccess &&
+            at.type == cudaMemoryTypeDevice) {
+            set_error("fw_ecg: coords must be host memory");
+            return FW_ERR_ARG;
+        }
+        cudaGetLastError();
+    }
+    const int dim = stencil_dim(stencil);
+    Grid g = make_grid(ni, nj, nk, dim);
+    const double(*xyz)[3] = reinterpret_cast<const double(*)[3]>(coords);
+#define ECG_CASE(ST)                                                          \
+    case ST:                                                                  \
+        return precision == FW_F64                                            \
+                   ? launch_ecg<ST, double>((const double *)u,                \
+                                            (const double *)w, myo, g, dim,   \
+                                            xyz, n_leads, dr, out, stream)    \
+                   : launch_ecg<ST, float>((const float *)u, (const float *)w, \
+                                           myo, g, dim, xyz, n_leads, dr, out, \
+                                           stream);
+    switch (stencil) {
+        ECG_CASE(FW_STENCIL_ISO5)
+        ECG_CASE(FW_STENCIL_ANISO9)
+        ECG_CASE(FW_STENCIL_ISO7)
+        ECG_CASE(FW_STENCIL_ANISO19)
+    }
+#undef ECG_CASE
+    return FW_ERR_ARG;
+}
+
 int diffuse(int32_t stencil, int32_t precision, void *u_new, const void *u,
             const void *w, const int64_t *idx, int64_t n_idx, int64_t ni,
             int64_t nj, int64_t nk, cudaStream_t stream)

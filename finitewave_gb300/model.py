@@ -24,7 +24,8 @@ from . import _ffi
 from .stencil import (AsymmetricStencil2D, AsymmetricStencil3D,
                       IsotropicStencil2D, IsotropicStencil3D)
 from .stimulation import Stim
-from .tracker import (ActivationTime2DTracker, LocalActivationTime2DTracker,
+from .tracker import (ActivationTime2DTracker, ECG2DTracker,
+                      LocalActivationTime2DTracker,
                       _ProbeTracker)
 
 _NP = {"float64": np.float64, "float32": np.float32}
@@ -348,6 +349,8 @@ class CardiacModel:
                 self.stencil.kind not in (_ffi.ISO5, _ffi.ANISO9)):
             return False
         trs = self.tracker_sequence.sequence if self.tracker_sequence else []
+        if any(isinstance(t, ECG2DTracker) for t in trs):
+            return False
         if (sum(isinstance(t, ActivationTime2DTracker) for t in trs) > 2 or
                 sum(isinstance(t, LocalActivationTime2DTracker)
                     for t in trs) > 1):
@@ -450,7 +453,7 @@ class CardiacModel:
         a.n_stims = n_st
 
         # trackers (tracker.py:70-83)
-        n_at = n_lat = n_pr = 0
+        n_at = n_lat = n_pr = n_ecg = 0
         if self.tracker_sequence:
             for tr in self.tracker_sequence.sequence:
                 win = tr._window(ts, n0)
@@ -474,6 +477,22 @@ class CardiacModel:
                     d.cross_steps = tr._steps.data_ptr()
                     d.cross_count = tr._count.data_ptr()
                     d.capacity = int(tr.capacity)
+                elif isinstance(tr, ECG2DTracker):
+                    if n_ecg >= _ffi.MAX_ECG:
+                        raise RuntimeError("too many ECG trackers")
+                    buf = tr._reserve(count)
+                    d = a.ecg[n_ecg]
+                    n_ecg += 1
+                    d.win.first, d.win.last, d.win.stride = first, last, \
+                        int(tr.step)
+                    d.n_leads = len(tr.measure_coords)
+                    for c, xyz in enumerate(tr.measure_coords):
+                        for q in range(3):
+                            d.coords[c][q] = float(xyz[q])
+                    d.dr = float(self.dr)
+                    d.out = buf.data_ptr()
+                    d.sample_offset = 0
+                    d.capacity = count
                 elif isinstance(tr, _ProbeTracker):
                     buf = tr._reserve(count)
                     d = a.probe[n_pr]
@@ -492,6 +511,7 @@ class CardiacModel:
                     raise TypeError(f"{type(tr).__name__} is not a "
                                     "finitewave_gb300 tracker")
         a.n_at, a.n_lat, a.n_probe = n_at, n_lat, n_pr
+        a.n_ecg = n_ecg
         a.status = self._status.data_ptr()
         return _Segment(a, n0, n_seg, t_end, keep)
 

@@ -317,3 +317,50 @@ class Variable3DTracker(Variable2DTracker):
     def __init__(self):
         super().__init__()
         self.cell_ind = [1, 1, 1]
+
+
+class ECG2DTracker(Tracker):
+    """Pseudo-ECG at measurement points (cpuwave2D/tracker/ecg_2d_tracker.py:
+    6-153): on each tracked step, for every point (x, y, z) the sum over
+    myocytes (i, j) of (diffuse(u) - u) / (d * dr) with
+    d = (x - i)^2 + (y - j)^2 + z^2.  Computed on the device by a reduction
+    kernel (fw_ecg_tracker); the model runs in the plain form while one is
+    attached.  ``output`` is the (samples, points) array."""
+
+    def __init__(self, measure_coords=None):
+        super().__init__()
+        self.measure_coords = measure_coords
+        self.file_name = "ecg.npy"
+        self._chunks = []
+
+    def initialize(self, model):
+        self.model = model
+        self.measure_coords = np.atleast_2d(
+            np.asarray(self.measure_coords, dtype=np.float64))
+        if self.measure_coords.shape[1] != 3:
+            raise ValueError("measure_coords must hold (x, y, z) per point")
+        if not 1 <= len(self.measure_coords) <= _ffi.MAX_ECG_LEADS:
+            raise ValueError(f"1..{_ffi.MAX_ECG_LEADS} measurement points")
+        self._chunks = []
+
+    def _reserve(self, count):
+        buf = torch.zeros((count, len(self.measure_coords)),
+                          dtype=torch.float64, device=self.model._device())
+        self._chunks.append(buf)
+        return buf
+
+    @property
+    def output(self):
+        if not self._chunks:
+            return np.zeros((0, len(np.atleast_2d(self.measure_coords))))
+        return torch.cat([c.cpu() if c.is_cuda else c
+                          for c in self._chunks]).numpy()
+
+    def write(self):
+        Path(self.path).mkdir(parents=True, exist_ok=True)
+        np.save(Path(self.path).joinpath(self.file_name).with_suffix(".npy"),
+                self.output)
+
+
+class ECG3DTracker(ECG2DTracker):
+    """(cpuwave3D/tracker/ecg_3d_tracker.py: d includes (z - k)^2)"""

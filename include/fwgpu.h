@@ -87,6 +87,8 @@ enum fw_stim_kind { FW_STIM_VOLTAGE = 0, FW_STIM_CURRENT = 1 };
 #define FW_MAX_LAT 2
 #define FW_MAX_PROBE 4
 #define FW_MAX_PROBE_VARS 8
+#define FW_MAX_ECG 2
+#define FW_MAX_ECG_LEADS 8
 
 /* A set of global step indices n with first <= n <= last and
  * n % stride == 0.  Trackers are active on exactly those steps; the host
@@ -158,6 +160,27 @@ typedef struct fw_probe_tracker {
     int64_t capacity; /* samples */
 } fw_probe_tracker;
 
+/* ECG2DTracker / ECG3DTracker (cpuwave2D/tracker/ecg_2d_tracker.py:61-79,
+ * 114-153; cpuwave3D/tracker/ecg_3d_tracker.py:51-69, 99-140): on active
+ * steps n, for every lead c
+ *   out[s * n_leads + c] += sum over myocytes p = (i, j[, k]) with d > 0 of
+ *                           (diffuse(u)[p] - u[p]) / (d * dr),
+ *   d = (x_c - i)^2 + (y_c - j)^2 + (z_c - k)^2   (k = 0 in 2D),
+ * u as the trackers see it (after stimuli, before the step) and diffuse(u)
+ * the stencil sum with the model's weights; s = sample_offset +
+ * (n - win.first) / win.stride.  `out` (capacity x n_leads float64) must
+ * be zero where samples are added.  Plain form only. */
+typedef struct fw_ecg_tracker {
+    fw_window win;
+    int32_t n_leads;
+    int32_t reserved;
+    double coords[FW_MAX_ECG_LEADS][3];
+    double dr;
+    double *out;
+    int64_t sample_offset;
+    int64_t capacity; /* samples */
+} fw_ecg_tracker;
+
 /* Everything one model instance needs to advance.  Replaces the body of
  * CardiacModel.run (core/model/cardiac_model.py:164-189) together with the
  * model's run_diffusion_kernel / run_ionic_kernel. */
@@ -195,6 +218,9 @@ typedef struct fw_step_args {
                                    node-major, (N, 4) for ISO5 or (N, 8)
                                    for ANISO9, from fw_pack_weights; NULL
                                    when not available                       */
+    int32_t n_ecg;
+    int32_t reserved;
+    fw_ecg_tracker ecg[FW_MAX_ECG];
 } fw_step_args;
 
 /* A planned batch of tissues (fw_batch_plan).  Host-side handle; the
@@ -212,8 +238,8 @@ FW_API int fw_version(void);
 
 /* sizeof of the ABI structs as compiled into the library, so a binding can
  * check its own layout: which = 0 fw_step_args, 1 fw_stim, 2 fw_at_tracker,
- * 3 fw_lat_tracker, 4 fw_probe_tracker, 5 fw_window, 6 fw_batch.  0 for
- * unknown. */
+ * 3 fw_lat_tracker, 4 fw_probe_tracker, 5 fw_window, 6 fw_batch,
+ * 7 fw_ecg_tracker.  0 for unknown. */
 FW_API size_t fw_struct_size(int32_t which);
 
 /* Number of kernels this library has launched in the process so far
@@ -272,6 +298,17 @@ FW_API int fw_ionic(int32_t model, int32_t precision, void *u_new, const void *u
  * implied because each stencil row sums to one).  2D stencils only. */
 FW_API int fw_pack_weights(int32_t stencil, const float *w, int64_t n,
                            float *out, void *stream);
+
+/* One ECG sample: the sum of fw_ecg_tracker for the potential u (N nodes)
+ * with weights w (nw, N) over the nodes with myo[p] != 0, for n_leads
+ * leads at coords (n_leads x 3 float64 in HOST memory, passed to the kernel
+ * by value), added to out[0..n_leads-1] (float64, device).  Replaces compute_ecg after model.diffusion_kernel
+ * (ecg_2d_tracker.py:61-79 with :114-153; ecg_3d_tracker.py:51-69 with
+ * :99-140). */
+FW_API int fw_ecg(int32_t stencil, int32_t precision, const void *u,
+                  const void *w, const int8_t *myo, int64_t ni, int64_t nj,
+                  int64_t nk, const double *coords, int32_t n_leads,
+                  double dr, double *out, void *stream);
 
 /* Advance n_steps time steps starting at global step n_begin (the model's
  * step counter).  On return the current u is a->u[n_steps & 1]. */

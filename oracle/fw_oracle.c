@@ -512,3 +512,37 @@ EXPORT void fwo_ionic_fk(double *un, const double *u, double *v, double *w,
         un[p] += dt * (-J_fi - J_so - J_si);
     }
 }
+
+/* compute_ecg (cpuwave2D/tracker/ecg_2d_tracker.py:114-153 with dim 2,
+ * cpuwave3D/tracker/ecg_3d_tracker.py:99-140 with dim 3): for every lead c,
+ * the sum over myocytes in index order of (u_tr - u) / (d * dr) where d > 0.
+ * Sequential: the reference's pure-Python order. */
+EXPORT void fwo_ecg(const double *u_tr, const double *u, const double *coords,
+                    int64_t n_c, double dr, const int64_t *idx, int64_t n_idx,
+                    int64_t nj, int64_t nk, int dim, double *out)
+{
+    for (int64_t c = 0; c < n_c; ++c) {
+        const double x = coords[3 * c], y = coords[3 * c + 1],
+                     z = coords[3 * c + 2];
+        double acc = 0.0;
+        for (int64_t t = 0; t < n_idx; ++t) {
+            const int64_t ii = idx[t];
+            double i, j, k;
+            if (dim == 2) {
+                i = (double)(ii / nj);
+                j = (double)(ii % nj);
+                k = 0.0;
+            } else {
+                i = (double)(ii / (nj * nk));
+                j = (double)((ii % (nj * nk)) / nk);
+                k = (double)((ii % (nj * nk)) % nk);
+            }
+            const double d = dim == 2
+                                 ? (x - i) * (x - i) + (y - j) * (y - j) + z * z
+                                 : (x - i) * (x - i) + (y - j) * (y - j) +
+                                       (z - k) * (z - k);
+            if (d > 0) acc += (u_tr[ii] - u[ii]) / (d * dr);
+        }
+        out[c] = acc;
+    }
+}

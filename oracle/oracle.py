@@ -78,6 +78,8 @@ def lib():
             "fwo_ionic_ap": [_P, _P, _P, _P, _I] + [_D] * 6,
             "fwo_ionic_ms": [_P, _P, _P, _P, _I] + [_D] * 6,
             "fwo_ionic_fk": [_P, _P, _P, _P, _P, _I] + [_D] * 12,
+            "fwo_ecg": [_P, _P, _P, _I, _D, _P, _I, _I, _I, ctypes.c_int,
+                        _P],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -175,6 +177,14 @@ def _ionic(model, st, un, u, idx, dt, p):
         MODELS[model]["ionic"](L, un, u, st, idx, dt, p)
 
 
+def _ecg(u_tr, u, coords, dr, idx, shape):
+    out = np.zeros(len(coords))
+    nk = shape[2] if len(shape) == 3 else 1
+    lib().fwo_ecg(_p(u_tr), _p(u), _p(coords), len(coords), dr, _p(idx),
+                  idx.size, shape[1], nk, len(shape), _p(out))
+    return out
+
+
 def _diffuse(kind, un, u, w, idx):
     L = lib()
     if kind in ("iso5", "aniso9"):
@@ -216,7 +226,7 @@ def run(case):
     conductivity, D_al, D_ac, D_model (optional), params (overrides),
     stims (list of dicts: kind 'voltage'|'current', t, value, duration,
     u_max, and one of box / matrix / coords), trackers (list of dicts:
-    kind 'at'|'lat'|'probe', threshold, start_time, end_time, step,
+    kind 'at'|'lat'|'probe'|'ecg', threshold, start_time, end_time, step,
     cells, vars), special (optional special_boundaries array),
     init (optional overrides of initial values).
     Returns dict with state arrays, u_new, t, step and tracker outputs.
@@ -255,6 +265,11 @@ def run(case):
             tr["activated"] = np.zeros(mesh.shape, dtype=bool)
         elif tr["kind"] == "probe":
             tr["samples"] = {v: [] for v in tr["vars"]}
+        elif tr["kind"] == "ecg":
+            tr["coords"] = np.ascontiguousarray(
+                np.atleast_2d(tr["coords"]), dtype=np.float64)
+            tr["u_tr"] = np.zeros(mesh.shape)
+            tr["samples"] = []
         trackers.append(tr)
 
     t = 0
@@ -294,6 +309,11 @@ def run(case):
                 for var in tr["vars"]:
                     arr = u if var == "u" else st[var]
                     tr["samples"][var].append(arr[ci].copy())
+            elif tr["kind"] == "ecg":
+                # ECG2DTracker.calc_ecg (ecg_2d_tracker.py:61-79)
+                _diffuse(kind, tr["u_tr"], u, w, idx)
+                tr["samples"].append(_ecg(tr["u_tr"], u, tr["coords"], dr,
+                                          idx, mesh.shape))
         t += dt
         step += 1
         u_new, u = u, u_new
@@ -309,6 +329,8 @@ def run(case):
             outs.append(tr["act_t"])
         elif tr["kind"] == "lat":
             outs.append(np.array(tr["act_t"]))
+        elif tr["kind"] == "ecg":
+            outs.append(np.array(tr["samples"]))
         else:
             outs.append({v: np.squeeze(tr["samples"][v])
                          for v in tr["vars"]})

@@ -166,3 +166,28 @@ def courtemanche(dim):
     gold = {v: g[f"d{dim}_{v}"] for v in MODEL_VARS["crn"]}
     gold.update({f"mv_{v}": g[f"d{dim}_mv_{v}"] for v in probe["vars"]})
     return case, gold
+
+
+def ecg(dim):
+    """ECG trackers: the planar 50 x 5 Aliev-Panfilov cable with two leads
+    (2D) or the 14 x 10 x 8 anisotropic slab with three leads (3D)."""
+    g = load("ecg")
+    if dim == 2:
+        mesh = np.ones((50, 5), dtype=np.int8)
+        mesh[0, :] = mesh[-1, :] = mesh[:, 0] = mesh[:, -1] = 0
+        case = dict(model="ap", mesh=mesh, dt=0.0015, dr=0.25, t_max=15,
+                    stencil="iso5",
+                    stims=[dict(kind="current", t=5, value=5, duration=0.5,
+                                box=[(0, 5), (0, 5)])],
+                    trackers=[dict(kind="ecg", step=10,
+                                   coords=[[25, 2, 0], [10, -3, 1.5]])])
+    else:
+        case = dict(model="ap", mesh=g["mesh3"], fibers=g["fib3"],
+                    stencil="aniso19", dt=0.01, dr=0.25, t_max=10,
+                    D_al=1.0, D_ac=1.0 / 9,
+                    stims=[dict(kind="voltage", t=0, value=1.0,
+                                box=[(0, 14), (0, 3), (0, 8)])],
+                    trackers=[dict(kind="ecg", step=5,
+                                   coords=[[7, 12, 4], [-2, 5, 3],
+                                           [7, 5, 10.5]])])
+    return case, {"ecg": g[f"d{dim}_ecg"], "u": g[f"d{dim}_u"]}

@@ -477,6 +477,51 @@ def case_fibrosis(fw):
     return out
 
 
+def case_ecg(fw):
+    """ECG trackers: the reference's planar 50 x 5 Aliev-Panfilov model
+    (tests/test_trackers_2d.py:43-58, 261-278) with two leads every 10
+    steps, and a 3D anisotropic Aliev-Panfilov slab with three leads."""
+    out = {}
+    tissue = fw.CardiacTissue2D([50, 5])
+    ss = fw.StimSequence()
+    ss.add_stim(fw.StimCurrentCoord2D(5, 5, 0.5, 0, 5, 0, 5))
+    model = fw.AlievPanfilov2D()
+    model.dt, model.dr, model.t_max = 0.0015, 0.25, 15
+    model.prog_bar = False
+    model.cardiac_tissue = tissue
+    model.stim_sequence = ss
+    tr = fw.ECG2DTracker()
+    tr.start_time = 0
+    tr.step = 10
+    tr.measure_coords = np.array([[25, 2, 0], [10, -3, 1.5]])
+    _attach(fw, model, [tr])
+    model.run()
+    out["d2_ecg"] = tr.output
+    out["d2_u"] = model.u
+    rng = np.random.default_rng(909)
+    mesh3 = _fibrosis(rng, (14, 10, 8), 0.1)
+    fib3 = _seeded_fibers_3d(rng, (14, 10, 8))
+    tissue = fw.CardiacTissue3D((14, 10, 8))
+    tissue.mesh = mesh3.copy()
+    tissue.fibers = fib3
+    ss = fw.StimSequence()
+    ss.add_stim(fw.StimVoltageCoord3D(0, 1, 0, 14, 0, 3, 0, 8))
+    model = fw.AlievPanfilov3D()
+    model.dt, model.dr, model.t_max = 0.01, 0.25, 10
+    model.prog_bar = False
+    model.cardiac_tissue = tissue
+    model.stim_sequence = ss
+    tr = fw.ECG3DTracker()
+    tr.step = 5
+    tr.measure_coords = np.array([[7, 12, 4], [-2, 5, 3], [7, 5, 10.5]])
+    _attach(fw, model, [tr])
+    model.run()
+    out["d3_ecg"] = tr.output
+    out["d3_u"] = model.u
+    out["mesh3"], out["fib3"] = mesh3, fib3
+    return out
+
+
 CASES = {
     "weights_2d": case_weights_2d,
     "weights_3d": case_weights_3d,
@@ -489,6 +534,7 @@ CASES = {
     "tp06": case_tp06,
     "courtemanche": case_courtemanche,
     "fibrosis": case_fibrosis,
+    "ecg": case_ecg,
 }
 
 

@@ -80,6 +80,9 @@ def build(case, npfloat="float64", form=None, fused_k=0, fused_variant=0):
         elif tr["kind"] == "lat":
             o = fg.LocalActivationTime2DTracker()
             o.threshold = tr["threshold"]
+        elif tr["kind"] == "ecg":
+            o = fg.ECG2DTracker() if dim == 2 else fg.ECG3DTracker()
+            o.measure_coords = np.asarray(tr["coords"], dtype=np.float64)
         else:
             o = fg.MultiVariable2DTracker() if dim == 2 \
                 else fg.MultiVariable3DTracker()

@@ -145,3 +145,12 @@ def test_detailed_models(oracle, name, dim):
     if name == "tp06":
         # the reference never updates Ca_i
         assert np.all(r["cai"] == 0.00007)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_ecg_bitwise(oracle, dim):
+    """compute_ecg after the diffusion kernel, every tracked step."""
+    case, g = cases.ecg(dim)
+    r = oracle.run(case)
+    assert np.array_equal(r["u"], g["u"])
+    assert np.array_equal(r["trackers"][0], g["ecg"])
