@@ -39,6 +39,40 @@ def _np_name(npfloat):
     return name
 
 
+class _DeviceArray(np.ndarray):
+    """Host copy of a device state array whose item assignments write
+    through: ``model.u[1:-1, 1:-1] = 1`` (as the reference's commands do on
+    its numpy state) updates the device array.  Views write through as
+    well; copies (``.copy()``, arithmetic results) are plain arrays."""
+
+    def __array_finalize__(self, obj):
+        if self.base is None or obj is None:
+            self._owner = self._name = self._root = None
+            return
+        self._owner = getattr(obj, "_owner", None)
+        self._name = getattr(obj, "_name", None)
+        self._root = getattr(obj, "_root", None)
+
+    def __setitem__(self, key, value):
+        super().__setitem__(key, value)
+        owner = getattr(self, "_owner", None)
+        if owner is not None and self._root is not None:
+            setattr(owner, self._name, np.asarray(self._root))
+
+    def __array_wrap__(self, arr, context=None, return_scalar=False):
+        # ufunc results are new arrays: plain numpy
+        out = np.asarray(arr)
+        if return_scalar and out.ndim == 0:
+            return out[()]
+        return out
+
+
+def _device_array(owner, name, host):
+    a = host.view(_DeviceArray)
+    a._owner, a._name, a._root = owner, name, a
+    return a
+
+
 class _StateVar:
     """Descriptor: a state variable held on the device, seen as numpy."""
 
@@ -50,7 +84,7 @@ class _StateVar:
             return self
         dev = obj.__dict__.get("_dev")
         if dev and self.name in dev:
-            return dev[self.name].cpu().numpy()
+            return _device_array(obj, self.name, dev[self.name].cpu().numpy())
         return obj.__dict__.get("_host", {}).get(self.name, np.ndarray)
 
     def __set__(self, obj, value):
