@@ -760,10 +760,9 @@ def run_gb300(args):
 
     # dominant-kernel timing: launches of one segment averaged
     kms, kl = device_steps(model, chunk, 3, torch)
-    form_used = model._form()
-    kernel_name = ("k_fused_tma" if form_used == 1 and model._wpack is not None
-                   and args.fused_variant in (0, 3) else
-                   "k_fused" if form_used == 1 else "k_step")
+    choice = getattr(model, "_fused_choice", None)
+    kernel_name = ("k_step" if choice is None else
+                   "k_fused_tma" if choice[0] == 3 else "k_fused")
     steps_per_launch = (3 * chunk) / max(1, kl)
     per_launch_s = (kms / 1e3) / max(1, kl)
     alg_bytes = B_ALG["float32"] * myo * steps_per_launch
@@ -868,9 +867,11 @@ def run_gb300(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind,
-                         "traffic": traffic_from_profiles(myo,
-                                                          steps_per_launch),
+                         "traffic": (traffic_from_profiles(
+                             myo, steps_per_launch)
+                             if choice == (3, 4) else None),
                          "kernel": kernel_name,
+                         "fused_variant_k": list(choice) if choice else None,
                          "alg_bytes_per_myocyte_step": B_ALG["float32"],
                          "time_steps_per_launch": steps_per_launch},
             "batched": batched,

@@ -108,8 +108,11 @@ class CardiacModel:
     (parameters in the library's order) and ``select_stencil``.
 
     Extra attributes over the reference: ``device`` (CUDA device, default
-    the current one) and ``form`` ('plain', 'fused' or None for automatic:
-    fused for float32 where the library has it, plain otherwise).
+    the current one), ``form`` ('plain', 'fused' or None for automatic:
+    fused for float32 where the library has it, plain otherwise),
+    ``fused_k`` / ``fused_variant`` (the fused kernel's time steps per
+    launch and kernel; 0 = chosen by ``autotune``) and ``autotune`` (time
+    the fused candidates once per configuration, finitewave_gb300.autotune).
     """
 
     _model_id = None
@@ -152,6 +155,7 @@ class CardiacModel:
         self.form = None
         self.fused_k = 0
         self.fused_variant = 0
+        self.autotune = True
         self._dev = {}
         self._t_hist = []
 
@@ -427,12 +431,9 @@ class CardiacModel:
         self._finish_segment(seg)
         return seg.n_seg
 
-    def _prepare_segment(self, limit):
-        """The fw_step_args of the next segment of at most `limit` steps
-        (stimulus and tracker windows in global step indices)."""
-        ts, t_end, n_seg = self._segment_times(limit)
-        n0 = int(self.step)
-        self._t_hist.append(ts)
+    def _bare_args(self):
+        """fw_step_args with the model's arrays, parameters and kernel
+        choice, and no stimuli or trackers."""
         a = _ffi.StepArgs()
         a.model = self._model_id
         a.stencil = self.stencil.kind
@@ -452,9 +453,24 @@ class CardiacModel:
         for i, p in enumerate(self._params()):
             a.params[i] = p
         a.dt = float(self.dt)
+        a.form = self._form()
         a.fused_k = int(self.fused_k)
         a.fused_variant = int(self.fused_variant)
-        a.form = self._form()
+        if (a.form == _ffi.FORM_FUSED and not a.fused_k and
+                not a.fused_variant and self.autotune):
+            from . import autotune
+            a.fused_variant, a.fused_k = autotune.choose(self)
+        self._fused_choice = (a.fused_variant, a.fused_k) \
+            if a.form == _ffi.FORM_FUSED else None
+        return a
+
+    def _prepare_segment(self, limit):
+        """The fw_step_args of the next segment of at most `limit` steps
+        (stimulus and tracker windows in global step indices)."""
+        a = self._bare_args()
+        ts, t_end, n_seg = self._segment_times(limit)
+        n0 = int(self.step)
+        self._t_hist.append(ts)
         keep = []
 
         # stimuli (stim_sequence.py:65-77)
