@@ -33,7 +33,9 @@ from .tracker import (ActionPotential2DTracker, ActionPotential3DTracker,
                       ECG2DTracker, ECG3DTracker,
                       LocalActivationTime2DTracker,
                       LocalActivationTime3DTracker, MultiVariable2DTracker,
-                      MultiVariable3DTracker, Tracker, TrackerSequence,
+                      MultiVariable3DTracker, Period2DTracker,
+                      Period3DTracker, SpiralWaveCore2DTracker,
+                      SpiralWaveCore3DTracker, Tracker, TrackerSequence,
                       Variable2DTracker, Variable3DTracker)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

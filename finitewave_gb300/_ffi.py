@@ -20,6 +20,8 @@ FW_ERR_UNSUPPORTED = -3
 FW_DEV_LAT_OVERFLOW = 1
 FW_DEV_PROBE_OVERFLOW = 2
 FW_DEV_BATCH_FAULT = 4
+FW_DEV_TIMEOUT = 8
+FW_DEV_TIP_OVERFLOW = 16
 
 MODEL_AP, MODEL_MS, MODEL_FK, MODEL_TP06, MODEL_CRN = 1, 2, 3, 4, 5
 ISO5, ANISO9, ISO7, ANISO19 = 1, 2, 3, 4
@@ -35,6 +37,7 @@ MAX_LAT = 2
 MAX_PROBE = 4
 MAX_PROBE_VARS = 8
 MAX_ECG = 2
+MAX_TIP = 1
 MAX_ECG_LEADS = 8
 
 STENCIL_NW = {ISO5: 5, ANISO9: 9, ISO7: 7, ANISO19: 19}
@@ -75,6 +78,17 @@ class EcgTracker(ctypes.Structure):
                 ("out", _vp), ("sample_offset", _i64), ("capacity", _i64)]
 
 
+class Tip(ctypes.Structure):
+    _fields_ = [("sample", _i32), ("k", _i32), ("i", _i32), ("j", _i32),
+                ("x", _f64), ("y", _f64)]
+
+
+class TipTracker(ctypes.Structure):
+    _fields_ = [("win", Window), ("threshold", _f64), ("u_prev", _vp),
+                ("out", _vp), ("count", _vp), ("capacity", _i64),
+                ("sample_offset", _i64)]
+
+
 class StepArgs(ctypes.Structure):
     _fields_ = [("model", _i32), ("stencil", _i32), ("precision", _i32),
                 ("form", _i32), ("ni", _i64), ("nj", _i64), ("nk", _i64),
@@ -88,8 +102,9 @@ class StepArgs(ctypes.Structure):
                 ("probe", ProbeTracker * MAX_PROBE),
                 ("status", _vp), ("fused_k", _i32),
                 ("fused_variant", _i32), ("weights_packed", _vp),
-                ("n_ecg", _i32), ("reserved", _i32),
-                ("ecg", EcgTracker * MAX_ECG)]
+                ("n_ecg", _i32), ("n_tip", _i32),
+                ("ecg", EcgTracker * MAX_ECG),
+                ("tip", TipTracker * MAX_TIP)]
 
 
 class Batch(ctypes.Structure):
@@ -136,7 +151,8 @@ _SIGS = {
 
 # symbol -> ctypes structure whose size must match the library's
 _STRUCTS = {0: StepArgs, 1: Stim, 2: AtTracker, 3: LatTracker,
-            4: ProbeTracker, 5: Window, 6: Batch, 7: EcgTracker}
+            4: ProbeTracker, 5: Window, 6: Batch, 7: EcgTracker,
+            8: TipTracker, 9: Tip}
 
 
 def load(path=None):

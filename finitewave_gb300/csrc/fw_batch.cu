@@ -436,7 +436,8 @@ int check_tissue(const fw_step_args *a, int i)
                   (long long)a->ni, (long long)a->nj, (long long)a->nk);
         return FW_ERR_ARG;
     }
-    if (a->n_at > 1 || a->n_lat > 1 || a->n_probe != 0 || a->n_ecg != 0) {
+    if (a->n_at > 1 || a->n_lat > 1 || a->n_probe != 0 || a->n_ecg != 0 ||
+        a->n_tip != 0) {
         set_error("fw_batch: tissue %d: at most one activation and one local "
                   "activation tracker, no probes or ECG", i);
         return FW_ERR_UNSUPPORTED;

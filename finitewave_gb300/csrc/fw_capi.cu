@@ -153,8 +153,22 @@ int check_step_args(const fw_step_args *a, int64_t n_steps)
             return FW_ERR_ARG;
         }
     }
-    if (a->n_ecg > 0 && a->form == FW_FORM_FUSED) {
-        set_error("fw_step: ECG trackers run in the plain form only");
+    if (a->n_tip < 0 || a->n_tip > FW_MAX_TIP) {
+        set_error("fw_step: n_tip %d out of range (0..%d)", a->n_tip,
+                  FW_MAX_TIP);
+        return FW_ERR_ARG;
+    }
+    for (int i = 0; i < a->n_tip; ++i) {
+        const fw_tip_tracker &P = a->tip[i];
+        if (!valid_window(P.win) || !P.u_prev || !P.out || !P.count ||
+            P.capacity < 0 || P.capacity > INT32_MAX || P.sample_offset < 0) {
+            set_error("fw_step: spiral tip tracker %d invalid", i);
+            return FW_ERR_ARG;
+        }
+    }
+    if ((a->n_ecg > 0 || a->n_tip > 0) && a->form == FW_FORM_FUSED) {
+        set_error("fw_step: ECG and spiral tip trackers run in the plain "
+                  "form only");
         return FW_ERR_UNSUPPORTED;
     }
     return FW_OK;
@@ -178,6 +192,8 @@ size_t fw_struct_size(int32_t which)
     case 5: return sizeof(fw_window);
     case 6: return sizeof(fw_batch);
     case 7: return sizeof(fw_ecg_tracker);
+    case 8: return sizeof(fw_tip_tracker);
+    case 9: return sizeof(fw_tip);
     }
     return 0;
 }

@@ -292,6 +292,104 @@ int launch_ecg(const T *u, const T *w, const int8_t *myo, const Grid &g,
     return FW_OK;
 }
 
+// Spiral-wave tips (spiral_wave_core_2d_tracker.py:88-249): the cell
+// (i, j)-(i+1, j+1) holds a tip when the threshold isoline crosses it in
+// both the previous and the current potential; the tip is the intersection
+// of the two bilinear isolines inside the cell (_correct_tip_pos), found in
+// float64.
+template <class T>
+struct TipK {
+    const T *u_prev;
+    const T *u;
+    int64_t ni, nj, nk;   // slice (i, j) planes; k the z index (nk = 1 in 2D)
+    double thr;
+    fw_tip *out;
+    int32_t *count;
+    int64_t capacity;
+    int32_t sample;
+    int32_t *status;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_tips(TipK<T> k)
+{
+    const int64_t di = k.ni - 10, dj = k.nj - 10;
+    if (di <= 0 || dj <= 0) return;
+    const int64_t cells = di * dj * k.nk;
+    const T thr = (T)k.thr;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+         t < cells; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kk = t % k.nk;
+        const int64_t r = t / k.nk;
+        const int64_t j = 5 + r % dj, i = 5 + r / dj;
+        // element (i, j) of z layer kk; rows of a layer are nj * nk apart
+        const int64_t si = k.nj * k.nk, sj = k.nk;
+        const int64_t p = i * si + j * sj + kk;
+        // neighbours: (i+1, j) = p + si, (i, j+1) = p + sj
+        const T *up = k.u_prev, *uc = k.u;
+        auto crosses = [&](const T *u) {
+            const T a = u[p], b = u[p + si], c = u[p + sj], d = u[p + si + sj];
+            if (a >= thr && (b < thr || c < thr || d < thr)) return 1;
+            if (a < thr && (b >= thr || c >= thr || d >= thr)) return 1;
+            return 0;
+        };
+        int counter = crosses(up);
+        if (counter == 1) counter += crosses(uc);
+        if (counter != 2) continue;
+        // _correct_tip_pos (spiral_wave_core_2d_tracker.py:98-146)
+        const double u00 = up[p], u01 = up[p + sj], u10 = up[p + si],
+                     u11 = up[p + si + sj];
+        const double n00 = uc[p], n01 = uc[p + sj], n10 = uc[p + si],
+                     n11 = uc[p + si + sj];
+        const double th = k.thr;
+        const double AC = u00 - u01 + u11 - u10;
+        const double GC = u01 - u00;
+        const double BC = u10 - u00;
+        const double DC = u00 - th;
+        const double AD = n00 - n01 + n11 - n10;
+        const double GD = n01 - n00;
+        const double BD = n10 - n00;
+        const double DD = n00 - th;
+        const double Q = BC * AD - BD * AC;
+        const double R = GC * AD - GD * AC;
+        const double S = DC * AD - DD * AC;
+        const double QOnR = Q / R;
+        const double SOnR = S / R;
+        const double Tq = AC * QOnR;
+        const double U = AC * SOnR - BC + GC * QOnR;
+        const double V = GC * SOnR - DC;
+        const double disc = U * U - 4. * Tq * V;
+        if (disc < 0) continue;
+        const double T2 = 2. * Tq;
+        if (T2 == 0.) continue;
+        const double sq = sqrt(disc);
+        const double xn = (-U - sq) / T2, xp = (-U + sq) / T2;
+        const double yn = -QOnR * xn - SOnR, yp = -QOnR * xp - SOnR;
+        double cx, cy;
+        if (0 <= xn && xn <= 1 && 0 <= yn && yn <= 1) {
+            cx = xn;
+            cy = yn;
+        } else if (0 <= xp && xp <= 1 && 0 <= yp && yp <= 1) {
+            cx = xp;
+            cy = yp;
+        } else {
+            continue;
+        }
+        const int32_t slot = atomicAdd(k.count, 1);
+        if (slot < k.capacity) {
+            fw_tip &o = k.out[slot];
+            o.sample = k.sample;
+            o.k = (int32_t)kk;
+            o.i = (int32_t)i;
+            o.j = (int32_t)j;
+            o.x = (double)j + cy;
+            o.y = (double)i + cx;
+        } else if (k.status) {
+            atomicOr(k.status, FW_DEV_TIP_OVERFLOW);
+        }
+    }
+}
+
 template <int ST, class T>
 __global__ void k_diffuse(T *un, const T *u, const T *w, const int64_t *idx,
                           int64_t n_idx, int64_t n, int64_t si, int64_t sj)
@@ -451,6 +549,31 @@ int run_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                                        E.n_leads, E.dr,
                                        E.out + smp * E.n_leads, stream);
             if (rc) return rc;
+        }
+        for (int i = 0; i < a->n_tip; ++i) {
+            const fw_tip_tracker &P = a->tip[i];
+            if (!in_window(P.win, n)) continue;
+            TipK<T> tk;
+            tk.u_prev = (const T *)P.u_prev;
+            tk.u = cur;
+            tk.ni = g.ni;
+            tk.nj = g.nj;
+            tk.nk = g.nk;
+            tk.thr = P.threshold;
+            tk.out = P.out;
+            tk.count = P.count;
+            tk.capacity = P.capacity;
+            tk.sample = (int32_t)(P.sample_offset + (n - P.win.first) / P.win.stride);
+            tk.status = a->status;
+            const int64_t cells = (g.ni > 10 && g.nj > 10)
+                                      ? (g.ni - 10) * (g.nj - 10) * g.nk : 0;
+            if (cells > 0) {
+                k_tips<T><<<grid_for(cells, kThreads, 152 * 8), kThreads, 0,
+                            stream>>>(tk);
+                FW_CHECK_LAUNCH("k_tips");
+            }
+            FW_CUDA_CHECK(cudaMemcpyAsync(P.u_prev, cur, g.n * sizeof(T),
+                                          cudaMemcpyDeviceToDevice, stream));
         }
     }
     return FW_OK;

@@ -25,7 +25,7 @@ from .stencil import (AsymmetricStencil2D, AsymmetricStencil3D,
                       IsotropicStencil2D, IsotropicStencil3D)
 from .stimulation import Stim
 from .tracker import (ActivationTime2DTracker, ECG2DTracker,
-                      LocalActivationTime2DTracker,
+                      LocalActivationTime2DTracker, SpiralWaveCore2DTracker,
                       _ProbeTracker)
 
 _NP = {"float64": np.float64, "float32": np.float32}
@@ -387,7 +387,8 @@ class CardiacModel:
                 self.stencil.kind not in (_ffi.ISO5, _ffi.ANISO9)):
             return False
         trs = self.tracker_sequence.sequence if self.tracker_sequence else []
-        if any(isinstance(t, ECG2DTracker) for t in trs):
+        if any(isinstance(t, (ECG2DTracker, SpiralWaveCore2DTracker))
+               for t in trs):
             return False
         if (sum(isinstance(t, ActivationTime2DTracker) for t in trs) > 2 or
                 sum(isinstance(t, LocalActivationTime2DTracker)
@@ -412,6 +413,9 @@ class CardiacModel:
 
     def _check_status(self):
         st = int(self._status.item())
+        if st & _ffi.FW_DEV_TIP_OVERFLOW:
+            raise RuntimeError("SpiralWaveCore tracker: more tips than its "
+                               "capacity in one run segment")
         if st & _ffi.FW_DEV_PROBE_OVERFLOW:
             raise RuntimeError("probe tracker buffer overflow")
         if st & _ffi.FW_DEV_LAT_OVERFLOW:
@@ -503,7 +507,7 @@ class CardiacModel:
         a.n_stims = n_st
 
         # trackers (tracker.py:70-83)
-        n_at = n_lat = n_pr = n_ecg = 0
+        n_at = n_lat = n_pr = n_ecg = n_tip = 0
         if self.tracker_sequence:
             for tr in self.tracker_sequence.sequence:
                 win = tr._window(ts, n0)
@@ -543,6 +547,21 @@ class CardiacModel:
                     d.out = buf.data_ptr()
                     d.sample_offset = 0
                     d.capacity = count
+                elif isinstance(tr, SpiralWaveCore2DTracker):
+                    if n_tip >= _ffi.MAX_TIP:
+                        raise RuntimeError("at most one spiral-wave core "
+                                           "tracker per model")
+                    buf = tr._reserve(first, int(tr.step))
+                    d = a.tip[n_tip]
+                    n_tip += 1
+                    d.win.first, d.win.last, d.win.stride = first, last, \
+                        int(tr.step)
+                    d.threshold = float(tr.threshold)
+                    d.u_prev = tr._u_prev.data_ptr()
+                    d.out = buf.data_ptr()
+                    d.count = tr._count.data_ptr()
+                    d.capacity = int(tr.capacity)
+                    d.sample_offset = 0
                 elif isinstance(tr, _ProbeTracker):
                     buf = tr._reserve(count)
                     d = a.probe[n_pr]
@@ -562,6 +581,7 @@ class CardiacModel:
                                     "finitewave_gb300 tracker")
         a.n_at, a.n_lat, a.n_probe = n_at, n_lat, n_pr
         a.n_ecg = n_ecg
+        a.n_tip = n_tip
         a.status = self._status.data_ptr()
         return _Segment(a, n0, n_seg, t_end, keep)
 

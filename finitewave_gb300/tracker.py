@@ -364,3 +364,146 @@ class ECG2DTracker(Tracker):
 
 class ECG3DTracker(ECG2DTracker):
     """(cpuwave3D/tracker/ecg_3d_tracker.py: d includes (z - k)^2)"""
+
+
+class SpiralWaveCore2DTracker(Tracker):
+    """Spiral-wave tips (cpuwave2D/tracker/spiral_wave_core_2d_tracker.py:
+    9-249): on each tracked step, the cells whose ``threshold`` isoline is
+    crossed both at the previous tracked step and now, refined to the
+    intersection of the two bilinear isolines.  Found on the device
+    (fw_tip_tracker); the model runs in the plain form while one is
+    attached.  ``output`` is a pandas DataFrame with columns x, y, time,
+    step (x, y, z, time, step in 3D) when pandas is installed, else a dict
+    of the same columns as numpy arrays."""
+
+    _columns = ("x", "y")
+
+    def __init__(self):
+        super().__init__()
+        self.threshold = 0.5
+        self.file_name = "spiral_wave_core"
+        self.capacity = 1 << 16   # tips held per run() segment
+
+    def initialize(self, model):
+        self.model = model
+        # the reference copies model.u when the trackers are initialised,
+        # before the model sets its initial potential (zeros)
+        self._u_prev = model._dev["u"].clone()
+        self._count = torch.zeros(1, dtype=torch.int32,
+                                  device=model._device())
+        self._chunks = []   # (tips tensor, count snapshot, first step, stride)
+
+    def _reserve(self, first, stride):
+        self._close_chunk()
+        buf = torch.empty((int(self.capacity), 4), dtype=torch.float64,
+                          device=self.model._device())
+        self._count.zero_()
+        self._chunks.append([buf, None, first, stride])
+        return buf
+
+    def _close_chunk(self):
+        if self._chunks and self._chunks[-1][1] is None:
+            self._chunks[-1][1] = self._count.clone()
+
+    def _records(self):
+        self._close_chunk()
+        recs = []
+        for buf, count, first, stride in self._chunks:
+            c = int(count.item())
+            if c > self.capacity:
+                raise RuntimeError("SpiralWaveCore tracker: more tips than "
+                                   f"capacity={self.capacity} in one run "
+                                   "segment; raise capacity")
+            raw = buf[:c].cpu().numpy()
+            ints = raw[:, :2].copy().view(np.int32).reshape(c, 4)
+            sample, k, i, j = (ints[:, q].astype(np.int64) for q in range(4))
+            steps = first + sample * stride
+            recs.append((steps, k, i, j, raw[:, 2], raw[:, 3]))
+        if not recs:
+            z = np.zeros(0)
+            return (z.astype(np.int64),) * 4 + (z, z)
+        return tuple(np.concatenate(c) for c in zip(*recs))
+
+    @property
+    def output(self):
+        steps, k, i, j, x, y = self._records()
+        order = np.lexsort((j, i, k, steps))
+        steps, k, x, y = steps[order], k[order], x[order], y[order]
+        times = self.model._time_of_steps(steps) if steps.size else \
+            np.zeros(0)
+        cols = {"x": x, "y": y}
+        if len(self._columns) == 3:
+            cols["z"] = k
+        cols["time"] = times
+        cols["step"] = steps
+        try:
+            import pandas as pd
+        except ImportError:
+            return cols
+        return pd.DataFrame(cols)
+
+    def write(self):
+        out = self.output
+        path = Path(self.path, self.file_name).with_suffix(".csv")
+        if hasattr(out, "to_csv"):
+            out.to_csv(path)
+        else:
+            names = list(out)
+            np.savetxt(path, np.column_stack([out[n] for n in names]),
+                       delimiter=",", header=",".join(names), comments="")
+
+
+class SpiralWaveCore3DTracker(SpiralWaveCore2DTracker):
+    """(cpuwave3D/tracker/spiral_wave_core_3d_tracker.py): the 2D search in
+    every z layer; tips carry their layer as z."""
+
+    _columns = ("x", "y", "z")
+
+
+class Period2DTracker(LocalActivationTime2DTracker):
+    """Activation periods at given cells (cpuwave2D/tracker/
+    period_2d_tracker.py:7-95): the differences of each cell's successive
+    threshold crossings, from the device's crossing record.  ``output`` is a
+    pandas Series of arrays (one per cell) when pandas is installed, else a
+    list of arrays."""
+
+    def __init__(self):
+        super().__init__()
+        self.cell_ind = []
+        self.file_name = "period"
+
+    def _cells_flat(self):
+        cells = np.atleast_2d(np.asarray(self.cell_ind, dtype=np.int64))
+        return np.ravel_multi_index(tuple(cells.T), self._shape)
+
+    @property
+    def output(self):
+        flat = self._cells_flat()
+        count = self._count.cpu().numpy()[flat]
+        if (count > self.capacity).any():
+            raise RuntimeError("Period tracker: a cell crossed the threshold "
+                               f"more than capacity={self.capacity} times")
+        steps = self._steps.cpu().numpy()[:, flat]
+        periods = []
+        for c in range(len(flat)):
+            t = self.model._time_of_steps(steps[:count[c], c].astype(np.int64))
+            periods.append(np.diff(t))
+        try:
+            import pandas as pd
+        except ImportError:
+            return periods
+        return pd.Series(periods)
+
+    def write(self):
+        out = self.output
+        path = Path(self.path, self.file_name).with_suffix(".csv")
+        if hasattr(out, "to_csv"):
+            out.to_csv(path)
+        else:
+            with open(path, "w") as f:
+                for c, p in enumerate(out):
+                    f.write(f"{c}," + ",".join(repr(float(x)) for x in p) + "\n")
+
+
+class Period3DTracker(Period2DTracker):
+    """(cpuwave3D/tracker/period_3d_tracker.py)"""

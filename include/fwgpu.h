@@ -49,6 +49,7 @@ extern "C" {
 #define FW_DEV_PROBE_OVERFLOW 2 /* a probe sample index beyond capacity     */
 #define FW_DEV_BATCH_FAULT 4    /* a batch tile descriptor out of range     */
 #define FW_DEV_TIMEOUT 8        /* a bounded on-chip wait gave up           */
+#define FW_DEV_TIP_OVERFLOW 16  /* more spiral tips than the tracker holds  */
 
 /* ------------------------------------------------------------ enumerations */
 enum fw_model {
@@ -87,6 +88,7 @@ enum fw_stim_kind { FW_STIM_VOLTAGE = 0, FW_STIM_CURRENT = 1 };
 #define FW_MAX_LAT 2
 #define FW_MAX_PROBE 4
 #define FW_MAX_PROBE_VARS 8
+#define FW_MAX_TIP 1
 #define FW_MAX_ECG 2
 #define FW_MAX_ECG_LEADS 8
 
@@ -181,6 +183,33 @@ typedef struct fw_ecg_tracker {
     int64_t capacity; /* samples */
 } fw_ecg_tracker;
 
+/* One spiral-wave tip: grid cell (k, i, j) of the crossing and its position
+ * x = j + dy, y = i + dx inside the cell (the reference's [x, y]). */
+typedef struct fw_tip {
+    int32_t sample;   /* index of the tracked step (sample_offset + ...)  */
+    int32_t k, i, j;  /* k = z index (0 in 2D)                            */
+    double x, y;
+} fw_tip;
+
+/* SpiralWaveCore2DTracker / 3DTracker (cpuwave2D/tracker/
+ * spiral_wave_core_2d_tracker.py:88-249, cpuwave3D/tracker/
+ * spiral_wave_core_3d_tracker.py): on active steps, every cell (i, i+1) x
+ * (j, j+1) of every z layer with 5 <= i < ni - 5, 5 <= j < nj - 5 whose
+ * threshold isoline is crossed in both u_prev (the potential at the
+ * tracker's previous active step) and u is refined to the intersection of
+ * the two bilinear isolines; found tips are appended to `out` (order is not
+ * kept: the host sorts by sample, k, i, j) and `count` is advanced; then
+ * u_prev := u.  More than `capacity` tips set FW_DEV_TIP_OVERFLOW. */
+typedef struct fw_tip_tracker {
+    fw_window win;
+    double threshold;
+    void *u_prev;      /* (N) in the model precision, the last active u   */
+    fw_tip *out;
+    int32_t *count;    /* device, tips written so far                     */
+    int64_t capacity;  /* tips                                            */
+    int64_t sample_offset;
+} fw_tip_tracker;
+
 /* Everything one model instance needs to advance.  Replaces the body of
  * CardiacModel.run (core/model/cardiac_model.py:164-189) together with the
  * model's run_diffusion_kernel / run_ionic_kernel. */
@@ -219,8 +248,9 @@ typedef struct fw_step_args {
                                    for ANISO9, from fw_pack_weights; NULL
                                    when not available                       */
     int32_t n_ecg;
-    int32_t reserved;
+    int32_t n_tip;
     fw_ecg_tracker ecg[FW_MAX_ECG];
+    fw_tip_tracker tip[FW_MAX_TIP];
 } fw_step_args;
 
 /* A planned batch of tissues (fw_batch_plan).  Host-side handle; the
@@ -239,7 +269,7 @@ FW_API int fw_version(void);
 /* sizeof of the ABI structs as compiled into the library, so a binding can
  * check its own layout: which = 0 fw_step_args, 1 fw_stim, 2 fw_at_tracker,
  * 3 fw_lat_tracker, 4 fw_probe_tracker, 5 fw_window, 6 fw_batch,
- * 7 fw_ecg_tracker.  0 for unknown. */
+ * 7 fw_ecg_tracker, 8 fw_tip_tracker, 9 fw_tip.  0 for unknown. */
 FW_API size_t fw_struct_size(int32_t which);
 
 /* Number of kernels this library has launched in the process so far

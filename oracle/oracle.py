@@ -177,6 +177,59 @@ def _ionic(model, st, un, u, idx, dt, p):
         MODELS[model]["ionic"](L, un, u, st, idx, dt, p)
 
 
+def _tips_2d(u, u_new, threshold):
+    """_track_tip_line (spiral_wave_core_2d_tracker.py:152-249) restated in
+    numpy: cells (i, j), 5 <= i < ni - 5, 5 <= j < nj - 5, crossed by the
+    isoline in both u and u_new, refined by _correct_tip_pos; returns
+    [x, y] rows in the reference's raster order."""
+    ni, nj = u.shape
+
+    def crosses(a):
+        c = a[5:ni - 5, 5:nj - 5]
+        d1, d2, d3 = (a[6:ni - 4, 5:nj - 5], a[5:ni - 5, 6:nj - 4],
+                      a[6:ni - 4, 6:nj - 4])
+        up = (c >= threshold) & ((d1 < threshold) | (d2 < threshold) |
+                                 (d3 < threshold))
+        dn = (c < threshold) & ((d1 >= threshold) | (d2 >= threshold) |
+                                (d3 >= threshold))
+        return up | dn
+    cand = crosses(u) & crosses(u_new)
+    ii, jj = np.nonzero(cand)
+    ii, jj = ii + 5, jj + 5
+    with np.errstate(divide="ignore", invalid="ignore"):
+        AC = u[ii, jj] - u[ii, jj + 1] + u[ii + 1, jj + 1] - u[ii + 1, jj]
+        GC = u[ii, jj + 1] - u[ii, jj]
+        BC = u[ii + 1, jj] - u[ii, jj]
+        DC = u[ii, jj] - threshold
+        AD = (u_new[ii, jj] - u_new[ii, jj + 1] + u_new[ii + 1, jj + 1] -
+              u_new[ii + 1, jj])
+        GD = u_new[ii, jj + 1] - u_new[ii, jj]
+        BD = u_new[ii + 1, jj] - u_new[ii, jj]
+        DD = u_new[ii, jj] - threshold
+        Q = BC * AD - BD * AC
+        R = GC * AD - GD * AC
+        S = DC * AD - DD * AC
+        QOnR = Q / R
+        SOnR = S / R
+        T = AC * QOnR
+        U = AC * SOnR - BC + GC * QOnR
+        V = GC * SOnR - DC
+        disc = U * U - 4. * T * V
+        T2 = 2. * T
+        sq = np.sqrt(np.where(disc < 0, 0.0, disc))
+        xn = (-U - sq) / T2
+        xp = (-U + sq) / T2
+        yn = -QOnR * xn - SOnR
+        yp = -QOnR * xp - SOnR
+    ok = (disc >= 0) & (T2 != 0.)
+    n_in = (0 <= xn) & (xn <= 1) & (0 <= yn) & (yn <= 1)
+    p_in = (0 <= xp) & (xp <= 1) & (0 <= yp) & (yp <= 1)
+    cx = np.where(n_in, xn, xp)
+    cy = np.where(n_in, yn, yp)
+    keep = ok & (n_in | p_in)
+    return np.stack([jj[keep] + cy[keep], ii[keep] + cx[keep]], axis=1)
+
+
 def _ecg(u_tr, u, coords, dr, idx, shape):
     out = np.zeros(len(coords))
     nk = shape[2] if len(shape) == 3 else 1
@@ -226,7 +279,7 @@ def run(case):
     conductivity, D_al, D_ac, D_model (optional), params (overrides),
     stims (list of dicts: kind 'voltage'|'current', t, value, duration,
     u_max, and one of box / matrix / coords), trackers (list of dicts:
-    kind 'at'|'lat'|'probe'|'ecg', threshold, start_time, end_time, step,
+    kind 'at'|'lat'|'probe'|'ecg'|'tips', threshold, start_time, end_time, step,
     cells, vars), special (optional special_boundaries array),
     init (optional overrides of initial values).
     Returns dict with state arrays, u_new, t, step and tracker outputs.
@@ -270,6 +323,11 @@ def run(case):
                 np.atleast_2d(tr["coords"]), dtype=np.float64)
             tr["u_tr"] = np.zeros(mesh.shape)
             tr["samples"] = []
+        elif tr["kind"] == "tips":
+            # SpiralWaveCore*Tracker copies model.u at initialisation, while
+            # it is still zero (cardiac_model.py:96-108)
+            tr["u_prev"] = np.zeros(mesh.shape)
+            tr["rows"] = []
         trackers.append(tr)
 
     t = 0
@@ -309,6 +367,16 @@ def run(case):
                 for var in tr["vars"]:
                     arr = u if var == "u" else st[var]
                     tr["samples"][var].append(arr[ci].copy())
+            elif tr["kind"] == "tips":
+                if u.ndim == 2:
+                    layers = [(-1, tr["u_prev"], u)]
+                else:
+                    layers = [(k, tr["u_prev"][:, :, k], u[:, :, k])
+                              for k in range(u.shape[2])]
+                for k, up, uc in layers:
+                    for x, y in _tips_2d(up, uc, tr["threshold"]):
+                        tr["rows"].append((x, y, k, t, step))
+                tr["u_prev"] = u.copy()
             elif tr["kind"] == "ecg":
                 # ECG2DTracker.calc_ecg (ecg_2d_tracker.py:61-79)
                 _diffuse(kind, tr["u_tr"], u, w, idx)
@@ -331,6 +399,8 @@ def run(case):
             outs.append(np.array(tr["act_t"]))
         elif tr["kind"] == "ecg":
             outs.append(np.array(tr["samples"]))
+        elif tr["kind"] == "tips":
+            outs.append(np.array(tr["rows"], dtype=np.float64).reshape(-1, 5))
         else:
             outs.append({v: np.squeeze(tr["samples"][v])
                          for v in tr["vars"]})

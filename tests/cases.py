@@ -191,3 +191,32 @@ def ecg(dim):
                                    coords=[[7, 12, 4], [-2, 5, 3],
                                            [7, 5, 10.5]])])
     return case, {"ecg": g[f"d{dim}_ecg"], "u": g[f"d{dim}_u"]}
+
+
+def tips(dim):
+    """Spiral tips and periods: Aliev-Panfilov S1-S2 cross field on a 64^2
+    sheet (2D) or a 48 x 48 x 3 slab (3D), tips every 20 steps, local
+    activation (periods) at a few cells."""
+    g = load("tips")
+    n = 64 if dim == 2 else 48
+    shape = (n, n) if dim == 2 else (n, n, 3)
+    mesh = np.ones(shape, dtype=np.int8)
+    mesh[0], mesh[-1] = 0, 0
+    mesh[:, 0], mesh[:, -1] = 0, 0
+    if dim == 3:
+        mesh[:, :, 0] = mesh[:, :, -1] = 0
+    zb = [] if dim == 2 else [(0, 3)]
+    case = dict(model="ap", mesh=mesh, dt=0.01, dr=0.25, t_max=60,
+                stencil="iso5" if dim == 2 else "iso7",
+                stims=[dict(kind="voltage", t=0, value=1.0,
+                            box=[(0, n), (1, 4)] + zb),
+                       dict(kind="voltage", t=30, value=1.0,
+                            box=[(0, n // 2), (0, n)] + zb)],
+                trackers=[dict(kind="tips", threshold=0.5, step=20),
+                          dict(kind="lat", threshold=0.5)])
+    cells = g[f"d{dim}_cells"]
+    lens = g[f"d{dim}_period_len"]
+    flat = g[f"d{dim}_periods"]
+    periods = np.split(flat, np.cumsum(lens)[:-1]) if len(lens) else []
+    return case, {"tips": g[f"d{dim}_tips"], "u": g[f"d{dim}_u"],
+                  "cells": cells, "periods": periods}

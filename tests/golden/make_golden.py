@@ -522,6 +522,77 @@ def case_ecg(fw):
     return out
 
 
+def case_tips(fw):
+    """Spiral-wave tips and activation periods: Aliev-Panfilov S1-S2 cross
+    field stimulation (S1 columns 1-3 at t = 0, S2 on the first half of
+    the rows at t = 30) on a 64^2 sheet and a 48 x 48 x 3 slab (one
+    interior layer).  The tips
+    are recorded with the reference's own SpiralWaveCore tracker methods
+    (its output needs pandas, absent here), the periods from its
+    Period2DTracker's layers as its output computes them."""
+    out = {}
+
+    def tip_recorder(base):
+        class Rec(base):
+            def initialize(self, model):
+                super().initialize(model)
+                self.rec = []
+
+            def _track(self):
+                if self.model.u.ndim == 2:
+                    layers = [(None, self.u_prev, self.model.u)]
+                else:
+                    layers = [(k, self.u_prev[:, :, k], self.model.u[:, :, k])
+                              for k in range(self.model.u.shape[2])]
+                for k, up, uc in layers:
+                    for x, y in self.track_tip_line(up, uc, self.threshold):
+                        self.rec.append((x, y, -1 if k is None else k,
+                                         self.model.t, self.model.step))
+                self.u_prev = self.model.u.copy()
+        return Rec
+
+    for dim in (2, 3):
+        n = 64 if dim == 2 else 48
+        shape = (n, n) if dim == 2 else (n, n, 3)
+        tissue = (fw.CardiacTissue2D if dim == 2 else fw.CardiacTissue3D)(
+            list(shape))
+        ss = fw.StimSequence()
+        if dim == 2:
+            ss.add_stim(fw.StimVoltageCoord2D(0, 1, 0, n, 1, 4))
+            ss.add_stim(fw.StimVoltageCoord2D(30, 1, 0, n // 2, 0, n))
+            model = fw.AlievPanfilov2D()
+            tip = tip_recorder(fw.SpiralWaveCore2DTracker)()
+            per = fw.Period2DTracker()
+        else:
+            ss.add_stim(fw.StimVoltageCoord3D(0, 1, 0, n, 1, 4, 0, 3))
+            ss.add_stim(fw.StimVoltageCoord3D(30, 1, 0, n // 2, 0, n, 0, 3))
+            model = fw.AlievPanfilov3D()
+            tip = tip_recorder(fw.SpiralWaveCore3DTracker)()
+            per = fw.Period3DTracker()
+        model.dt, model.dr, model.t_max = 0.01, 0.25, 60
+        model.prog_bar = False
+        model.cardiac_tissue = tissue
+        model.stim_sequence = ss
+        tip.threshold = 0.5
+        tip.step = 20
+        cells = [[n // 2, n // 2], [10, 40], [40, 10]] if dim == 2 else \
+            [[24, 24, 1], [10, 40, 1]]
+        per.cell_ind = cells
+        per.threshold = 0.5
+        _attach(fw, model, [tip, per])
+        model.run()
+        rec = np.array(tip.rec, dtype=np.float64).reshape(-1, 5)
+        out[f"d{dim}_tips"] = rec
+        lats = np.array(per.act_t).T
+        periods = [np.diff(row[row != -1]) for row in lats]
+        out[f"d{dim}_period_len"] = np.array([len(p) for p in periods])
+        out[f"d{dim}_periods"] = np.concatenate(periods) if periods else \
+            np.zeros(0)
+        out[f"d{dim}_u"] = model.u
+        out[f"d{dim}_cells"] = np.array(cells)
+    return out
+
+
 CASES = {
     "weights_2d": case_weights_2d,
     "weights_3d": case_weights_3d,
@@ -535,6 +606,7 @@ CASES = {
     "courtemanche": case_courtemanche,
     "fibrosis": case_fibrosis,
     "ecg": case_ecg,
+    "tips": case_tips,
 }
 
 

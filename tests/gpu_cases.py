@@ -80,6 +80,14 @@ def build(case, npfloat="float64", form=None, fused_k=0, fused_variant=0):
         elif tr["kind"] == "lat":
             o = fg.LocalActivationTime2DTracker()
             o.threshold = tr["threshold"]
+        elif tr["kind"] == "tips":
+            o = fg.SpiralWaveCore2DTracker() if dim == 2 \
+                else fg.SpiralWaveCore3DTracker()
+            o.threshold = tr["threshold"]
+        elif tr["kind"] == "period":
+            o = fg.Period2DTracker() if dim == 2 else fg.Period3DTracker()
+            o.threshold = tr["threshold"]
+            o.cell_ind = tr["cells"]
         elif tr["kind"] == "ecg":
             o = fg.ECG2DTracker() if dim == 2 else fg.ECG3DTracker()
             o.measure_coords = np.asarray(tr["coords"], dtype=np.float64)

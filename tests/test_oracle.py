@@ -154,3 +154,24 @@ def test_ecg_bitwise(oracle, dim):
     r = oracle.run(case)
     assert np.array_equal(r["u"], g["u"])
     assert np.array_equal(r["trackers"][0], g["ecg"])
+
+
+def _periods_from_layers(layers, cells):
+    lats = np.array(layers)
+    out = []
+    for c in np.atleast_2d(cells):
+        row = lats[(slice(None),) + tuple(c)]
+        out.append(np.diff(row[row != -1]))
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_spiral_tips_and_periods_bitwise(oracle, dim):
+    case, g = cases.tips(dim)
+    r = oracle.run(case)
+    assert np.array_equal(r["u"], g["u"])
+    assert g["tips"].shape[0] > 0
+    assert np.array_equal(r["trackers"][0], g["tips"])
+    for got, want in zip(_periods_from_layers(r["trackers"][1], g["cells"]),
+                         g["periods"]):
+        assert np.array_equal(got, want)
