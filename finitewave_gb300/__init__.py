@@ -12,10 +12,11 @@ hand-written sm_103a CUDA (``libfwgpu.so``, C ABI in ``include/fwgpu.h``).
 from .batch import TissueBatch
 from .command import Command, CommandSequence
 from .fibrosis import Diffuse2DPattern, Diffuse3DPattern, FibrosisPattern
-from .model import (AlievPanfilov2D, AlievPanfilov3D, CardiacModel,
+from .model import (AlievPanfilov2D, AlievPanfilov3D, Barkley2D, Barkley3D,
+                    BuenoOrovio2D, BuenoOrovio3D, CardiacModel,
                     Courtemanche2D, Courtemanche3D, FentonKarma2D,
-                    FentonKarma3D, MitchellSchaeffer2D, MitchellSchaeffer3D,
-                    TP062D, TP063D)
+                    FentonKarma3D, LuoRudy912D, LuoRudy913D,
+                    MitchellSchaeffer2D, MitchellSchaeffer3D, TP062D, TP063D)
 from .serving import Request, SimulationServer, device_footprint
 from .state import StateLoader, StateSaver, StateSaverCollection
 from .stencil import (AsymmetricStencil2D, AsymmetricStencil3D,

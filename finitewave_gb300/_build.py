@@ -34,12 +34,16 @@ UNITS = {
     "fw_fused_ap.cu": ["--prec-div=false", "--ftz=true"],
     "fw_fused_ms.cu": ["--prec-div=false", "--ftz=true"],
     "fw_fused_fk.cu": ["--prec-div=false", "--ftz=true"],
+    "fw_fused_bk.cu": ["--prec-div=false", "--ftz=true"],
     "fw_step_detailed_tp06_f64.cu": ["--fmad=false"],
     "fw_step_detailed_tp06_f32.cu": ["--prec-div=false", "--prec-sqrt=false",
                                      "--ftz=true"],
     "fw_step_detailed_crn_f64.cu": ["--fmad=false"],
     "fw_step_detailed_crn_f32.cu": ["--prec-div=false", "--prec-sqrt=false",
                                     "--ftz=true"],
+    "fw_step_detailed_lr91_f64.cu": ["--fmad=false"],
+    "fw_step_detailed_lr91_f32.cu": ["--prec-div=false", "--prec-sqrt=false",
+                                     "--ftz=true"],
 }
 
 

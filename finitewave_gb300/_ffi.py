@@ -24,6 +24,7 @@ FW_DEV_TIMEOUT = 8
 FW_DEV_TIP_OVERFLOW = 16
 
 MODEL_AP, MODEL_MS, MODEL_FK, MODEL_TP06, MODEL_CRN = 1, 2, 3, 4, 5
+MODEL_BK, MODEL_BO, MODEL_LR91 = 6, 7, 8
 ISO5, ANISO9, ISO7, ANISO19 = 1, 2, 3, 4
 F64, F32 = 0, 1
 FORM_PLAIN, FORM_FUSED = 0, 1

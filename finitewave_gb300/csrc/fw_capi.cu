@@ -44,6 +44,9 @@ Info model_info(int32_t model)
     case FW_MODEL_FK: return {ModelFK::NS, ModelFK::NP};
     case FW_MODEL_TP06: return {ModelTP06::NS, ModelTP06::NP};
     case FW_MODEL_CRN: return {ModelCRN::NS, ModelCRN::NP};
+    case FW_MODEL_BK: return {ModelBK::NS, ModelBK::NP};
+    case FW_MODEL_BO: return {ModelBO::NS, ModelBO::NP};
+    case FW_MODEL_LR91: return {ModelLR91::NS, ModelLR91::NP};
     }
     return {-1, -1};
 }
@@ -220,6 +223,7 @@ int fw_state_is_f64(int32_t model, int32_t precision, int32_t index)
     switch (model) {
     case FW_MODEL_TP06: return fw::ModelTP06::is_conc(index) ? 1 : 0;
     case FW_MODEL_CRN: return fw::ModelCRN::is_conc(index) ? 1 : 0;
+    case FW_MODEL_LR91: return fw::ModelLR91::is_conc(index) ? 1 : 0;
     default: return 0;
     }
 }

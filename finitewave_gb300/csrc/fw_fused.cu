@@ -42,6 +42,7 @@ int step_fused(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     case FW_MODEL_AP: return step_fused_ap(a, n_begin, n_steps, stream);
     case FW_MODEL_MS: return step_fused_ms(a, n_begin, n_steps, stream);
     case FW_MODEL_FK: return step_fused_fk(a, n_begin, n_steps, stream);
+    case FW_MODEL_BK: return step_fused_bk(a, n_begin, n_steps, stream);
     }
     set_error("fw_step (fused): model %d has no fused form", a->model);
     return FW_ERR_UNSUPPORTED;

@@ -145,6 +145,8 @@ int step_fused_ms(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                   cudaStream_t stream);
 int step_fused_fk(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                   cudaStream_t stream);
+int step_fused_bk(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                  cudaStream_t stream);
 
 int batch_plan_size(const fw_step_args *const *tissues, int32_t n,
                     int64_t *bytes);
@@ -169,6 +171,8 @@ FW_DECLARE_DETAILED(tp06_f64)
 FW_DECLARE_DETAILED(tp06_f32)
 FW_DECLARE_DETAILED(crn_f64)
 FW_DECLARE_DETAILED(crn_f32)
+FW_DECLARE_DETAILED(lr91_f64)
+FW_DECLARE_DETAILED(lr91_f32)
 #undef FW_DECLARE_DETAILED
 
 }  // namespace fw

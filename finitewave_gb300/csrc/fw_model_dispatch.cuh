@@ -22,6 +22,8 @@ int dispatch_model(int32_t model, int32_t precision, const F &f)
         FW_MODEL_CASE(FW_MODEL_AP, ModelAP)
         FW_MODEL_CASE(FW_MODEL_MS, ModelMS)
         FW_MODEL_CASE(FW_MODEL_FK, ModelFK)
+        FW_MODEL_CASE(FW_MODEL_BK, ModelBK)
+        FW_MODEL_CASE(FW_MODEL_BO, ModelBO)
     }
 #undef FW_MODEL_CASE
     set_error("model %d not supported", model);
@@ -58,6 +60,8 @@ int dispatch_model_stencil(int32_t model, int32_t stencil, int32_t precision,
     case FW_MODEL_AP: return dispatch_stencil<ModelAP>(stencil, precision, f);
     case FW_MODEL_MS: return dispatch_stencil<ModelMS>(stencil, precision, f);
     case FW_MODEL_FK: return dispatch_stencil<ModelFK>(stencil, precision, f);
+    case FW_MODEL_BK: return dispatch_stencil<ModelBK>(stencil, precision, f);
+    case FW_MODEL_BO: return dispatch_stencil<ModelBO>(stencil, precision, f);
     }
     set_error("model %d not supported", model);
     return FW_ERR_UNSUPPORTED;

@@ -192,4 +192,127 @@ struct ModelFK {
     }
 };
 
+// Barkley.  params: a, b, eap (barkley_2d.py:69-71, ionic_kernel_2d
+// signature :141); calc_v (:114-138) then the voltage update with the new v
+// (:141-170).
+struct ModelBK {
+    static constexpr int NS = 1, NP = 3;
+    template <class T>
+    struct St {
+        T v;
+    };
+    template <class T>
+    __device__ static __forceinline__ St<T> load(void *const *s, int64_t p)
+    {
+        return {((const T *)s[0])[p]};
+    }
+    template <class T>
+    __device__ static __forceinline__ void store(void *const *s, int64_t p,
+                                                 const St<T> &x)
+    {
+        ((T *)s[0])[p] = x.v;
+    }
+    template <class T>
+    __device__ static __forceinline__ double probe(const St<T> &x, int)
+    {
+        return (double)x.v;
+    }
+    template <class T>
+    __device__ static __forceinline__ St<T> from_array(const T *a)
+    {
+        return {a[0]};
+    }
+    template <class T>
+    __device__ static __forceinline__ T update(T u, T un, St<T> &x,
+                                               const Params<T, NP> &P, T dt)
+    {
+        const T a = P.v[0], b = P.v[1], eap = P.v[2];
+        T v = x.v;
+        v += dt * (u - v);
+        x.v = v;
+        return un + dt * (u * ((T)1 - u) * (u - (v + b) / a)) / eap;
+    }
+};
+
+// Bueno-Orovio (minimal ventricular).  params in ionic_kernel_2d's order
+// (bueno_orovio_2d.py, signature after the state arrays): u_o, u_u,
+// theta_v, theta_w, theta_v_m, theta_o, tau_v1_m, tau_v2_m, tau_v_p,
+// tau_w1_m, tau_w2_m, k_w_m, u_w_m, tau_w_p, tau_fi, tau_o1, tau_o2,
+// tau_so1, tau_so2, k_so, u_so, tau_s1, tau_s2, k_s, u_s, tau_si, tau_w_inf,
+// w_inf_.  calc_v, calc_w, calc_s, J_fi, J_so, J_si with the updated gates
+// (ionic_kernel_2d, bueno_orovio_2d.py).
+struct ModelBO {
+    static constexpr int NS = 3, NP = 28;
+    enum {
+        u_o, u_u, theta_v, theta_w, theta_v_m, theta_o, tau_v1_m, tau_v2_m,
+        tau_v_p, tau_w1_m, tau_w2_m, k_w_m, u_w_m, tau_w_p, tau_fi, tau_o1,
+        tau_o2, tau_so1, tau_so2, k_so, u_so, tau_s1, tau_s2, k_s, u_s, tau_si,
+        tau_w_inf, w_inf_
+    };
+    template <class T>
+    struct St {
+        T v, w, s;
+    };
+    template <class T>
+    __device__ static __forceinline__ St<T> load(void *const *s, int64_t p)
+    {
+        return {((const T *)s[0])[p], ((const T *)s[1])[p],
+                ((const T *)s[2])[p]};
+    }
+    template <class T>
+    __device__ static __forceinline__ void store(void *const *s, int64_t p,
+                                                 const St<T> &x)
+    {
+        ((T *)s[0])[p] = x.v;
+        ((T *)s[1])[p] = x.w;
+        ((T *)s[2])[p] = x.s;
+    }
+    template <class T>
+    __device__ static __forceinline__ double probe(const St<T> &x, int i)
+    {
+        return i == 0 ? (double)x.v : i == 1 ? (double)x.w : (double)x.s;
+    }
+    template <class T>
+    __device__ static __forceinline__ St<T> from_array(const T *a)
+    {
+        return {a[0], a[1], a[2]};
+    }
+    template <class T>
+    __device__ static __forceinline__ T update(T u, T un, St<T> &x,
+                                               const Params<T, NP> &P, T dt)
+    {
+        const T one = (T)1, two = (T)2;
+        // calc_v_inf, calc_tau_v_m, calc_v
+        const T v_inf = u < P.v[theta_v_m] ? one : (T)0;
+        const T tau_v_m = (u - P.v[theta_v_m]) < 0 ? P.v[tau_v1_m] : P.v[tau_v2_m];
+        const T dv = (u - P.v[theta_v]) < 0 ? (v_inf - x.v) / tau_v_m
+                                            : -x.v / P.v[tau_v_p];
+        x.v += dt * dv;
+        // calc_w_inf, calc_tau_w_m, calc_w
+        const T w_inf = (u - P.v[theta_o]) < 0 ? one - u / P.v[tau_w_inf]
+                                               : P.v[w_inf_];
+        const T tau_w_m = P.v[tau_w1_m] + (P.v[tau_w2_m] - P.v[tau_w1_m]) *
+                                              (one + fw_tanh(P.v[k_w_m] * (u - P.v[u_w_m]))) /
+                                              two;
+        const T dw = (u - P.v[theta_w]) < 0 ? (w_inf - x.w) / tau_w_m
+                                            : -x.w / P.v[tau_w_p];
+        x.w += dt * dw;
+        // calc_tau_s, calc_s
+        const T tau_s = (u - P.v[theta_w]) < 0 ? P.v[tau_s1] : P.v[tau_s2];
+        x.s += dt * ((one + fw_tanh(P.v[k_s] * (u - P.v[u_s]))) / two - x.s) /
+               tau_s;
+        // calc_Jfi, calc_Jso (calc_tau_o, calc_tau_so), calc_Jsi
+        const T Hv = (u - P.v[theta_v]) >= 0 ? one : (T)0;
+        const T J_fi = -x.v * Hv * (u - P.v[theta_v]) * (P.v[u_u] - u) / P.v[tau_fi];
+        const T tau_o = (u - P.v[theta_o]) < 0 ? P.v[tau_o1] : P.v[tau_o2];
+        const T tau_so = P.v[tau_so1] + (P.v[tau_so2] - P.v[tau_so1]) *
+                                            (one + fw_tanh(P.v[k_so] * (u - P.v[u_so]))) /
+                                            two;
+        const T Hw = (u - P.v[theta_w]) >= 0 ? one : (T)0;
+        const T J_so = (u - P.v[u_o]) * (one - Hw) / tau_o + Hw / tau_so;
+        const T J_si = -Hw * x.w * x.s / P.v[tau_si];
+        return un + dt * (-J_fi - J_so - J_si);
+    }
+};
+
 }  // namespace fw

@@ -678,4 +678,168 @@ struct ModelCRN {
     }
 };
 
+// ---------------------------------------------------------------- LR91
+// Luo-Rudy 1991.  Parameters in the order of luo_rudy91_2d.py's
+// ionic_kernel_2d signature: gna, gsi, gk, gk1, gkp, gb, ko, ki, nai, nao,
+// cao, R, T, F, PR_NaK; state m, h, j, d, f, x, cai (LuoRudy912D.state_vars
+// minus u).  calc_ina uses the updated m, h, j; calc_isk and calc_ik the
+// gates before their update, as the reference does.  Under FW_F32 Ca_i is
+// stored as float64 and only its accumulation is float64.
+struct ModelLR91 {
+    static constexpr int NS = 7, NP = 15;
+    enum { gna, gsi, gk, gk1, gkp, gb, ko, ki, nai, nao, cao, R, T_, F, PR_NaK };
+    enum { s_m, s_h, s_j, s_d, s_f, s_x, s_cai };
+    static constexpr bool is_conc(int i) { return i == s_cai; }
+
+    template <class T>
+    struct St {
+        T m, h, j, d, f, x;
+        double cai;
+    };
+    template <class T>
+    __device__ static __forceinline__ St<T> load(void *const *S, int64_t p)
+    {
+        St<T> x;
+        x.m = ((const T *)S[s_m])[p];
+        x.h = ((const T *)S[s_h])[p];
+        x.j = ((const T *)S[s_j])[p];
+        x.d = ((const T *)S[s_d])[p];
+        x.f = ((const T *)S[s_f])[p];
+        x.x = ((const T *)S[s_x])[p];
+        x.cai = ((const double *)S[s_cai])[p];
+        return x;
+    }
+    template <class T>
+    __device__ static __forceinline__ void store(void *const *S, int64_t p,
+                                                 const St<T> &x)
+    {
+        ((T *)S[s_m])[p] = x.m;
+        ((T *)S[s_h])[p] = x.h;
+        ((T *)S[s_j])[p] = x.j;
+        ((T *)S[s_d])[p] = x.d;
+        ((T *)S[s_f])[p] = x.f;
+        ((T *)S[s_x])[p] = x.x;
+        ((double *)S[s_cai])[p] = x.cai;
+    }
+    template <class T>
+    __device__ static __forceinline__ double probe(const St<T> &x, int i)
+    {
+        switch (i) {
+        case s_m: return x.m;
+        case s_h: return x.h;
+        case s_j: return x.j;
+        case s_d: return x.d;
+        case s_f: return x.f;
+        case s_x: return x.x;
+        default: return x.cai;
+        }
+    }
+    // calc_gating_var (luo_rudy91_2d.py): tau = 1 / (a + b),
+    // inf = a / (a + b), var += dt (inf - var) / tau
+    template <class T>
+    __device__ static __forceinline__ T gating(T var, T dt, T a, T b)
+    {
+        const T tau = (T)1. / (a + b);
+        const T inf = a / (a + b);
+        return var + dt * (inf - var) / tau;
+    }
+
+    template <class T>
+    __device__ static __forceinline__ T update(T u, T un, St<T> &x,
+                                               const Params<T, NP> &P, T dt)
+    {
+        const T c1 = (T)1;
+        const T RTF = P.v[R] * P.v[T_] / P.v[F];
+        const T E_Na = RTF * mlog(P.v[nao] / P.v[nai]);
+        // calc_ina
+        T ina;
+        {
+            T alpha_h = 0, beta_h = 0, beta_J = 0, alpha_J = 0;
+            if (u >= (T)(-40.)) {
+                beta_h = (T)1. / ((T)0.13 * (c1 + mexp((u + (T)10.66) / (T)(-11.1))));
+                beta_J = (T)0.3 * mexp((T)(-2.535) * (T)1e-07 * u) /
+                         (c1 + mexp((T)(-0.1) * (u + (T)32)));
+            } else {
+                alpha_h = (T)0.135 * mexp(((T)80 + u) / (T)(-6.8));
+                beta_h = (T)3.56 * mexp((T)0.079 * u) +
+                         (T)3.1 * (T)1e5 * mexp((T)0.35 * u);
+                beta_J = (T)0.1212 * mexp((T)(-0.01052) * u) /
+                         (c1 + mexp((T)(-0.1378) * (u + (T)40.14)));
+                alpha_J = ((T)(-1.2714) * (T)1e5 * mexp((T)0.2444 * u) -
+                           (T)3.474 * (T)1e-5 * mexp((T)(-0.04391) * u)) *
+                          (u + (T)37.78) / (c1 + mexp((T)0.311 * (u + (T)79.23)));
+            }
+            T alpha_m;
+            if constexpr (sizeof(T) == 8)
+                alpha_m = (T)0.32 * (u + (T)47.13) /
+                          (c1 - mexp((T)(-0.1) * (u + (T)47.13)));
+            else
+                alpha_m = (T)3.2 * x_expm1((T)(-0.1) * (u + (T)47.13));
+            const T beta_m = (T)0.08 * mexp(-u / (T)11);
+            x.m = gating(x.m, dt, alpha_m, beta_m);
+            x.h = gating(x.h, dt, alpha_h, beta_h);
+            x.j = gating(x.j, dt, alpha_J, beta_J);
+            ina = P.v[gna] * x.m * x.m * x.m * x.h * x.j * (u - E_Na);
+        }
+        // calc_isk (gates before the update)
+        T isi;
+        {
+            const T cai = (T)x.cai;
+            const T E_Si = (T)7.7 - (T)13.0287 * mlog(cai);
+            isi = P.v[gsi] * x.d * x.f * (u - E_Si);
+            const T alpha_d = (T)0.095 * mexp((T)(-0.01) * (u - (T)5)) /
+                              (c1 + mexp((T)(-0.072) * (u - (T)5)));
+            const T beta_d = (T)0.07 * mexp((T)(-0.017) * (u + (T)44)) /
+                             (c1 + mexp((T)0.05 * (u + (T)44)));
+            const T alpha_f = (T)0.012 * mexp((T)(-0.008) * (u + (T)28)) /
+                              (c1 + mexp((T)0.15 * (u + (T)28)));
+            const T beta_f = (T)0.0065 * mexp((T)(-0.02) * (u + (T)30)) /
+                             (c1 + mexp((T)(-0.2) * (u + (T)30)));
+            x.d = gating(x.d, dt, alpha_d, beta_d);
+            x.f = gating(x.f, dt, alpha_f, beta_f);
+            x.cai += dt * ((T)(-0.0001) * isi + (T)0.07 * ((T)0.0001 - cai));
+        }
+        // calc_ik (gate before the update)
+        T ik;
+        {
+            const T E_K = RTF * mlog((P.v[ko] + P.v[PR_NaK] * P.v[nao]) /
+                                     (P.v[ki] + P.v[PR_NaK] * P.v[nai]));
+            const T G_K = P.v[gk] * fw_sqrt(P.v[ko] / (T)5.4);
+            T Xi;
+            if (u > (T)(-100)) {
+                if constexpr (sizeof(T) == 8)
+                    Xi = (T)2.837 * (mexp((T)0.04 * (u + (T)77)) - c1) /
+                         ((u + (T)77) * mexp((T)0.04 * (u + (T)35)));
+                else  // (e^z - 1) / (u + 77) = 0.04 / x_expm1(z)
+                    Xi = (T)(2.837 * 0.04) /
+                         (x_expm1((T)0.04 * (u + (T)77)) *
+                          mexp((T)0.04 * (u + (T)35)));
+            } else {
+                Xi = c1;
+            }
+            ik = G_K * x.x * Xi * (u - E_K);
+            const T alpha_x = (T)0.0005 * mexp((T)0.083 * (u + (T)50)) /
+                              (c1 + mexp((T)0.057 * (u + (T)50)));
+            const T beta_x = (T)0.0013 * mexp((T)(-0.06) * (u + (T)20)) /
+                             (c1 + mexp((T)(-0.04) * (u + (T)20)));
+            x.x = gating(x.x, dt, alpha_x, beta_x);
+        }
+        const T E_K1 = RTF * mlog(P.v[ko] / P.v[ki]);
+        // calc_ik1
+        const T alpha_K1 = (T)1.02 / (c1 + mexp((T)0.2385 * (u - E_K1 - (T)59.215)));
+        const T beta_K1 = ((T)0.49124 * mexp((T)0.08032 * (u - E_K1 + (T)5.476)) +
+                           mexp((T)0.06175 * (u - E_K1 - (T)594.31))) /
+                          (c1 + mexp((T)(-0.5143) * (u - E_K1 + (T)4.753)));
+        const T K_1x = alpha_K1 / (alpha_K1 + beta_K1);
+        const T G_K1 = P.v[gk1] * fw_sqrt(P.v[ko] / (T)5.4);
+        const T ik1 = G_K1 * K_1x * (u - E_K1);
+        // calc_ikp, calc_ib
+        const T K_p = (T)1. / (c1 + mexp(((T)7.488 - u) / (T)5.98));
+        const T ikp = P.v[gkp] * K_p * (u - E_K1);
+        const T ib = P.v[gb] * (u + (T)59.87);
+        const T ik1t = ik1 + ikp + ib;
+        return un - dt * (ina + isi + ik1t + ik);
+    }
+};
+
 }  // namespace fw

@@ -23,6 +23,9 @@ int step_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     if (a->model == FW_MODEL_CRN)
         return f64 ? plain_crn_f64(a, n_begin, n_steps, stream)
                    : plain_crn_f32(a, n_begin, n_steps, stream);
+    if (a->model == FW_MODEL_LR91)
+        return f64 ? plain_lr91_f64(a, n_begin, n_steps, stream)
+                   : plain_lr91_f32(a, n_begin, n_steps, stream);
     PlainDispatch d{a, n_begin, n_steps, stream};
     return dispatch_model_stencil(a->model, a->stencil, a->precision, d);
 }
@@ -31,7 +34,8 @@ int ionic(int32_t model, int32_t precision, void *u_new, const void *u,
           void *const *state, const int64_t *idx, int64_t n_idx, double dt,
           const double *params, cudaStream_t stream)
 {
-    if ((model == FW_MODEL_TP06 || model == FW_MODEL_CRN) &&
+    if ((model == FW_MODEL_TP06 || model == FW_MODEL_CRN ||
+         model == FW_MODEL_LR91) &&
         precision != FW_F64 && precision != FW_F32) {
         set_error("unknown precision %d", precision);
         return FW_ERR_ARG;
@@ -42,6 +46,9 @@ int ionic(int32_t model, int32_t precision, void *u_new, const void *u,
             u_new, u, state, idx, n_idx, dt, params, stream);
     if (model == FW_MODEL_CRN)
         return (f64 ? ionic_crn_f64 : ionic_crn_f32)(
+            u_new, u, state, idx, n_idx, dt, params, stream);
+    if (model == FW_MODEL_LR91)
+        return (f64 ? ionic_lr91_f64 : ionic_lr91_f32)(
             u_new, u, state, idx, n_idx, dt, params, stream);
     IonicDispatch d{u_new, u, state, idx, n_idx, dt, params, stream};
     return dispatch_model(model, precision, d);

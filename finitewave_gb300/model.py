@@ -377,7 +377,8 @@ class CardiacModel:
         n_seg = int(np.argmax(stop)) + 1 if stop.any() else limit
         return ts_all[:n_seg], float(ts_all[n_seg]), n_seg
 
-    _FUSED_MODELS = (_ffi.MODEL_AP, _ffi.MODEL_MS, _ffi.MODEL_FK)
+    _FUSED_MODELS = (_ffi.MODEL_AP, _ffi.MODEL_MS, _ffi.MODEL_FK,
+                     _ffi.MODEL_BK)
 
     def _fused_ok(self):
         """The fused form covers 2D float32 AP/MS/FK without special
@@ -843,6 +844,115 @@ class Courtemanche2D(CardiacModel):
 
 class Courtemanche3D(Courtemanche2D):
     """(cpuwave3D/model/courtemanche_3d.py:40-88)"""
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_3d(cardiac_tissue)
+
+
+class Barkley2D(CardiacModel):
+    """Barkley (cpuwave2D/model/barkley_2d.py:8-170)."""
+
+    _model_id = _ffi.MODEL_BK
+    _state_names = ("v",)
+    _param_names = ("a", "b", "eap")
+
+    def __init__(self):
+        super().__init__()
+        self.D_model = 1.
+        self.state_vars = ["u", "v"]
+        self.npfloat = "float64"
+        self.a = 0.75
+        self.b = 0.02
+        self.eap = 0.02
+        self.init_u = 0.0
+        self.init_v = 0
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_2d(cardiac_tissue)
+
+
+class Barkley3D(Barkley2D):
+    """(cpuwave3D/model/barkley_3d.py)"""
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_3d(cardiac_tissue)
+
+
+class BuenoOrovio2D(CardiacModel):
+    """Bueno-Orovio minimal ventricular model (cpuwave2D/model/
+    bueno_orovio_2d.py:13-180); parameters in ionic_kernel_2d's order."""
+
+    _model_id = _ffi.MODEL_BO
+    _state_names = ("v", "w", "s")
+    _param_names = ("u_o", "u_u", "theta_v", "theta_w", "theta_v_m",
+                    "theta_o", "tau_v1_m", "tau_v2_m", "tau_v_p", "tau_w1_m",
+                    "tau_w2_m", "k_w_m", "u_w_m", "tau_w_p", "tau_fi",
+                    "tau_o1", "tau_o2", "tau_so1", "tau_so2", "k_so", "u_so",
+                    "tau_s1", "tau_s2", "k_s", "u_s", "tau_si", "tau_w_inf",
+                    "w_inf_")
+
+    def __init__(self):
+        super().__init__()
+        self.D_model = 1.
+        self.state_vars = ["u", "v", "w", "s"]
+        self.npfloat = "float64"
+        self.u_o, self.u_u = 0.0, 1.55
+        self.theta_v, self.theta_w = 0.3, 0.13
+        self.theta_v_m, self.theta_o = 0.006, 0.006
+        self.tau_v1_m, self.tau_v2_m, self.tau_v_p = 60, 1150, 1.4506
+        self.tau_w1_m, self.tau_w2_m = 60, 15
+        self.k_w_m, self.u_w_m, self.tau_w_p = 65, 0.03, 200
+        self.tau_fi, self.tau_o1, self.tau_o2 = 0.11, 400, 6
+        self.tau_so1, self.tau_so2 = 30.0181, 0.9957
+        self.k_so, self.u_so = 2.0458, 0.65
+        self.tau_s1, self.tau_s2 = 2.7342, 16
+        self.k_s, self.u_s = 2.0994, 0.9087
+        self.tau_si, self.tau_w_inf, self.w_inf_ = 1.8875, 0.07, 0.94
+        self.init_u, self.init_v, self.init_w, self.init_s = 0.0, 1.0, 1.0, 0.0
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_2d(cardiac_tissue)
+
+
+class BuenoOrovio3D(BuenoOrovio2D):
+    """(cpuwave3D/model/bueno_orovio_3d.py)"""
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_3d(cardiac_tissue)
+
+
+class LuoRudy912D(CardiacModel):
+    """Luo-Rudy 1991 (cpuwave2D/model/luo_rudy91_2d.py); parameters in
+    ionic_kernel_2d's order.  Under npfloat float32, cai stays float64."""
+
+    _model_id = _ffi.MODEL_LR91
+    _reset_u_new = True
+    _state_names = ("m", "h", "j", "d", "f", "x", "cai")
+    _param_names = ("gna", "gsi", "gk", "gk1", "gkp", "gb", "ko", "ki",
+                    "nai", "nao", "cao", "R", "T", "F", "PR_NaK")
+
+    def __init__(self):
+        super().__init__()
+        self.D_model = 0.1
+        self.state_vars = ["u"] + list(self._state_names)
+        self.npfloat = "float64"
+        self.gna, self.gsi, self.gk = 23.0, 0.09, 0.282
+        self.gk1, self.gkp, self.gb = 0.6047, 0.0183, 0.03921
+        self.ko, self.ki, self.nai = 5.4, 145.0, 18.0
+        self.nao, self.cao = 140.0, 1.8
+        self.R, self.T, self.F = 8.314, 310.0, 96.5
+        self.PR_NaK = 0.01833
+        self.init_u = -84.5
+        self.init_m, self.init_h, self.init_j = 0.0017, 0.9832, 0.995484
+        self.init_d, self.init_f, self.init_x = 0.000003, 1.0, 0.0057
+        self.init_cai = 0.0002
+
+    def select_stencil(self, cardiac_tissue):
+        return _stencil_2d(cardiac_tissue)
+
+
+class LuoRudy913D(LuoRudy912D):
+    """(cpuwave3D/model/luo_rudy91_3d.py)"""
 
     def select_stencil(self, cardiac_tissue):
         return _stencil_3d(cardiac_tissue)

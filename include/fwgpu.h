@@ -57,7 +57,10 @@ enum fw_model {
     FW_MODEL_MS = 2,   /* Mitchell-Schaeffer   cpuwave2D/model/mitchell_schaeffer_2d.py */
     FW_MODEL_FK = 3,   /* Fenton-Karma (MLR-I) cpuwave2D/model/fenton_karma_2d.py    */
     FW_MODEL_TP06 = 4, /* ten Tusscher-Panfilov 2006 cpuwave2D/model/tp06_2d.py      */
-    FW_MODEL_CRN = 5   /* Courtemanche 1998    cpuwave2D/model/courtemanche_2d.py    */
+    FW_MODEL_CRN = 5,  /* Courtemanche 1998    cpuwave2D/model/courtemanche_2d.py    */
+    FW_MODEL_BK = 6,   /* Barkley              cpuwave2D/model/barkley_2d.py         */
+    FW_MODEL_BO = 7,   /* Bueno-Orovio         cpuwave2D/model/bueno_orovio_2d.py    */
+    FW_MODEL_LR91 = 8  /* Luo-Rudy 1991        cpuwave2D/model/luo_rudy91_2d.py      */
 };
 
 enum fw_stencil {

@@ -525,3 +525,162 @@ EXPORT void fwo_ionic_crn(double *un, const double *u, double *const *S,
         S[Q_wrel][p] = wrel;
     }
 }
+
+/* ------------------------------------------------------------ Barkley */
+/* ionic_kernel_2d (cpuwave2D/model/barkley_2d.py:114-170); P = a, b, eap;
+ * S = v. */
+EXPORT void fwo_ionic_bk(double *un, const double *u, double *const *S,
+                         const int64_t *idx, int64_t n_idx, double dt,
+                         const double *P)
+{
+    const double a = P[0], b = P[1], eap = P[2];
+    #pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < n_idx; ++t) {
+        const int64_t p = idx[t];
+        const double uu = u[p];
+        double v = S[0][p];
+        v += dt * (uu - v);
+        S[0][p] = v;
+        un[p] += dt * (uu * (1 - uu) * (uu - (v + b) / a)) / eap;
+    }
+}
+
+/* ------------------------------------------------------- Bueno-Orovio */
+/* ionic_kernel_2d and calc_* (cpuwave2D/model/bueno_orovio_2d.py:184-460);
+ * P in the kernel's parameter order; S = v, w, s. */
+EXPORT void fwo_ionic_bo(double *un, const double *u, double *const *S,
+                         const int64_t *idx, int64_t n_idx, double dt,
+                         const double *P)
+{
+    const double u_o = P[0], u_u = P[1], theta_v = P[2], theta_w = P[3],
+                 theta_v_m = P[4], theta_o = P[5], tau_v1_m = P[6],
+                 tau_v2_m = P[7], tau_v_p = P[8], tau_w1_m = P[9],
+                 tau_w2_m = P[10], k_w_m = P[11], u_w_m = P[12],
+                 tau_w_p = P[13], tau_fi = P[14], tau_o1 = P[15],
+                 tau_o2 = P[16], tau_so1 = P[17], tau_so2 = P[18],
+                 k_so = P[19], u_so = P[20], tau_s1 = P[21], tau_s2 = P[22],
+                 k_s = P[23], u_s = P[24], tau_si = P[25],
+                 tau_w_inf = P[26], w_inf_ = P[27];
+    #pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < n_idx; ++t) {
+        const int64_t p = idx[t];
+        const double uu = u[p];
+        double v = S[0][p], w = S[1][p], s = S[2][p];
+        const double v_inf = uu < theta_v_m ? 1.0 : 0.0;
+        const double tau_v_m = (uu - theta_v_m) < 0 ? tau_v1_m : tau_v2_m;
+        const double v_ = (uu - theta_v) < 0 ? (v_inf - v) / tau_v_m
+                                             : -v / tau_v_p;
+        v += dt * v_;
+        const double w_inf = (uu - theta_o) < 0 ? 1 - uu / tau_w_inf : w_inf_;
+        const double tau_w_m = tau_w1_m + (tau_w2_m - tau_w1_m) *
+                                              (1 + tanh(k_w_m * (uu - u_w_m))) / 2;
+        const double w_ = (uu - theta_w) < 0 ? (w_inf - w) / tau_w_m
+                                             : -w / tau_w_p;
+        w += dt * w_;
+        const double tau_s = (uu - theta_w) < 0 ? tau_s1 : tau_s2;
+        s += dt * ((1 + tanh(k_s * (uu - u_s))) / 2 - s) / tau_s;
+        const double Hv = (uu - theta_v) >= 0 ? 1.0 : 0.0;
+        const double J_fi = -v * Hv * (uu - theta_v) * (u_u - uu) / tau_fi;
+        const double tau_o = (uu - theta_o) < 0 ? tau_o1 : tau_o2;
+        const double tau_so = tau_so1 + (tau_so2 - tau_so1) *
+                                            (1 + tanh(k_so * (uu - u_so))) / 2;
+        const double Hw = (uu - theta_w) >= 0 ? 1.0 : 0.0;
+        const double J_so = (uu - u_o) * (1 - Hw) / tau_o + Hw / tau_so;
+        const double J_si = -Hw * w * s / tau_si;
+        S[0][p] = v;
+        S[1][p] = w;
+        S[2][p] = s;
+        un[p] += dt * (-J_fi - J_so - J_si);
+    }
+}
+
+/* ---------------------------------------------------------------- LR91 */
+static inline double lr_gate(double var, double dt, double a, double b)
+{
+    const double tau = 1. / (a + b);
+    const double inf = a / (a + b);
+    return var + dt * (inf - var) / tau;
+}
+
+/* ionic_kernel_2d and calc_* (cpuwave2D/model/luo_rudy91_2d.py); P = gna,
+ * gsi, gk, gk1, gkp, gb, ko, ki, nai, nao, cao, R, T, F, PR_NaK; S = m, h,
+ * j, d, f, x, cai. */
+EXPORT void fwo_ionic_lr91(double *un, const double *u, double *const *S,
+                           const int64_t *idx, int64_t n_idx, double dt,
+                           const double *P)
+{
+    const double gna = P[0], gsi = P[1], gk = P[2], gk1 = P[3], gkp = P[4],
+                 gb = P[5], ko = P[6], ki = P[7], nai = P[8], nao = P[9],
+                 R = P[11], T = P[12], F = P[13], PR_NaK = P[14];
+    const double E_Na = (R * T / F) * log(nao / nai);
+    #pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < n_idx; ++t) {
+        const int64_t p = idx[t];
+        const double uu = u[p];
+        double m = S[0][p], h = S[1][p], j = S[2][p], d = S[3][p],
+               f = S[4][p], x = S[5][p], cai = S[6][p];
+        /* calc_ina */
+        double alpha_h = 0, beta_h = 0, beta_J = 0, alpha_J = 0;
+        if (uu >= -40.) {
+            beta_h = 1. / (0.13 * (1 + exp((uu + 10.66) / -11.1)));
+            beta_J = 0.3 * exp(-2.535 * 1e-07 * uu) / (1 + exp(-0.1 * (uu + 32)));
+        } else {
+            alpha_h = 0.135 * exp((80 + uu) / -6.8);
+            beta_h = 3.56 * exp(0.079 * uu) + 3.1 * 1e5 * exp(0.35 * uu);
+            beta_J = 0.1212 * exp(-0.01052 * uu) / (1 + exp(-0.1378 * (uu + 40.14)));
+            alpha_J = (-1.2714 * 1e5 * exp(0.2444 * uu) -
+                       3.474 * 1e-5 * exp(-0.04391 * uu)) *
+                      (uu + 37.78) / (1 + exp(0.311 * (uu + 79.23)));
+        }
+        const double alpha_m = 0.32 * (uu + 47.13) / (1 - exp(-0.1 * (uu + 47.13)));
+        const double beta_m = 0.08 * exp(-uu / 11);
+        m = lr_gate(m, dt, alpha_m, beta_m);
+        h = lr_gate(h, dt, alpha_h, beta_h);
+        j = lr_gate(j, dt, alpha_J, beta_J);
+        const double ina = gna * m * m * m * h * j * (uu - E_Na);
+        /* calc_isk */
+        const double E_Si = 7.7 - 13.0287 * log(cai);
+        const double isi = gsi * d * f * (uu - E_Si);
+        const double alpha_d = 0.095 * exp(-0.01 * (uu - 5)) / (1 + exp(-0.072 * (uu - 5)));
+        const double beta_d = 0.07 * exp(-0.017 * (uu + 44)) / (1 + exp(0.05 * (uu + 44)));
+        const double alpha_f = 0.012 * exp(-0.008 * (uu + 28)) / (1 + exp(0.15 * (uu + 28)));
+        const double beta_f = 0.0065 * exp(-0.02 * (uu + 30)) / (1 + exp(-0.2 * (uu + 30)));
+        d = lr_gate(d, dt, alpha_d, beta_d);
+        f = lr_gate(f, dt, alpha_f, beta_f);
+        cai += dt * (-0.0001 * isi + 0.07 * (0.0001 - cai));
+        /* calc_ik */
+        const double E_K = (R * T / F) * log((ko + PR_NaK * nao) / (ki + PR_NaK * nai));
+        const double G_K = gk * sqrt(ko / 5.4);
+        double Xi;
+        if (uu > -100)
+            Xi = 2.837 * (exp(0.04 * (uu + 77)) - 1) /
+                 ((uu + 77) * exp(0.04 * (uu + 35)));
+        else
+            Xi = 1;
+        const double ik = G_K * x * Xi * (uu - E_K);
+        const double alpha_x = 0.0005 * exp(0.083 * (uu + 50)) / (1 + exp(0.057 * (uu + 50)));
+        const double beta_x = 0.0013 * exp(-0.06 * (uu + 20)) / (1 + exp(-0.04 * (uu + 20)));
+        x = lr_gate(x, dt, alpha_x, beta_x);
+        const double E_K1 = (R * T / F) * log(ko / ki);
+        /* calc_ik1, calc_ikp, calc_ib */
+        const double alpha_K1 = 1.02 / (1 + exp(0.2385 * (uu - E_K1 - 59.215)));
+        const double beta_K1 = (0.49124 * exp(0.08032 * (uu - E_K1 + 5.476)) +
+                                exp(0.06175 * (uu - E_K1 - 594.31))) /
+                               (1 + exp(-0.5143 * (uu - E_K1 + 4.753)));
+        const double K_1x = alpha_K1 / (alpha_K1 + beta_K1);
+        const double G_K1 = gk1 * sqrt(ko / 5.4);
+        const double ik1 = G_K1 * K_1x * (uu - E_K1);
+        const double K_p = 1. / (1 + exp((7.488 - uu) / 5.98));
+        const double ikp = gkp * K_p * (uu - E_K1);
+        const double ib = gb * (uu + 59.87);
+        const double ik1t = ik1 + ikp + ib;
+        un[p] -= dt * (ina + isi + ik1t + ik);
+        S[0][p] = m;
+        S[1][p] = h;
+        S[2][p] = j;
+        S[3][p] = d;
+        S[4][p] = f;
+        S[5][p] = x;
+        S[6][p] = cai;
+    }
+}

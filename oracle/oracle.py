@@ -85,7 +85,8 @@ def lib():
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = ctypes.c_int if name == "fwo_set_threads" else None
-        for extra in ("fwo_ionic_tp06", "fwo_ionic_crn"):
+        for extra in ("fwo_ionic_tp06", "fwo_ionic_crn", "fwo_ionic_bk",
+                      "fwo_ionic_bo", "fwo_ionic_lr91"):
             if hasattr(L, extra):
                 getattr(L, extra).restype = None
         _lib = L
@@ -485,3 +486,36 @@ register_model("crn", dict(params=CRN_PARAMS,
                            init={k: CRN_INIT[k] for k in ["u"] + CRN_STATE},
                            D_model=0.154, reset_u_new=True,
                            ionic=_detailed_ionic("fwo_ionic_crn", CRN_STATE)))
+
+
+# Barkley, Bueno-Orovio, Luo-Rudy 1991 (barkley_2d.py:56-75,
+# bueno_orovio_2d.py:93-137, luo_rudy91_2d.py:59-103; parameters in the
+# order of their ionic_kernel_2d signatures)
+BK_PARAMS = dict(a=0.75, b=0.02, eap=0.02)
+BO_PARAMS = dict(
+    u_o=0.0, u_u=1.55, theta_v=0.3, theta_w=0.13, theta_v_m=0.006,
+    theta_o=0.006, tau_v1_m=60, tau_v2_m=1150, tau_v_p=1.4506, tau_w1_m=60,
+    tau_w2_m=15, k_w_m=65, u_w_m=0.03, tau_w_p=200, tau_fi=0.11, tau_o1=400,
+    tau_o2=6, tau_so1=30.0181, tau_so2=0.9957, k_so=2.0458, u_so=0.65,
+    tau_s1=2.7342, tau_s2=16, k_s=2.0994, u_s=0.9087, tau_si=1.8875,
+    tau_w_inf=0.07, w_inf_=0.94)
+LR91_PARAMS = dict(
+    gna=23.0, gsi=0.09, gk=0.282, gk1=0.6047, gkp=0.0183, gb=0.03921,
+    ko=5.4, ki=145.0, nai=18.0, nao=140.0, cao=1.8, R=8.314, T=310.0,
+    F=96.5, PR_NaK=0.01833)
+LR91_STATE = ["m", "h", "j", "d", "f", "x", "cai"]
+register_model("bk", dict(params=BK_PARAMS, init=dict(u=0.0, v=0.0),
+                          D_model=1.0, reset_u_new=False,
+                          ionic=_detailed_ionic("fwo_ionic_bk", ["v"])))
+register_model("bo", dict(params=BO_PARAMS,
+                          init=dict(u=0.0, v=1.0, w=1.0, s=0.0),
+                          D_model=1.0, reset_u_new=False,
+                          ionic=_detailed_ionic("fwo_ionic_bo",
+                                                ["v", "w", "s"])))
+register_model("lr91", dict(params=LR91_PARAMS,
+                            init=dict(u=-84.5, m=0.0017, h=0.9832,
+                                      j=0.995484, d=0.000003, f=1.0,
+                                      x=0.0057, cai=0.0002),
+                            D_model=0.1, reset_u_new=True,
+                            ionic=_detailed_ionic("fwo_ionic_lr91",
+                                                  LR91_STATE)))

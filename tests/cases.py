@@ -220,3 +220,37 @@ def tips(dim):
     periods = np.split(flat, np.cumsum(lens)[:-1]) if len(lens) else []
     return case, {"tips": g[f"d{dim}_tips"], "u": g[f"d{dim}_u"],
                   "cells": cells, "periods": periods}
+
+
+EXTRA_VARS = {"bk": ["u", "v"], "bo": ["u", "v", "w", "s"],
+              "lr91": ["u", "m", "h", "j", "d", "f", "x", "cai"]}
+MODEL_VARS.update(EXTRA_VARS)
+
+
+def models_extra(name, dim):
+    """Barkley ('bk'), Bueno-Orovio ('bo') or Luo-Rudy 1991 ('lr91') on the
+    20^2 anisotropic fibrotic sheet (2D) or the 8 x 8 x 6 block (3D)."""
+    g = load("models_extra")
+    cv, cd, t_max, thr, var = {"bk": (5, 0.1, 12, 0.5, "v"),
+                               "bo": (5, 0.5, 30, 0.5, "v"),
+                               "lr91": (100, 1.0, 20, -20.0, "m")}[name]
+    if dim == 2:
+        case = dict(model=name, mesh=g["mesh2"], fibers=g["fib2"],
+                    stencil="aniso9", dt=0.01, dr=0.25, t_max=t_max,
+                    stims=[dict(kind="current", t=0, value=cv, duration=cd,
+                                box=[(0, 20), (0, 4)])],
+                    trackers=[dict(kind="at", threshold=thr),
+                              dict(kind="probe", cells=[[10, 11]],
+                                   vars=["u", var], step=5)])
+    else:
+        case = dict(model=name, mesh=g["mesh3"], stencil="iso7", dt=0.01,
+                    dr=0.25, t_max=t_max,
+                    stims=[dict(kind="current", t=0, value=cv, duration=cd,
+                                box=[(0, 8), (0, 3), (0, 6)])],
+                    trackers=[dict(kind="at", threshold=thr),
+                              dict(kind="probe", cells=[[4, 5, 3]],
+                                   vars=["u", var], step=5)])
+    gold = {v: g[f"{name}{dim}_{v}"] for v in EXTRA_VARS[name]}
+    gold["act_t"] = g[f"{name}{dim}_act_t"]
+    gold.update({f"mv_{v}": g[f"{name}{dim}_mv_{v}"] for v in ["u", var]})
+    return case, gold

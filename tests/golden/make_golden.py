@@ -593,6 +593,55 @@ def case_tips(fw):
     return out
 
 
+def case_models_extra(fw):
+    """Barkley, Bueno-Orovio and Luo-Rudy 1991 on small 2D (anisotropic,
+    fibrotic) and 3D (isotropic) tissues, current S1, an activation tracker
+    and probes of u and the first state variable."""
+    out = {}
+    rng = np.random.default_rng(1111)
+    mesh2 = _fibrosis(rng, (20, 20), 0.1)
+    fib2 = _seeded_fibers_2d(rng, (20, 20))
+    mesh3 = _fibrosis(rng, (8, 8, 6), 0.1)
+    spec = {"bk": (fw.Barkley2D, fw.Barkley3D, 5, 0.1, 12, 0.5, "v"),
+            "bo": (fw.BuenoOrovio2D, fw.BuenoOrovio3D, 5, 0.5, 30, 0.5, "v"),
+            "lr91": (fw.LuoRudy912D, fw.LuoRudy913D, 100, 1.0, 20, -20.0,
+                     "m")}
+    for name, (c2, c3, cv, cd, t_max, thr, var) in spec.items():
+        for dim in (2, 3):
+            ss = fw.StimSequence()
+            if dim == 2:
+                tissue = fw.CardiacTissue2D((20, 20))
+                tissue.mesh = mesh2.copy()
+                tissue.fibers = fib2
+                model = c2()
+                ss.add_stim(fw.StimCurrentCoord2D(0, cv, cd, 0, 20, 0, 4))
+                at, mv = fw.ActivationTime2DTracker(), fw.MultiVariable2DTracker()
+                mv.cell_ind = [[10, 11]]
+            else:
+                tissue = fw.CardiacTissue3D((8, 8, 6))
+                tissue.mesh = mesh3.copy()
+                model = c3()
+                ss.add_stim(fw.StimCurrentCoord3D(0, cv, cd, 0, 8, 0, 3, 0, 6))
+                at, mv = fw.ActivationTime3DTracker(), fw.MultiVariable3DTracker()
+                mv.cell_ind = [[4, 5, 3]]
+            model.dt, model.dr, model.t_max = 0.01, 0.25, t_max
+            model.prog_bar = False
+            model.cardiac_tissue = tissue
+            model.stim_sequence = ss
+            at.threshold = thr
+            mv.var_list = ["u", var]
+            mv.step = 5
+            _attach(fw, model, [at, mv])
+            model.run()
+            for v in model.state_vars:
+                out[f"{name}{dim}_{v}"] = getattr(model, v)
+            out[f"{name}{dim}_act_t"] = at.output
+            for v in mv.var_list:
+                out[f"{name}{dim}_mv_{v}"] = mv.output[v]
+    out["mesh2"], out["fib2"], out["mesh3"] = mesh2, fib2, mesh3
+    return out
+
+
 CASES = {
     "weights_2d": case_weights_2d,
     "weights_3d": case_weights_3d,
@@ -607,6 +656,7 @@ CASES = {
     "fibrosis": case_fibrosis,
     "ecg": case_ecg,
     "tips": case_tips,
+    "models_extra": case_models_extra,
 }
 
 

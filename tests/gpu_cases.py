@@ -7,7 +7,10 @@ _MODELS = {("ap", 2): fg.AlievPanfilov2D, ("ap", 3): fg.AlievPanfilov3D,
            ("ms", 2): fg.MitchellSchaeffer2D, ("ms", 3): fg.MitchellSchaeffer3D,
            ("fk", 2): fg.FentonKarma2D, ("fk", 3): fg.FentonKarma3D,
            ("tp06", 2): fg.TP062D, ("tp06", 3): fg.TP063D,
-           ("crn", 2): fg.Courtemanche2D, ("crn", 3): fg.Courtemanche3D}
+           ("crn", 2): fg.Courtemanche2D, ("crn", 3): fg.Courtemanche3D,
+           ("bk", 2): fg.Barkley2D, ("bk", 3): fg.Barkley3D,
+           ("bo", 2): fg.BuenoOrovio2D, ("bo", 3): fg.BuenoOrovio3D,
+           ("lr91", 2): fg.LuoRudy912D, ("lr91", 3): fg.LuoRudy913D}
 
 
 def register(name, cls2d, cls3d):

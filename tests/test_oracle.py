@@ -175,3 +175,19 @@ def test_spiral_tips_and_periods_bitwise(oracle, dim):
     for got, want in zip(_periods_from_layers(r["trackers"][1], g["cells"]),
                          g["periods"]):
         assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("name", ["bk", "bo", "lr91"])
+def test_models_extra(oracle, name, dim):
+    """Barkley (+ - * / only: bitwise), Bueno-Orovio (tanh) and Luo-Rudy
+    1991 (exp / log / sqrt) against the reference."""
+    case, g = cases.models_extra(name, dim)
+    r = oracle.run(case)
+    at, mv = r["trackers"]
+    tol = 0.0 if name == "bk" else DETAILED_RTOL
+    for v in cases.EXTRA_VARS[name]:
+        assert _rel_err(r[v], g[v]) <= tol, v
+    for v, x in mv.items():
+        assert _rel_err(x, g["mv_" + v]) <= tol, v
+    assert np.array_equal(at, g["act_t"])
