@@ -20,7 +20,8 @@ from .model import (AlievPanfilov2D, AlievPanfilov3D, Barkley2D, Barkley3D,
 from .serving import Request, SimulationServer, device_footprint
 from .state import StateLoader, StateSaver, StateSaverCollection
 from .stencil import (AsymmetricStencil2D, AsymmetricStencil3D,
-                      IsotropicStencil2D, IsotropicStencil3D, Stencil)
+                      IsotropicStencil2D, IsotropicStencil3D, Stencil,
+                      SymmetricStencil2D)
 from .stimulation import (Stim, StimCurrent, StimCurrentArea2D,
                           StimCurrentArea3D, StimCurrentCoord2D,
                           StimCurrentCoord3D, StimCurrentMatrix2D,

@@ -25,7 +25,7 @@ FW_DEV_TIP_OVERFLOW = 16
 
 MODEL_AP, MODEL_MS, MODEL_FK, MODEL_TP06, MODEL_CRN = 1, 2, 3, 4, 5
 MODEL_BK, MODEL_BO, MODEL_LR91 = 6, 7, 8
-ISO5, ANISO9, ISO7, ANISO19 = 1, 2, 3, 4
+ISO5, ANISO9, ISO7, ANISO19, SYM9 = 1, 2, 3, 4, 5
 F64, F32 = 0, 1
 FORM_PLAIN, FORM_FUSED = 0, 1
 STIM_VOLTAGE, STIM_CURRENT = 0, 1
@@ -41,7 +41,7 @@ MAX_ECG = 2
 MAX_TIP = 1
 MAX_ECG_LEADS = 8
 
-STENCIL_NW = {ISO5: 5, ANISO9: 9, ISO7: 7, ANISO19: 19}
+STENCIL_NW = {ISO5: 5, ANISO9: 9, ISO7: 7, ANISO19: 19, SYM9: 9}
 
 _i32, _i64, _f64, _vp = (ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
                          ctypes.c_void_p)

@@ -35,13 +35,15 @@ inline int stencil_nw(int st)
     case FW_STENCIL_ANISO9: return 9;
     case FW_STENCIL_ISO7: return 7;
     case FW_STENCIL_ANISO19: return 19;
+    case FW_STENCIL_SYM9: return 9;
     }
     return 0;
 }
 
 inline int stencil_dim(int st)
 {
-    return (st == FW_STENCIL_ISO5 || st == FW_STENCIL_ANISO9) ? 2 : 3;
+    return (st == FW_STENCIL_ISO5 || st == FW_STENCIL_ANISO9 ||
+            st == FW_STENCIL_SYM9) ? 2 : 3;
 }
 
 // Grid strides of the axes i and j (k has stride 1).  In 2D the reference's

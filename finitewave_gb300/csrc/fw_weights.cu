@@ -209,6 +209,89 @@ __global__ void k_aniso9(WArgs a, T *w)
     }
 }
 
+// SymmetricStencil2D (symmetric_stencil_2d.py:31-250): the diffusion tensor
+// D * conductivity averaged to the cell corners,
+//   0.25 * (D[i,j] + D[i+1,j] + D[i,j+1] + D[i+1,j+1])  (np.roll wrap),
+// and the flux through each of the node's four corner cells distributed to
+// the cell's four nodes (compute_components), accumulated in the
+// reference's corner order.
+__device__ __forceinline__ double dcorner(const WArgs &a, int64_t q, int c0,
+                                          int c1)
+{
+    const int64_t qi = roll_next(a, q, 0), qj = roll_next(a, q, 1);
+    const int64_t qij = roll_next(a, qi, 1);
+    return 0.25 * (dcomp(a, q, c0, c1) * cond_at(a, q) +
+                   dcomp(a, qi, c0, c1) * cond_at(a, qi) +
+                   dcomp(a, qj, c0, c1) * cond_at(a, qj) +
+                   dcomp(a, qij, c0, c1) * cond_at(a, qij));
+}
+
+// compute_components (symmetric_stencil_2d.py:96-140)
+__device__ __forceinline__ void sym_corner(const WArgs &a, int64_t q, int m0,
+                                           int m1, int m2, int m3, int qx,
+                                           int qy, double r[4])
+{
+    if (m0 + m1 + m2 + m3 < 3) {
+        r[0] = r[1] = r[2] = r[3] = 0.0;
+        return;
+    }
+    const double dxx = dcorner(a, q, 0, 0), dxy = dcorner(a, q, 0, 1),
+                 dyx = dcorner(a, q, 1, 0), dyy = dcorner(a, q, 1, 1);
+    const double qdx = (double)qx * dxx + (double)qy * dyx;
+    const double qdy = (double)qx * dxy + (double)qy * dyy;
+    const double d0 = m0, d1 = m1, d2 = m2, d3 = m3;
+    const double w0 = (-d0) / (d0 + d1) * qdx - d0 / (d0 + d2) * qdy;
+    const double w1 = (-d1) / (d0 + d1) * qdx + d1 / (d1 + d3) * qdy;
+    const double w2 = d2 / (d2 + d3) * qdx - d2 / (d0 + d2) * qdy;
+    const double w3 = d3 / (d2 + d3) * qdx + d3 / (d1 + d3) * qdy;
+    r[0] = 0.5 * w0;
+    r[1] = 0.5 * w1;
+    r[2] = 0.5 * w2;
+    r[3] = 0.5 * w3;
+}
+
+template <class T>
+__global__ void k_sym9(WArgs a, T *w)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        double o[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (m01(a, p) && !on_ring(a, p)) {
+            const int64_t si = a.nj;
+#define M(di, dj) m01(a, p + (di) * si + (dj))
+#define Q(di, dj) (p + (di) * si + (dj))
+            double r[4];
+            // corner (i-1, j-1): nodes (i-1,j-1), (i-1,j), (i,j-1), (i,j)
+            sym_corner(a, Q(-1, -1), M(-1, -1), M(-1, 0), M(0, -1), M(0, 0),
+                       -1, -1, r);
+            o[0] += r[0]; o[1] += r[1]; o[3] += r[2]; o[4] += r[3];
+            // corner (i-1, j)
+            sym_corner(a, Q(-1, 0), M(-1, 0), M(-1, 1), M(0, 0), M(0, 1), -1,
+                       1, r);
+            o[1] += r[0]; o[2] += r[1]; o[4] += r[2]; o[5] += r[3];
+            // corner (i, j-1)
+            sym_corner(a, Q(0, -1), M(0, -1), M(0, 0), M(1, -1), M(1, 0), 1,
+                       -1, r);
+            o[3] += r[0]; o[4] += r[1]; o[6] += r[2]; o[7] += r[3];
+            // corner (i, j)
+            sym_corner(a, Q(0, 0), M(0, 0), M(0, 1), M(1, 0), M(1, 1), 1, 1,
+                       r);
+            o[4] += r[0]; o[5] += r[1]; o[7] += r[2]; o[8] += r[3];
+#undef M
+#undef Q
+        }
+        // weights *= D_model * dt / dr**2: the factor first
+        // (symmetric_stencil_2d.py:64), unlike the other stencils
+        const double scale = a.D_model * a.dt / a.dr2;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            double x = o[k] * scale;
+            if (k == 4) x += 1.0;
+            w[k * a.n + p] = (T)x;
+        }
+    }
+}
+
 // AsymmetricStencil3D.compute_weights + its serial njit accumulation
 // (asymmetric_stencil_3d.py:61-105, 164-458): six faces, each a major flux
 // and two six-point minor fluxes.
@@ -309,6 +392,7 @@ void launch(int32_t stencil, const WArgs &a, void *w, cudaStream_t s)
     case FW_STENCIL_ANISO9: k_aniso9<T><<<blocks, threads, 0, s>>>(a, wt); break;
     case FW_STENCIL_ISO7: k_iso7<T><<<blocks, threads, 0, s>>>(a, wt); break;
     case FW_STENCIL_ANISO19: k_aniso19<T><<<blocks, threads, 0, s>>>(a, wt); break;
+    case FW_STENCIL_SYM9: k_sym9<T><<<blocks, threads, 0, s>>>(a, wt); break;
     }
 }
 
@@ -326,7 +410,8 @@ int build_weights(int32_t stencil, int32_t precision, const int8_t *mesh,
         return FW_ERR_ARG;
     }
     int dim = stencil_dim(stencil);
-    bool aniso = stencil == FW_STENCIL_ANISO9 || stencil == FW_STENCIL_ANISO19;
+    bool aniso = stencil == FW_STENCIL_ANISO9 || stencil == FW_STENCIL_ANISO19 ||
+                 stencil == FW_STENCIL_SYM9;
     if (!mesh || !w_out || (aniso && !fibers) || ni < 1 || nj < 1 ||
         (dim == 3 && nk < 1)) {
         set_error("fw_build_weights: null pointer or empty grid");

@@ -30,6 +30,7 @@ class Stencil:
     """Base class (core/stencil/stencil.py:4-46)."""
 
     kind = None  # one of _ffi.ISO5 / ANISO9 / ISO7 / ANISO19
+    build_kind = None  # weight builder, when it differs from `kind`
 
     def compute_weights(self, model, cardiac_tissue):
         raise NotImplementedError
@@ -65,7 +66,8 @@ class Stencil:
         dtype = torch.float64 if prec == _ffi.F64 else torch.float32
         w = torch.empty((nw, *shape), dtype=dtype, device=device)
         nk = shape[2] if dim == 3 else 1
-        _ffi.call("fw_build_weights", self.kind, prec, mesh_d.data_ptr(),
+        _ffi.call("fw_build_weights", self.build_kind or self.kind, prec,
+                  mesh_d.data_ptr(),
                   cond_d.data_ptr() if cond_d is not None else None,
                   cond_scalar, fib_d.data_ptr() if fib_d is not None else None,
                   float(D_al), float(D_ac), float(model.D_model),
@@ -130,6 +132,17 @@ class AsymmetricStencil2D(Stencil):
                              "diffusion.")
         return self._build(model, cardiac_tissue, cardiac_tissue.fibers,
                            self.D_al, self.D_ac)
+
+
+class SymmetricStencil2D(AsymmetricStencil2D):
+    """9-point symmetric anisotropic stencil (cpuwave2D/stencil/
+    symmetric_stencil_2d.py:7-250): the diffusion tensor averaged to the
+    cell corners and the flux of each corner cell split over its four
+    nodes.  Same weight layout and diffusion kernel as AsymmetricStencil2D;
+    only the weight construction differs (fw_build_weights with
+    FW_STENCIL_SYM9)."""
+
+    build_kind = _ffi.SYM9
 
 
 class IsotropicStencil3D(Stencil):

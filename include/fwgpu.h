@@ -67,7 +67,9 @@ enum fw_stencil {
     FW_STENCIL_ISO5 = 1,    /* IsotropicStencil2D   (i-1,j),(i,j-1),(i,j),(i,j+1),(i+1,j) */
     FW_STENCIL_ANISO9 = 2,  /* AsymmetricStencil2D  (i-1,j-1)...(i+1,j+1)                 */
     FW_STENCIL_ISO7 = 3,    /* IsotropicStencil3D   order of isotropic_stencil_3d.py:16-23  */
-    FW_STENCIL_ANISO19 = 4  /* AsymmetricStencil3D  order of asymmetric_stencil_3d.py:25-44 */
+    FW_STENCIL_ANISO19 = 4, /* AsymmetricStencil3D  order of asymmetric_stencil_3d.py:25-44 */
+    FW_STENCIL_SYM9 = 5     /* SymmetricStencil2D weights (fw_build_weights only): the
+                               9-point layout of ANISO9, stepped as ANISO9      */
 };
 
 /* Arithmetic policy.  FW_F64: every array float64 (the reference's default

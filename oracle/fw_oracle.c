@@ -546,3 +546,78 @@ EXPORT void fwo_ecg(const double *u_tr, const double *u, const double *coords,
         out[c] = acc;
     }
 }
+
+/* SymmetricStencil2D.compute_weights (cpuwave2D/stencil/symmetric_stencil_2d.
+ * py:31-250): D * conductivity averaged to the cell corners with np.roll
+ * wrap, compute_components per corner cell, accumulated in the reference's
+ * corner order, then weights *= (D_model * dt / dr**2) and +1 on w[4]. */
+static void sym_corner(double dxx, double dxy, double dyx, double dyy, int m0,
+                       int m1, int m2, int m3, int qx, int qy, double r[4])
+{
+    if (m0 + m1 + m2 + m3 < 3) {
+        r[0] = r[1] = r[2] = r[3] = 0.0;
+        return;
+    }
+    const double qdx = qx * dxx + qy * dyx;
+    const double qdy = qx * dxy + qy * dyy;
+    const double d0 = m0, d1 = m1, d2 = m2, d3 = m3;
+    r[0] = 0.5 * ((-d0) / (d0 + d1) * qdx - d0 / (d0 + d2) * qdy);
+    r[1] = 0.5 * ((-d1) / (d0 + d1) * qdx + d1 / (d1 + d3) * qdy);
+    r[2] = 0.5 * (d2 / (d2 + d3) * qdx - d2 / (d0 + d2) * qdy);
+    r[3] = 0.5 * (d3 / (d2 + d3) * qdx + d3 / (d1 + d3) * qdy);
+}
+
+EXPORT void fwo_weights_2d_sym9(const int8_t *mesh, const double *cond,
+                                const double *fibers, int64_t ni, int64_t nj,
+                                double D_al, double D_ac, double D_model,
+                                double dt, double dr2, double *w)
+{
+    const int64_t n = ni * nj;
+    const int64_t shape[2] = {ni, nj};
+    double *D[4];
+    for (int c = 0; c < 4; ++c) {
+        D[c] = (double *)malloc(sizeof(double) * n);
+        double *Dn = (double *)malloc(sizeof(double) * n);
+        const int c0 = c / 2, c1 = c % 2;
+        for (int64_t p = 0; p < n; ++p)
+            Dn[p] = dcomp(fibers, p, 2, c0, c1, D_al, D_ac) * cond[p];
+        for (int64_t i = 0; i < ni; ++i)
+            for (int64_t j = 0; j < nj; ++j) {
+                const int64_t i1 = (i + 1) % ni, j1 = (j + 1) % nj;
+                D[c][i * nj + j] = 0.25 * (Dn[i * nj + j] + Dn[i1 * nj + j] +
+                                           Dn[i * nj + j1] + Dn[i1 * nj + j1]);
+            }
+        free(Dn);
+    }
+    (void)shape;
+#define M(i, j) (mesh[(i) * nj + (j)] == 1)
+    for (int64_t p = 0; p < n * 9; ++p) w[p] = 0.0;
+    const double scale = D_model * dt / dr2;
+    for (int64_t i = 1; i + 1 < ni; ++i)
+        for (int64_t j = 1; j + 1 < nj; ++j) {
+            if (!M(i, j)) continue;
+            double *o = w + (i * nj + j) * 9, r[4];
+            int64_t q = (i - 1) * nj + (j - 1);
+            sym_corner(D[0][q], D[1][q], D[2][q], D[3][q], M(i - 1, j - 1),
+                       M(i - 1, j), M(i, j - 1), M(i, j), -1, -1, r);
+            o[0] += r[0]; o[1] += r[1]; o[3] += r[2]; o[4] += r[3];
+            q = (i - 1) * nj + j;
+            sym_corner(D[0][q], D[1][q], D[2][q], D[3][q], M(i - 1, j),
+                       M(i - 1, j + 1), M(i, j), M(i, j + 1), -1, 1, r);
+            o[1] += r[0]; o[2] += r[1]; o[4] += r[2]; o[5] += r[3];
+            q = i * nj + (j - 1);
+            sym_corner(D[0][q], D[1][q], D[2][q], D[3][q], M(i, j - 1),
+                       M(i, j), M(i + 1, j - 1), M(i + 1, j), 1, -1, r);
+            o[3] += r[0]; o[4] += r[1]; o[6] += r[2]; o[7] += r[3];
+            q = i * nj + j;
+            sym_corner(D[0][q], D[1][q], D[2][q], D[3][q], M(i, j),
+                       M(i, j + 1), M(i + 1, j), M(i + 1, j + 1), 1, 1, r);
+            o[4] += r[0]; o[5] += r[1]; o[7] += r[2]; o[8] += r[3];
+        }
+#undef M
+    for (int64_t p = 0; p < n; ++p) {
+        for (int k = 0; k < 9; ++k) w[p * 9 + k] *= scale;
+        w[p * 9 + 4] += 1.0;
+    }
+    for (int c = 0; c < 4; ++c) free(D[c]);
+}

@@ -71,6 +71,8 @@ def lib():
                                       _P],
             "fwo_weights_3d_aniso19": [_P, _P, _P, _I, _I, _I, _D, _D, _D, _D,
                                        _D, _P],
+            "fwo_weights_2d_sym9": [_P, _P, _P, _I, _I, _D, _D, _D, _D, _D,
+                                    _P],
             "fwo_diffuse_2d_iso5": [_P, _P, _P, _P, _I, _I, _I],
             "fwo_diffuse_2d_aniso9": [_P, _P, _P, _P, _I, _I, _I],
             "fwo_diffuse_3d_iso7": [_P, _P, _P, _P, _I, _I, _I, _I],
@@ -107,7 +109,8 @@ def weights(kind, mesh, D_model, dt, dr, conductivity=1.0, fibers=None,
             D_al=1.0, D_ac=1.0 / 9):
     """Stencil weights in the reference layout (*mesh.shape, nw), float64.
 
-    kind: 'iso5' | 'aniso9' | 'iso7' | 'aniso19'.
+    kind: 'iso5' | 'aniso9' | 'iso7' | 'aniso19' | 'sym9' (SymmetricStencil2D,
+    stepped with the 9-point diffusion).
     """
     mesh = np.ascontiguousarray(mesh, dtype=np.int8)
     cond = np.ascontiguousarray(conductivity * np.ones(mesh.shape))
@@ -130,6 +133,11 @@ def weights(kind, mesh, D_model, dt, dr, conductivity=1.0, fibers=None,
         w = np.zeros((*mesh.shape, 19))
         L.fwo_weights_3d_aniso19(_p(mesh), _p(cond), _p(f), *mesh.shape,
                                  D_al, D_ac, D_model, dt, dr ** 2, _p(w))
+    elif kind == "sym9":
+        f = np.ascontiguousarray(fibers, dtype=np.float64)
+        w = np.zeros((*mesh.shape, 9))
+        L.fwo_weights_2d_sym9(_p(mesh), _p(cond), _p(f), *mesh.shape,
+                              D_al, D_ac, D_model, dt, dr ** 2, _p(w))
     else:
         raise ValueError(kind)
     return w
@@ -289,8 +297,9 @@ def run(case):
     mesh = np.ascontiguousarray(case["mesh"], dtype=np.int8)
     dt, dr, t_max = case["dt"], case["dr"], case["t_max"]
     D_model = case.get("D_model", spec["D_model"])
-    kind = case["stencil"]
-    w = weights(kind, mesh, D_model, dt, dr, case.get("conductivity", 1.0),
+    wkind = case["stencil"]
+    kind = "aniso9" if wkind == "sym9" else wkind
+    w = weights(wkind, mesh, D_model, dt, dr, case.get("conductivity", 1.0),
                 case.get("fibers"), case.get("D_al", 1.0),
                 case.get("D_ac", 1.0 / 9))
     special = case.get("special")

@@ -134,6 +134,12 @@ def case_weights_2d(fw):
     st.D_al, st.D_ac = 1.0, 0.111
     out["w_aniso9_c1_dac0111"] = st.compute_weights(model, tissue)
     out["D_al_b"], out["D_ac_b"] = 1.0, 0.111
+    # SymmetricStencil2D (symmetric_stencil_2d.py:31-250)
+    st_sym = fw.SymmetricStencil2D()
+    st_sym.D_al, st_sym.D_ac = 1.0, 0.111
+    out["w_sym9_c1_dac0111"] = st_sym.compute_weights(model, tissue)
+    tissue.conductivity = cond
+    out["w_sym9_carr"] = fw.SymmetricStencil2D().compute_weights(model, tissue)
     return out
 
 

@@ -24,7 +24,7 @@ def build(case, npfloat="float64", form=None, fused_k=0, fused_variant=0):
     tissue = fg.CardiacTissue2D(mesh.shape) if dim == 2 \
         else fg.CardiacTissue3D(mesh.shape)
     tissue.mesh = mesh.astype(np.int8).copy()
-    if case["stencil"] in ("aniso9", "aniso19"):
+    if case["stencil"] in ("aniso9", "aniso19", "sym9"):
         tissue.fibers = case["fibers"]
     tissue.conductivity = case.get("conductivity", 1.0)
     model = _MODELS[(case["model"], dim)]()
@@ -38,7 +38,9 @@ def build(case, npfloat="float64", form=None, fused_k=0, fused_variant=0):
         setattr(model, k, v)
     if "D_model" in case:
         model.D_model = case["D_model"]
-    if case["stencil"] == "aniso9":
+    if case["stencil"] == "sym9":
+        st = fg.SymmetricStencil2D()
+    elif case["stencil"] == "aniso9":
         st = fg.AsymmetricStencil2D()
     elif case["stencil"] == "aniso19":
         st = fg.AsymmetricStencil3D()

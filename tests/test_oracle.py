@@ -191,3 +191,16 @@ def test_models_extra(oracle, name, dim):
     for v, x in mv.items():
         assert _rel_err(x, g["mv_" + v]) <= tol, v
     assert np.array_equal(at, g["act_t"])
+
+
+def test_weights_sym9(oracle):
+    """SymmetricStencil2D weights (its own scaling order) bitwise."""
+    g = cases.load("weights_2d")
+    a = (float(g["D_model"]), float(g["dt"]), float(g["dr"]))
+    assert np.array_equal(
+        oracle.weights("sym9", g["mesh"], *a, g["cond"], g["fibers"]),
+        g["w_sym9_carr"])
+    assert np.array_equal(
+        oracle.weights("sym9", g["mesh"], *a, 1.0, g["fibers"],
+                       float(g["D_al_b"]), float(g["D_ac_b"])),
+        g["w_sym9_c1_dac0111"])
