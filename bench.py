@@ -558,16 +558,56 @@ def accuracy_tp06(fg, n=192, t_max=350.0):
     return build
 
 
+def accuracy_batched(fg, torch, n_tissues=16, steps=2000):
+    """Local activation times of the batched float32 form (TissueBatch, one
+    persistent launch over all tissues) against each tissue's float64 plain
+    run: the first n_tissues tissues of the batched configuration, `steps`
+    time steps of their S1-S2 protocol."""
+    from finitewave_gb300 import metrics
+    specs = batched_specs()[:n_tissues]
+    runs = {}
+    for prec in ("float32", "float64"):
+        models = [batched_tissue(fg, s, prec) for s in specs]
+        for m in models:
+            m.t_max = steps * m.dt
+        if prec == "float32":
+            fg.TissueBatch(models).run()
+        else:
+            for m in models:
+                m.form = "plain"
+                m.run()
+        torch.cuda.synchronize()
+        runs[prec] = [(m.tracker_sequence.sequence[0], m) for m in models]
+    good = total = worst = differ = 0
+    for (l32, m32), (l64, m64) in zip(runs["float32"], runs["float64"]):
+        myo = m64._myo_d.cpu().numpy().astype(bool).ravel()
+        c64 = l64._count.cpu().numpy()
+        w, wk, d = metrics.lat_error_steps(
+            l32._count.cpu().numpy(), l32._steps.cpu().numpy(), c64,
+            l64._steps.cpu().numpy(), myo)
+        n = int(c64[myo].sum())
+        good += w * n
+        total += n
+        worst = max(worst, wk)
+        differ += d
+    return {"tissues": len(specs), "time_steps": steps,
+            "lat_crossings": total,
+            "lat_within_1_step": good / total if total else 1.0,
+            "lat_max_err_steps": worst, "lat_nodes_count_differs": differ}
+
+
 def run_accuracy(args, fg, torch, reps):
-    """Float32 against float64 on two configurations: max |dV|, activation
+    """Float32 against float64 on three configurations: max |dV|, activation
     and local activation time errors in steps, APD90 error at 16 probes,
-    conduction-velocity error in percent."""
+    conduction-velocity error in percent; and the batched form's local
+    activation times against the float64 plain form."""
     return {"aliev_panfilov_2d_1024": dict(
                 units="normalised u; time in model units",
                 **_accuracy_pair(fg, accuracy_ap(fg), None)),
             "tp06_2d_192": dict(
                 units="mV; ms",
-                **_accuracy_pair(fg, accuracy_tp06(fg), None))}
+                **_accuracy_pair(fg, accuracy_tp06(fg), None)),
+            "batched_16_tissues": accuracy_batched(fg, torch)}
 
 
 def peaks():
