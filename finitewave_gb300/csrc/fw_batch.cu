@@ -23,6 +23,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -580,7 +581,19 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
             T.lat_count = L.cross_count;
         }
         T.status = a->status;
-        const int32_t nt = (int32_t)tissue_tiles(a);
+    }
+    // tile list grouped by (model, stencil): CTAs taking consecutive tiles
+    // then run the same specialisation of the tile code (one of six inlined
+    // copies) instead of switching between them from tile to tile
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const int kx = tissues[x]->model * 8 + tissues[x]->stencil;
+        const int ky = tissues[y]->model * 8 + tissues[y]->stencil;
+        return kx < ky;
+    });
+    for (int i : order) {
+        const int32_t nt = (int32_t)tissue_tiles(tissues[i]);
         for (int32_t k = 0; k < nt; ++k) tl[t_count + k] = BTile{i, k};
         t_count += nt;
     }
