@@ -26,13 +26,23 @@ _BATCH_MODELS = (_ffi.MODEL_AP, _ffi.MODEL_MS, _ffi.MODEL_FK)
 
 
 class TissueBatch:
-    """A batch of models run together (see the module docstring)."""
+    """A batch of models run together (see the module docstring).
 
-    def __init__(self, models=()):
+    chunk: advance the batch in chunks of at most this many steps (None: as
+    long as every model allows).  graphs: replay each chunk's launches from
+    a captured CUDA graph -- the launches of a chunk depend only on its
+    length and on the plan and scratch buffers (each chunk is planned at
+    offset 0 into the same plan buffer), so equal chunks replay one graph
+    and the per-launch host cost disappears."""
+
+    def __init__(self, models=(), chunk=None, graphs=True):
         self.models = list(models)
+        self.chunk = chunk
+        self.graphs = graphs
         self._plan = None
         self._scratch = None
         self._batch = None   # the last plan's fw_batch handle
+        self._graphs = {}
 
     def add(self, model):
         self.models.append(model)
@@ -70,8 +80,9 @@ class TissueBatch:
     def _buffers(self, plan_bytes, dev):
         if self._plan is None or self._plan.numel() < plan_bytes or \
                 self._plan.device != dev:
-            self._plan = torch.empty(max(plan_bytes, 1 << 16),
+            self._plan = torch.empty(max(2 * plan_bytes, 1 << 16),
                                      dtype=torch.uint8, device=dev)
+            self._graphs = {}     # captured against the old buffer
         if self._scratch is None or self._scratch.device != dev:
             nb = ctypes.c_int64()
             _ffi.call("fw_batch_scratch_size", ctypes.byref(nb))
@@ -79,6 +90,26 @@ class TissueBatch:
             self._scratch = torch.zeros(nb.value, dtype=torch.uint8,
                                         device=dev)
         return self._plan, self._scratch
+
+    def _launch(self, b, scratch, n, dev):
+        """fw_batch_run(b, scratch, 0, n), replayed from a CUDA graph when
+        the same launches were captured before."""
+        stream = torch.cuda.current_stream(dev)
+        if not self.graphs:
+            _ffi.call("fw_batch_run", ctypes.byref(b), scratch.data_ptr(), 0,
+                      n, stream.cuda_stream)
+            return
+        key = (n, b.plan, b.n_tissues, b.n_tiles, b.ksteps, b.grid,
+               scratch.data_ptr())
+        g = self._graphs.get(key)
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                _ffi.call("fw_batch_run", ctypes.byref(b),
+                          scratch.data_ptr(), 0, n,
+                          torch.cuda.current_stream().cuda_stream)
+            self._graphs[key] = g
+        g.replay()
 
     # ------------------------------------------------------------------ run
     def run(self, initialize=True):
@@ -103,6 +134,8 @@ class TissueBatch:
         stream = torch.cuda.current_stream(dev).cuda_stream
         while active:
             limit = min(_MAX_SEGMENT, min(remaining[i] for i in active))
+            if self.chunk:
+                limit = min(limit, int(self.chunk))
             n = min(ms[i]._segment_times(limit)[2] for i in active)
             segs = [ms[i]._prepare_segment(n) for i in active]
             k = len(segs)
@@ -115,8 +148,7 @@ class TissueBatch:
             b = _ffi.Batch()
             _ffi.call("fw_batch_plan", ptrs, k, n_begin, plan.data_ptr(),
                       plan.numel(), ctypes.byref(b), stream)
-            _ffi.call("fw_batch_run", ctypes.byref(b), scratch.data_ptr(),
-                      0, n, stream)
+            self._launch(b, scratch, n, dev)
             self._batch = b
             still = []
             for i, seg in zip(active, segs):

@@ -633,8 +633,14 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
         return FW_ERR_ARG;
     }
     if (n_steps == 0) return FW_OK;
-    FW_CUDA_CHECK(cudaFuncSetAttribute(
-        k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
+    // the plan set the shared-memory attribute on this device; set it again
+    // unless the stream is being captured into a CUDA graph (the launches
+    // alone are recorded then)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    FW_CUDA_CHECK(cudaStreamIsCapturing(stream, &cap));
+    if (cap == cudaStreamCaptureStatusNone)
+        FW_CUDA_CHECK(cudaFuncSetAttribute(
+            k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
     const BTissue *desc = reinterpret_cast<const BTissue *>(b->plan);
     const BTile *tl = reinterpret_cast<const BTile *>(
         (const unsigned char *)b->plan + align_up(sizeof(BTissue) * b->n_tissues, 256));

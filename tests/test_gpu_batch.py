@@ -107,3 +107,22 @@ def test_batch_rejects_unsupported(gc):
     m, _ = gc.build(case, npfloat="float64")
     with pytest.raises(ValueError, match="float32"):
         fg.TissueBatch([m]).run()
+
+
+def test_batch_graph_chunks_equal_direct(gc):
+    """Fixed chunks replayed from captured CUDA graphs give the same result
+    as direct launches (and as one long run)."""
+    import finitewave_gb300 as fg
+    cs = _batch_cases()[:4]
+    out = []
+    for chunk, graphs in ((None, False), (150, False), (150, True)):
+        built = [gc.build(c, npfloat="float32") for c in cs]
+        b = fg.TissueBatch([m for m, _ in built], chunk=chunk, graphs=graphs)
+        b.run()
+        torch.cuda.synchronize()
+        if graphs:
+            assert b._graphs, "no graph was captured"
+        out.append([_outputs(m, o) for m, o in built])
+    for i in range(len(cs)):
+        _same(out[1][i], out[0][i], f"chunked {i}")
+        _same(out[2][i], out[0][i], f"graphs {i}")
