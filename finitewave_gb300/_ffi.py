@@ -22,6 +22,7 @@ FW_DEV_PROBE_OVERFLOW = 2
 FW_DEV_BATCH_FAULT = 4
 FW_DEV_TIMEOUT = 8
 FW_DEV_TIP_OVERFLOW = 16
+FW_DEV_NONFINITE = 32
 
 MODEL_AP, MODEL_MS, MODEL_FK, MODEL_TP06, MODEL_CRN = 1, 2, 3, 4, 5
 MODEL_BK, MODEL_BO, MODEL_LR91 = 6, 7, 8

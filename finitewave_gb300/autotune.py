@@ -70,21 +70,24 @@ def key(model):
                      "%dD" % len(shape), "2^%d" % int(math.log2(max(n, 1)))])
 
 
-def _time_candidate(model, args, variant, k, steps, stream):
+def _time_candidate(model, args, variant, k, steps, stream, reps=3):
     args.fused_variant = variant
     args.fused_k = k
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    # one warm-up segment, then the timed one
+    # one warm-up segment, then the fastest of `reps` timed ones
     _ffi.call("fw_step", ctypes.byref(args), 0, steps, stream.cuda_stream)
-    e0.record(stream)
-    _ffi.call("fw_step", ctypes.byref(args), 0, steps, stream.cuda_stream)
-    e1.record(stream)
-    e1.synchronize()
-    return e0.elapsed_time(e1)
+    best = float("inf")
+    for _ in range(reps):
+        e0.record(stream)
+        _ffi.call("fw_step", ctypes.byref(args), 0, steps, stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return best
 
 
-def tune(model, steps=48):
+def tune(model, steps=96):
     """Time every fused candidate for `model` (initialised, fused form) on
     scratch copies of its arrays; returns {"variant": v, "k": k, "ms": {...}}.
     """

@@ -315,7 +315,9 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
         const int lr = r0 + r;
         const int64_t p = (int64_t)(oi + lr) * T.nj + gj;
         if ((myo_bits >> r) & 1u) {
-            u_out[p] = S.u[fb][lr + 1][col + 1];
+            const float uo = S.u[fb][lr + 1][col + 1];
+            u_out[p] = uo;
+            if (!isfinite(uo) && T.status) atomicOr(T.status, FW_DEV_NONFINITE);
             M::template store<float>(T.state, p, st[r]);
         }
         if (T.has_lat) T.lat_activated[p] = (lat_act >> r) & 1u;

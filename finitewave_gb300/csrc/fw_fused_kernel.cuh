@@ -461,7 +461,9 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
         const int lr = r0 + r;
         const int64_t p = (int64_t)(oi + lr) * k.nj + gj;
         if ((myo_bits >> r) & 1u) {
-            k.u_out[p] = S.u[fb][lr + 1][col + 1];
+            const float uo = S.u[fb][lr + 1][col + 1];
+            k.u_out[p] = uo;
+            if (!isfinite(uo) && k.status) atomicOr(k.status, FW_DEV_NONFINITE);
             M::template store<float>(k.state, p, st[r]);
         }
 #pragma unroll

@@ -425,7 +425,10 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             const int lr = r0 + r;
             const int64_t p = (int64_t)(oi + lr) * f.nj + gj;
             if ((myo_bits >> r) & 1u) {
-                f.u_out[p] = fin[lr + 1][col + xo];
+                const float uo = fin[lr + 1][col + xo];
+                f.u_out[p] = uo;
+                if (!isfinite(uo) && f.status)
+                    atomicOr(f.status, FW_DEV_NONFINITE);
                 M::template store<float>(f.state, p, st[r]);
             }
 #pragma unroll

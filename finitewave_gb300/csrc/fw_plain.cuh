@@ -151,6 +151,7 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<M, T>::value))
         un = M::template update<T>(uc, un, st, P, dt);
         M::template store<T>(k.state, p, st);
         k.un[p] = un;
+        if (!isfinite(un) && k.status) atomicOr(k.status, FW_DEV_NONFINITE);
     }
 }
 

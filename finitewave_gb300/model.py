@@ -16,6 +16,7 @@ uploads it, so state loaders, savers and commands work unchanged.
 """
 import copy
 import ctypes
+import warnings
 
 import numpy as np
 import torch
@@ -414,6 +415,12 @@ class CardiacModel:
 
     def _check_status(self):
         st = int(self._status.item())
+        if st & _ffi.FW_DEV_NONFINITE:
+            # the reference carries on with NaN silently; keep its results
+            # and say so
+            warnings.warn(f"{type(self).__name__}: the potential became inf "
+                          "or NaN (time step too large for the model?)",
+                          RuntimeWarning, stacklevel=3)
         if st & _ffi.FW_DEV_TIP_OVERFLOW:
             raise RuntimeError("SpiralWaveCore tracker: more tips than its "
                                "capacity in one run segment")

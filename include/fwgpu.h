@@ -50,6 +50,7 @@ extern "C" {
 #define FW_DEV_BATCH_FAULT 4    /* a batch tile descriptor out of range     */
 #define FW_DEV_TIMEOUT 8        /* a bounded on-chip wait gave up           */
 #define FW_DEV_TIP_OVERFLOW 16  /* more spiral tips than the tracker holds  */
+#define FW_DEV_NONFINITE 32     /* a myocyte's potential became inf or NaN  */
 
 /* ------------------------------------------------------------ enumerations */
 enum fw_model {

@@ -98,3 +98,18 @@ def test_resume_is_bitwise(fg, tmp_path, cls):
     second.run()
     for var in ref.state_vars:
         assert np.array_equal(getattr(second, var), getattr(ref, var)), var
+
+
+def test_nonfinite_potential_warns(fg):
+    """A diverging run (Barkley with a strong stimulus, as in the
+    reference, produces NaN) keeps the NaN results and warns."""
+    tissue = fg.CardiacTissue2D([12, 12])
+    model = fg.Barkley2D()
+    model.dt, model.dr, model.t_max = 0.01, 0.25, 12
+    model.cardiac_tissue = tissue
+    seq = fg.StimSequence()
+    seq.add_stim(fg.StimCurrentCoord2D(0, 5, 0.5, 0, 12, 0, 4))
+    model.stim_sequence = seq
+    with pytest.warns(RuntimeWarning, match="inf or NaN"):
+        model.run()
+    assert not np.isfinite(model.u).all()
