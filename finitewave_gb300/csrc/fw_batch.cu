@@ -254,34 +254,33 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
 
         if (own) {
             if ((at_on >> s) & 1u) {
+                // first crossing = smallest step; "never" (-1) is the largest
+                // unsigned value (activation_time_2d_tracker.py:61-63)
+                const uint32_t hit =
+                    fused::rows_gt<R>(wc, at_thr) & own & ~at_done;
+                if (hit) {
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    if (!((own >> r) & 1u) || ((at_done >> r) & 1u)) continue;
-                    if (wc[r + 1] > at_thr) {
-                        // first crossing = smallest step; "never" (-1) is the
-                        // largest unsigned value (activation_time_2d_tracker
-                        // .py:61-63)
+                    for (int r = 0; r < R; ++r) {
+                        if (!((hit >> r) & 1u)) continue;
                         const int64_t p = (int64_t)(oi + r0 + r) * T.nj + gj;
                         atomicMin(reinterpret_cast<unsigned *>(T.at_act) + p,
                                   (unsigned)n);
-                        at_done |= 1u << r;
                     }
+                    at_done |= hit;
                 }
             }
             if ((lat_on >> s) & 1u) {
+                // cross_threshold (local_activation_time_2d_tracker.py:71-89)
+                const uint32_t rise =
+                    fused::rows_ge<R>(wc, lat_thr) & own & ~lat_act;
+                const uint32_t fall =
+                    fused::rows_lt<R>(wc, lat_thr) & own & lat_act;
+                lat_act ^= rise | fall;
+                if (rise) {
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    if (!((own >> r) & 1u)) continue;
-                    const bool was = (lat_act >> r) & 1u;
-                    const float x = wc[r + 1];
-                    if (x >= lat_thr && !was) {
-                        // cross_threshold (local_activation_time_2d_tracker
-                        // .py:71-89)
-                        lat_act |= 1u << r;
-                        lat_append(T, (int64_t)(oi + r0 + r) * T.nj + gj, n);
-                    } else if (x < lat_thr && was) {
-                        lat_act &= ~(1u << r);
-                    }
+                    for (int r = 0; r < R; ++r)
+                        if ((rise >> r) & 1u)
+                            lat_append(T, (int64_t)(oi + r0 + r) * T.nj + gj, n);
                 }
             }
         }

@@ -149,6 +149,37 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.wait_group 0;\n" ::);
 }
 
+// Rows r < R of a strip (potential x[r + 1]) that compare with a threshold,
+// as bit masks: the trackers test whole strips without a branch per row and
+// branch only on the rare rows that record something.  Each comparison is
+// the reference's own, so NaN rows match none of them.
+template <int R>
+__device__ __forceinline__ uint32_t rows_gt(const float (&x)[R + 2], float thr)
+{
+    uint32_t m = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) m |= (x[r + 1] > thr ? 1u : 0u) << r;
+    return m;
+}
+
+template <int R>
+__device__ __forceinline__ uint32_t rows_ge(const float (&x)[R + 2], float thr)
+{
+    uint32_t m = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) m |= (x[r + 1] >= thr ? 1u : 0u) << r;
+    return m;
+}
+
+template <int R>
+__device__ __forceinline__ uint32_t rows_lt(const float (&x)[R + 2], float thr)
+{
+    uint32_t m = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) m |= (x[r + 1] < thr ? 1u : 0u) << r;
+    return m;
+}
+
 // Append step n to the crossing list of node p (rare: once per crossing).
 static __device__ __noinline__ void lat_record(const FLat &L, int64_t p,
                                                int64_t n_nodes, int64_t n,
@@ -383,41 +414,40 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
 #pragma unroll
             for (int a = 0; a < kMaxFusedAt; ++a) {
                 if (a >= k.n_at || !((k.at[a].on >> s) & 1u)) continue;
+                // (act_t < 0) & (u > threshold)
+                // (activation_time_2d_tracker.py:61-63): the first crossing
+                // has the smallest step and "never" (-1) is the largest
+                // unsigned value, so an unsigned atomic minimum keeps the
+                // first step without reading it
+                const uint32_t hit =
+                    rows_gt<R>(wc, k.at[a].thr) & own & ~(at_done >> (a * 8));
+                if (hit) {
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const uint32_t bit = 1u << (a * 8 + r);
-                    if (!((own >> r) & 1u) || (at_done & bit)) continue;
-                    if (wc[r + 1] > k.at[a].thr) {
-                        // (act_t < 0) & (u > threshold)
-                        // (activation_time_2d_tracker.py:61-63): the first
-                        // crossing has the smallest step and "never" (-1) is
-                        // the largest unsigned value, so an unsigned atomic
-                        // minimum keeps the first step without reading it
+                    for (int r = 0; r < R; ++r) {
+                        if (!((hit >> r) & 1u)) continue;
                         const int64_t p = (int64_t)(oi + r0 + r) * k.nj + gj;
                         atomicMin(reinterpret_cast<unsigned *>(k.at[a].act) + p,
                                   (unsigned)n);
-                        at_done |= bit;
                     }
+                    at_done |= hit << (a * 8);
                 }
             }
 #pragma unroll
             for (int l = 0; l < kMaxFusedLat; ++l) {
                 if (l >= k.n_lat || !((k.lat[l].on >> s) & 1u)) continue;
+                // cross_threshold (local_activation_time_2d_tracker.py:71-89):
+                // rows rising to >= threshold record the step, rows below it
+                // re-arm
+                const uint32_t was = (lat_act >> (l * 8)) & 0xffu;
+                const uint32_t rise = rows_ge<R>(wc, k.lat[l].thr) & own & ~was;
+                const uint32_t fall = rows_lt<R>(wc, k.lat[l].thr) & own & was;
+                lat_act ^= (rise | fall) << (l * 8);
+                if (rise) {
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    if (!((own >> r) & 1u)) continue;
-                    const uint32_t bit = 1u << (l * 8 + r);
-                    const bool was = (lat_act & bit) != 0;
-                    const float x = wc[r + 1];
-                    if (x >= k.lat[l].thr && !was) {
-                        // cross_threshold (local_activation_time_2d_tracker
-                        // .py:71-89)
-                        lat_act |= bit;
-                        lat_record(k.lat[l], (int64_t)(oi + r0 + r) * k.nj + gj,
-                                   k.n, n, k.status);
-                    } else if (x < k.lat[l].thr && was) {
-                        lat_act &= ~bit;
-                    }
+                    for (int r = 0; r < R; ++r)
+                        if ((rise >> r) & 1u)
+                            lat_record(k.lat[l], (int64_t)(oi + r0 + r) * k.nj + gj,
+                                       k.n, n, k.status);
                 }
             }
         }
@@ -426,7 +456,6 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
         // update is computed for every node and kept only where it is defined
         // (myocytes off the region's ring); the state of the other nodes is
         // never written back.
-        const bool probes_now = probe_mine && ((k.probe_on >> s) & 1u);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const float b1 = wc[r + 1];
@@ -445,10 +474,15 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
             }
             const float uu = M::template update<float>(b1, b1 + d, st[r], P, dt);
             nxt[lr + 1][col + 1] = ((upd >> r) & 1u) ? uu : b1;
-            if (probes_now && ((probe_mine >> r) & 1u))
-                write_probes<M>(k, S.probe_list, S.probe_count, lr, col, s, b1,
-                                st[r], ((myo_bits >> r) & 1u) != 0,
-                                (int64_t)(oi + lr) * k.nj + gj);
+        }
+        // probes: u after the stimuli, the state after the update
+        if (probe_mine && ((k.probe_on >> s) & 1u)) {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if ((probe_mine >> r) & 1u)
+                    write_probes<M>(k, S.probe_list, S.probe_count, r0 + r, col, s,
+                                    wc[r + 1], st[r], ((myo_bits >> r) & 1u) != 0,
+                                    (int64_t)(oi + r0 + r) * k.nj + gj);
         }
         __syncthreads();
     }

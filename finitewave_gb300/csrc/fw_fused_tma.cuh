@@ -349,42 +349,40 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
 #pragma unroll
                 for (int a = 0; a < kMaxFusedAt; ++a) {
                     if (a >= f.n_at || !((f.at[a].on >> s) & 1u)) continue;
+                    const uint32_t hit =
+                        rows_gt<R>(wc, f.at[a].thr) & own & ~(at_done >> (a * 8));
+                    if (hit) {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        const uint32_t bit = 1u << (a * 8 + r);
-                        if (!((own >> r) & 1u) || (at_done & bit)) continue;
-                        if (wc[r + 1] > f.at[a].thr) {
+                        for (int r = 0; r < R; ++r) {
+                            if (!((hit >> r) & 1u)) continue;
                             // first crossing: unsigned minimum, "never" = -1
                             // (activation_time_2d_tracker.py:61-63)
                             const int64_t p = (int64_t)(oi + r0 + r) * f.nj + gj;
                             atomicMin(reinterpret_cast<unsigned *>(f.at[a].act) + p,
                                       (unsigned)n);
-                            at_done |= bit;
                         }
+                        at_done |= hit << (a * 8);
                     }
                 }
 #pragma unroll
                 for (int l = 0; l < kMaxFusedLat; ++l) {
                     if (l >= f.n_lat || !((f.lat[l].on >> s) & 1u)) continue;
+                    // (local_activation_time_2d_tracker.py:71-89)
+                    const uint32_t was = (lat_act >> (l * 8)) & 0xffu;
+                    const uint32_t rise = rows_ge<R>(wc, f.lat[l].thr) & own & ~was;
+                    const uint32_t fall = rows_lt<R>(wc, f.lat[l].thr) & own & was;
+                    lat_act ^= (rise | fall) << (l * 8);
+                    if (rise) {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        if (!((own >> r) & 1u)) continue;
-                        const uint32_t bit = 1u << (l * 8 + r);
-                        const bool was = (lat_act & bit) != 0;
-                        const float x = wc[r + 1];
-                        if (x >= f.lat[l].thr && !was) {
-                            // (local_activation_time_2d_tracker.py:71-89)
-                            lat_act |= bit;
-                            lat_record(f.lat[l], (int64_t)(oi + r0 + r) * f.nj + gj,
-                                       f.n, n, f.status);
-                        } else if (x < f.lat[l].thr && was) {
-                            lat_act &= ~bit;
-                        }
+                        for (int r = 0; r < R; ++r)
+                            if ((rise >> r) & 1u)
+                                lat_record(f.lat[l],
+                                           (int64_t)(oi + r0 + r) * f.nj + gj, f.n, n,
+                                           f.status);
                     }
                 }
             }
 
-            const bool probes_now = probe_mine && ((f.probe_on >> s) & 1u);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const float b1 = wc[r + 1];
@@ -409,10 +407,16 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
                 }
                 const float uu = M::template update<float>(b1, un, st[r], P, dt);
                 nxt[lr + 1][col + xo] = ((upd >> r) & 1u) ? uu : b1;
-                if (probes_now && ((probe_mine >> r) & 1u))
-                    write_probes<M>(f, S.probe_list, S.probe_count, lr, col, s, b1,
-                                    st[r], ((myo_bits >> r) & 1u) != 0,
-                                    (int64_t)(oi + lr) * f.nj + gj);
+            }
+            // probes: u after the stimuli, the state after the update
+            if (probe_mine && ((f.probe_on >> s) & 1u)) {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+                    if ((probe_mine >> r) & 1u)
+                        write_probes<M>(f, S.probe_list, S.probe_count, r0 + r, col,
+                                        s, wc[r + 1], st[r],
+                                        ((myo_bits >> r) & 1u) != 0,
+                                        (int64_t)(oi + r0 + r) * f.nj + gj);
             }
             __syncthreads();
         }
