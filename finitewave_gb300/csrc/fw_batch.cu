@@ -253,7 +253,12 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
         }
 
         if (own) {
-            if ((at_on >> s) & 1u) {
+            float mx = wc[1];
+#pragma unroll
+            for (int r = 1; r < R; ++r) mx = fmaxf(mx, wc[r + 1]);
+            // the strip's maximum first (fmaxf skips NaN rows, which never
+            // cross): most sub-steps cross nowhere
+            if (((at_on >> s) & 1u) && mx > at_thr) {
                 // first crossing = smallest step; "never" (-1) is the largest
                 // unsigned value (activation_time_2d_tracker.py:61-63)
                 const uint32_t hit =

@@ -419,6 +419,12 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
                 // has the smallest step and "never" (-1) is the largest
                 // unsigned value, so an unsigned atomic minimum keeps the
                 // first step without reading it
+                // the strip's maximum first: most sub-steps cross nowhere
+                // (fmaxf skips NaN rows, which never cross)
+                float mx = wc[1];
+#pragma unroll
+                for (int r = 1; r < R; ++r) mx = fmaxf(mx, wc[r + 1]);
+                if (!(mx > k.at[a].thr)) continue;
                 const uint32_t hit =
                     rows_gt<R>(wc, k.at[a].thr) & own & ~(at_done >> (a * 8));
                 if (hit) {

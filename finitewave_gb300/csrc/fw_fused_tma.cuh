@@ -148,10 +148,9 @@ __device__ __forceinline__ int floor_to(int x, int m)
 
 template <int KMAX, int LH, int NS, int NWO>
 __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> &G,
-                                           uint64_t *bar, int tile)
+                                           uint64_t *bar, int bi, int bj)
 {
     constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
-    const int bi = tile / k.f.tiles_j, bj = tile % k.f.tiles_j;
     const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
     const int x4 = floor_to(oj - 1, 4), x16 = floor_to(oj, 16);
     constexpr unsigned bytes =
@@ -198,7 +197,12 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
     }
     __syncthreads();
     int tile = blockIdx.x;
-    if (tid == 0 && tile < k.tiles) issue_tile<KMAX>(k, S.stage[0], &S.bar[0], tile);
+    // tile = bi * tiles_j + bj, advanced by gridDim.x tiles per iteration
+    // without an integer division in the loop
+    const int tj = f.tiles_j;
+    const int di = (int)gridDim.x / tj, dj = (int)gridDim.x % tj;
+    int bi = tile / tj, bj = tile % tj;
+    if (tid == 0 && tile < k.tiles) issue_tile<KMAX>(k, S.stage[0], &S.bar[0], bi, bj);
 
     Params<float, M::NP> P;
 #pragma unroll
@@ -209,12 +213,17 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
     for (int it = 0; tile < k.tiles; ++it, tile += gridDim.x) {
         const int sg = it & 1;
         TmaStage<LH, NS, NWO> &G = S.stage[sg];
+        int ni_ = bi + di, nj_ = bj + dj;
+        if (nj_ >= tj) {
+            nj_ -= tj;
+            ++ni_;
+        }
         // prefetch the next tile into the other stage (its readers finished
         // at the barrier that closed the previous iteration)
         const int next = tile + gridDim.x;
         if (tid == 0 && next < k.tiles) {
             fence_proxy_async();
-            issue_tile<KMAX>(k, S.stage[sg ^ 1], &S.bar[sg ^ 1], next);
+            issue_tile<KMAX>(k, S.stage[sg ^ 1], &S.bar[sg ^ 1], ni_, nj_);
         }
         const bool ok = mbar_wait(&S.bar[sg], (parity >> sg) & 1u);
         parity ^= 1u << sg;
@@ -223,8 +232,9 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             return;
         }
 
-        const int bi = tile / f.tiles_j, bj = tile % f.tiles_j;
         const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
+        bi = ni_;
+        bj = nj_;
         const int xo = oj - floor_to(oj - 1, 4);   // 1..4
         const int xo8 = oj - floor_to(oj, 16);     // 0..15
         const int gj = oj + col;
@@ -308,7 +318,12 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             }
 
         // ---- sub-steps ----
-        for (int s = 0; s < f.ksteps; ++s) {
+        // unrolled for shallow blocks only (measured: faster at K <= 3,
+        // slower at K = 4)
+        constexpr int kUnrollSub = KMAX <= 3 ? KMAX : 1;
+#pragma unroll kUnrollSub
+        for (int s = 0; s < KMAX; ++s) {
+            if (s >= f.ksteps) break;
             const int64_t n = f.n0 + s;
             float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
             float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;
@@ -349,6 +364,12 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
 #pragma unroll
                 for (int a = 0; a < kMaxFusedAt; ++a) {
                     if (a >= f.n_at || !((f.at[a].on >> s) & 1u)) continue;
+                    // the strip's maximum first: most sub-steps cross nowhere
+                    // (fmaxf skips NaN rows, which never cross)
+                    float mx = wc[1];
+#pragma unroll
+                    for (int r = 1; r < R; ++r) mx = fmaxf(mx, wc[r + 1]);
+                    if (!(mx > f.at[a].thr)) continue;
                     const uint32_t hit =
                         rows_gt<R>(wc, f.at[a].thr) & own & ~(at_done >> (a * 8));
                     if (hit) {
