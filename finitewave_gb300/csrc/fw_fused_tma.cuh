@@ -318,12 +318,7 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             }
 
         // ---- sub-steps ----
-        // unrolled for shallow blocks only (measured: faster at K <= 3,
-        // slower at K = 4)
-        constexpr int kUnrollSub = KMAX <= 3 ? KMAX : 1;
-#pragma unroll kUnrollSub
-        for (int s = 0; s < KMAX; ++s) {
-            if (s >= f.ksteps) break;
+        for (int s = 0; s < f.ksteps; ++s) {
             const int64_t n = f.n0 + s;
             float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
             float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;

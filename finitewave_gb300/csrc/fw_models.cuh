@@ -84,10 +84,24 @@ struct ModelAP {
         const T a = P.v[0], k = P.v[1], eap = P.v[2], mu_1 = P.v[3],
                 mu_2 = P.v[4];
         T v = x.v;
-        v += (-dt) * (eap + (mu_1 * v) / (mu_2 + u)) *
-             (v + k * u * (u - a - (T)1.));
-        x.v = v;
-        return un + dt * ((-k) * u * (u - a) * (u - (T)1.) - u * v);
+        if constexpr (sizeof(T) == 4) {
+            // float32: the same update with fewer operations -- u - a - 1
+            // formed once for both equations, u (u - a) (u - 1) as
+            // ((u - (a + 1)) u + a) u, and explicit FMAs; it rounds
+            // differently from the float64 form, within float32 error
+            const T ua1 = u - (a + (T)1.);
+            const T q = __fdividef(mu_1 * v, mu_2 + u);
+            const T g = fmaf(k * u, ua1, v);
+            v = fmaf((-dt) * (eap + q), g, v);
+            x.v = v;
+            const T cub = fmaf(ua1, u, a) * u;
+            return fmaf(dt, fmaf(-k, cub, -(u * v)), un);
+        } else {
+            v += (-dt) * (eap + (mu_1 * v) / (mu_2 + u)) *
+                 (v + k * u * (u - a - (T)1.));
+            x.v = v;
+            return un + dt * ((-k) * u * (u - a) * (u - (T)1.) - u * v);
+        }
     }
 };
 
