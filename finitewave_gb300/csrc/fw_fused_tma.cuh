@@ -11,8 +11,8 @@
 // Every wait on an mbarrier is bounded; a timeout sets FW_DEV_TIMEOUT in the
 // status word and the CTA returns.  Unlike the cp.async kernel, the sub-steps
 // form the diffusion sum as  w_c u + sum_k w_k u_k  in one FMA chain, with
-// the centre weight w_c = 1 - sum_k w_k computed once per tile from the
-// staged off-centre weights (9 FMA per node and sub-step instead of 17
+// the centre weight w_c staged from the weights' own centre plane beside the
+// packed off-centre weights (9 FMA per node and sub-step instead of 17
 // operations for  u + sum_k w_k (u_k - u)).
 //
 // Layout requirements (checked by the host): nj % 16 == 0 (TMA row strides
@@ -42,6 +42,7 @@ struct TmaStage {
     alignas(128) float u[LH + 2][kBoxF];               // rows oi - 1 .. oi + LH
     alignas(128) float s[NS][LH][kBoxF];               // rows oi .. oi + LH - 1
     alignas(128) int8_t myo[LH][kBoxB];
+    alignas(128) float wc[LH][kBoxF];                  // centre weights, rows oi ..
 };
 
 template <int LH, int NS, int NWO>
@@ -59,6 +60,7 @@ struct TmaMaps {
     CUtensorMap myo;    // int8 (nj, ni)
     CUtensorMap u[2];   // f32 (nj, ni), the two potential buffers
     CUtensorMap s[kMaxTmaState];
+    CUtensorMap wc;     // the centre weight plane, f32 (nj, ni)
 };
 
 struct TmaK {
@@ -155,7 +157,7 @@ __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> 
     const int x4 = floor_to(oj - 1, 4), x16 = floor_to(oj, 16);
     constexpr unsigned bytes =
         sizeof(G.wa) + (NWO == 8 ? sizeof(G.wb) : 0) + sizeof(G.u) +
-        sizeof(G.s) + sizeof(G.myo);
+        sizeof(G.s) + sizeof(G.myo) + sizeof(G.wc);
     mbar_expect_tx(bar, bytes);
     tma_3d(&G.wa[0][0], &k.maps.w, 0, oj, oi, bar);
     if constexpr (NWO == 8) tma_3d(&G.wb[0][0], &k.maps.w, 4, oj, oi, bar);
@@ -163,6 +165,7 @@ __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> 
 #pragma unroll
     for (int q = 0; q < NS; ++q) tma_2d(&G.s[q][0][0], &k.maps.s[q], x4, oi, bar);
     tma_2d(&G.myo[0][0], &k.maps.myo, x16, oi, bar);
+    tma_2d(&G.wc[0][0], &k.maps.wc, x4, oi, bar);
 }
 
 template <class M, int ST, int KMAX, int LH, int R>
@@ -256,20 +259,11 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             st[r] = M::template from_array<float>(sv);
         }
         upd &= myo_bits;
-        // centre weights of the strip: every stencil row sums to one, so
-        // w_c = 1 - sum of the off-centre weights; the sub-steps then form
+        // centre weights of the strip (the stored plane); the sub-steps form
         // the reference's sum  w_c u + sum_k w_k u_k  as one FMA chain
         float wcen[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const float4 wa = G.wa[r0 + r][col];
-            float sw = wa.x + wa.y + wa.z + wa.w;
-            if constexpr (NWO == 8) {
-                const float4 wb = G.wb[r0 + r][col];
-                sw += wb.x + wb.y + wb.z + wb.w;
-            }
-            wcen[r] = 1.f - sw;
-        }
+        for (int r = 0; r < R; ++r) wcen[r] = G.wc[r0 + r][col + xo];
 
         // probe cells of this tile
         uint32_t probe_mine = 0;
@@ -518,7 +512,8 @@ inline int sm_count()
 // True when the TMA form can run this configuration.
 inline bool tma_usable(const fw_step_args *a)
 {
-    return a->weights_packed && a->nj % 16 == 0 && a->ni < (1 << 30) &&
+    return a->weights_packed && a->weights && ((uintptr_t)a->weights & 15) == 0 &&
+           a->nj % 16 == 0 && a->ni < (1 << 30) &&
            a->nj < (1 << 30) && tensor_map_encoder() != nullptr;
 }
 
@@ -549,6 +544,12 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                         a->nj, a->ni, kBoxF, LH + 2);
     for (int q = 0; q < M::NS && ok; ++q)
         ok = encode_2d(&k.maps.s[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->state[q],
+                       a->nj, a->ni, kBoxF, LH);
+    // the centre plane of the (nw, ni * nj) float32 weights
+    const float *wcen_plane = (const float *)a->weights +
+                              (int64_t)Stencil2D<ST>::CENTRE * a->ni * a->nj;
+    if (ok)
+        ok = encode_2d(&k.maps.wc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, wcen_plane,
                        a->nj, a->ni, kBoxF, LH);
     if (!ok) {
         set_error("fw_step (fused TMA): tensor map encoding failed");
