@@ -1,9 +1,10 @@
 """Pick the fused kernel's shape per (model, stencil, grid size) by timing.
 
 The fused float32 form has several kernels -- the TMA pipeline (64 x 32
-regions, one persistent CTA per SM) and the cp.async kernels (64 x 32
-regions with two CTAs per SM, or 64 x 64 regions) -- and a temporal-block
-depth K (time steps per launch: 2, 3, 4 or 8).  Which is fastest depends on
+regions, one persistent CTA per SM, with 4 x 1 or 2 x 2 nodes per thread)
+and the cp.async kernels (64 x 32 regions with two CTAs per SM, or 64 x 64
+regions) -- and a temporal-block depth K (time steps per launch: 2, 3, 4
+or 8).  Which is fastest depends on
 the model's register and instruction load, the stencil and the grid.  The
 first fused run of a configuration times every candidate for a few launches
 on scratch copies of the model's arrays (no effect on the model, its
@@ -27,9 +28,9 @@ from . import _ffi
 _lock = threading.Lock()
 _memo = {}
 
-# (fused_variant, fused_k) candidates; variant 3 only where the TMA kernel
-# can run (packed weights, nj % 16 == 0)
-_TMA = [(3, 2), (3, 3), (3, 4), (3, 8)]
+# (fused_variant, fused_k) candidates; variants 3 and 4 only where the TMA
+# kernels can run (packed weights, nj % 16 == 0)
+_TMA = [(3, 2), (3, 3), (3, 4), (3, 8), (4, 2), (4, 4), (4, 8)]
 _CPASYNC = [(1, 2), (1, 4), (1, 8), (2, 2), (2, 4), (2, 8)]
 
 

@@ -141,6 +141,16 @@ __device__ __forceinline__ void tma_3d(void *dst, const CUtensorMap *map, int x,
         : "memory");
 }
 
+__device__ __forceinline__ void tma_4d(void *dst, const CUtensorMap *map, int x,
+                                       int y, int z, int w, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::"
+        "bytes [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ int floor_to(int x, int m)
 {
     return x >= 0 ? x - x % m : -((-x + m - 1) / m) * m;
@@ -148,7 +158,9 @@ __device__ __forceinline__ int floor_to(int x, int m)
 
 // ---- kernel ----------------------------------------------------------------------
 
-template <int KMAX, int LH, int NS, int NWO>
+// PAIRS: the weight map is the column-pair view of encode_weights_pairs, and
+// the weights land as [row][column parity][column pair] (k_fused_tma2).
+template <int KMAX, int LH, int NS, int NWO, bool PAIRS = false>
 __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> &G,
                                            uint64_t *bar, int bi, int bj)
 {
@@ -159,8 +171,13 @@ __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> 
         sizeof(G.wa) + (NWO == 8 ? sizeof(G.wb) : 0) + sizeof(G.u) +
         sizeof(G.s) + sizeof(G.myo) + sizeof(G.wc);
     mbar_expect_tx(bar, bytes);
-    tma_3d(&G.wa[0][0], &k.maps.w, 0, oj, oi, bar);
-    if constexpr (NWO == 8) tma_3d(&G.wb[0][0], &k.maps.w, 4, oj, oi, bar);
+    if constexpr (PAIRS) {
+        tma_4d(&G.wa[0][0], &k.maps.w, 0, oj / 2, 0, oi, bar);
+        if constexpr (NWO == 8) tma_4d(&G.wb[0][0], &k.maps.w, 4, oj / 2, 0, oi, bar);
+    } else {
+        tma_3d(&G.wa[0][0], &k.maps.w, 0, oj, oi, bar);
+        if constexpr (NWO == 8) tma_3d(&G.wb[0][0], &k.maps.w, 4, oj, oi, bar);
+    }
     tma_2d(&G.u[0][0], &k.maps.u[k.in_buf], x4, oi - 1, bar);
 #pragma unroll
     for (int q = 0; q < NS; ++q) tma_2d(&G.s[q][0][0], &k.maps.s[q], x4, oi, bar);
@@ -454,6 +471,366 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
     }
 }
 
+// ---- column-pair kernel ----------------------------------------------------------
+//
+// The same tile pipeline as k_fused_tma with each thread on two adjacent
+// columns and two rows (a 2 x 2 block of nodes) instead of one column and
+// four rows: a row of the potential window is then one float2 load plus its
+// two outer neighbours (3 loads for 2 nodes instead of 6), and the state,
+// centre weights and updated potential move as float2.  The weights arrive
+// from the column-pair view of the packed array (encode_weights_pairs) as
+// [row][column parity][column pair], so the lanes of a warp read contiguous
+// float4s.  Each node's arithmetic is k_fused_tma's, in the same order.
+// Needs an even region origin (even KMAX), which makes the float2 offsets
+// 8-byte aligned.
+
+// w_c u + sum_k w_k u_k in k_fused_tma's order: rows above (ul, uc, ur),
+// the node's own row (ml, mr) and below (dl, dc, dr).
+template <int ST>
+__device__ __forceinline__ float stencil_fma(float wcen, float c, const float4 &wa,
+                                             const float4 &wb, float ul, float uc,
+                                             float ur, float ml, float mr, float dl,
+                                             float dc, float dr)
+{
+    float un = wcen * c;
+    if constexpr (ST == FW_STENCIL_ISO5) {
+        un = fmaf(wa.x, uc, un);
+        un = fmaf(wa.y, ml, un);
+        un = fmaf(wa.z, mr, un);
+        un = fmaf(wa.w, dc, un);
+    } else {
+        un = fmaf(wa.x, ul, un);
+        un = fmaf(wa.y, uc, un);
+        un = fmaf(wa.z, ur, un);
+        un = fmaf(wa.w, ml, un);
+        un = fmaf(wb.x, mr, un);
+        un = fmaf(wb.y, dl, un);
+        un = fmaf(wb.z, dc, un);
+        un = fmaf(wb.w, dr, un);
+    }
+    return un;
+}
+
+template <class M, int ST, int KMAX, int LH>
+__global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
+    k_fused_tma2(const __grid_constant__ TmaK k)
+{
+    constexpr int LW = kTW, HW = kTW / 2;   // columns, column pairs
+    constexpr int R = 2;                     // rows per thread
+    constexpr int NT = HW * (LH / R);
+    constexpr int TI = LH - 2 * KMAX, TJ = LW - 2 * KMAX;
+    constexpr int NS = M::NS;
+    constexpr int NWO = Stencil2D<ST>::NWO;
+    static_assert(KMAX % 2 == 0, "column pairs need an even region origin");
+    static_assert(LH % R == 0 && TI > 0 && TJ > 0, "tile shape");
+    static_assert(NS <= kMaxTmaState, "state arrays");
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned mis = smem_u32(smem_raw) & 127u;
+    TmaSmem<LH, NS, NWO> &S = *reinterpret_cast<TmaSmem<LH, NS, NWO> *>(
+        smem_raw + (mis ? 128u - mis : 0u));
+    const FusedK &f = k.f;
+
+    const int tid = threadIdx.x;
+    const int cp = tid % HW;        // column pair
+    const int c0 = 2 * cp;          // first of the thread's two columns
+    const int r0 = (tid / HW) * R;
+    // node j = 2 r + h sits at row r0 + r, column c0 + h; the masks below do
+    // not depend on the tile
+    uint32_t own_c = 0, ring_c = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int lr = r0 + r, lc = c0 + h, j = 2 * r + h;
+            if (lc >= KMAX && lc < KMAX + TJ && lr >= KMAX && lr < KMAX + TI)
+                own_c |= 1u << j;
+            if (lc > 0 && lc < LW - 1 && lr > 0 && lr < LH - 1) ring_c |= 1u << j;
+        }
+
+    if (tid == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    int tile = blockIdx.x;
+    const int tj = f.tiles_j;
+    const int di = (int)gridDim.x / tj, dj = (int)gridDim.x % tj;
+    int bi = tile / tj, bj = tile % tj;
+    if (tid == 0 && tile < k.tiles)
+        issue_tile<KMAX, LH, NS, NWO, true>(k, S.stage[0], &S.bar[0], bi, bj);
+
+    Params<float, M::NP> P;
+#pragma unroll
+    for (int i = 0; i < M::NP; ++i) P.v[i] = f.params[i];
+    const float dt = f.dt;
+    unsigned parity = 0u;
+
+    for (int it = 0; tile < k.tiles; ++it, tile += gridDim.x) {
+        const int sg = it & 1;
+        TmaStage<LH, NS, NWO> &G = S.stage[sg];
+        int ni_ = bi + di, nj_ = bj + dj;
+        if (nj_ >= tj) {
+            nj_ -= tj;
+            ++ni_;
+        }
+        const int next = tile + gridDim.x;
+        if (tid == 0 && next < k.tiles) {
+            fence_proxy_async();
+            issue_tile<KMAX, LH, NS, NWO, true>(k, S.stage[sg ^ 1], &S.bar[sg ^ 1],
+                                                ni_, nj_);
+        }
+        const bool ok = mbar_wait(&S.bar[sg], (parity >> sg) & 1u);
+        parity ^= 1u << sg;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0 && f.status) atomicOr(f.status, FW_DEV_TIMEOUT);
+            return;
+        }
+
+        const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
+        bi = ni_;
+        bj = nj_;
+        const int xo = oj - floor_to(oj - 1, 4);   // 2 or 4 (oj is even)
+        const int xo8 = oj - floor_to(oj, 16);     // 0..14, even
+        const int gj0 = oj + c0;
+        const int cx = c0 + xo;                    // float2-aligned window column
+
+        typename M::template St<float> st[2 * R];
+        uint32_t myo_bits = 0, inb = 0;
+        float wcen[2 * R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int lr = r0 + r, gi = oi + lr;
+            const bool row_in = (unsigned)gi < (unsigned)f.ni;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = 2 * r + h;
+                if (row_in && (unsigned)(gj0 + h) < (unsigned)f.nj) inb |= 1u << j;
+                if (G.myo[lr][c0 + h + xo8]) myo_bits |= 1u << j;
+            }
+            float sv0[kMaxTmaState], sv1[kMaxTmaState];
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                const float2 v2 = *reinterpret_cast<const float2 *>(&G.s[q][lr][cx]);
+                sv0[q] = v2.x;
+                sv1[q] = v2.y;
+            }
+            st[2 * r] = M::template from_array<float>(sv0);
+            st[2 * r + 1] = M::template from_array<float>(sv1);
+            const float2 w2 = *reinterpret_cast<const float2 *>(&G.wc[lr][cx]);
+            wcen[2 * r] = w2.x;
+            wcen[2 * r + 1] = w2.y;
+        }
+        myo_bits &= inb;
+        const uint32_t own = own_c & inb;
+        const uint32_t upd = ring_c & myo_bits;
+
+        // probe cells of this tile
+        uint32_t probe_mine = 0;
+        if (f.n_probe) {
+            for (int i = tid; i < (LH * LW + 31) / 32; i += NT) S.probe_bits[i] = 0;
+            if (tid == 0) S.probe_count = 0;
+            __syncthreads();
+            for (int t = 0; t < f.n_probe; ++t) {
+                const FProbe &pr = f.probe[t];
+                for (int c = tid; c < pr.n_cells; c += NT) {
+                    const int64_t p = pr.cells[c];
+                    const int gi = (int)(p / f.nj), gjj = (int)(p % f.nj);
+                    const int lr = gi - oi, lc = gjj - oj;
+                    if (lr >= KMAX && lr < KMAX + TI && lc >= KMAX &&
+                        lc < KMAX + TJ) {
+                        const int e = atomicAdd(&S.probe_count, 1);
+                        if (e < kMaxFusedProbeEntries) {
+                            S.probe_list[e] = ProbeEntry{(int16_t)lr, (int16_t)lc,
+                                                         (int16_t)t, c};
+                            const int bit = lr * LW + lc;
+                            atomicOr(&S.probe_bits[bit >> 5], 1u << (bit & 31));
+                        } else if (f.status) {
+                            atomicOr(f.status, FW_DEV_PROBE_OVERFLOW);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 2 * R; ++j) {
+                const int bit = (r0 + j / 2) * LW + c0 + (j & 1);
+                if ((S.probe_bits[bit >> 5] >> (bit & 31)) & 1u) probe_mine |= 1u << j;
+            }
+        }
+        uint32_t lat_act = 0, at_done = 0;
+#pragma unroll
+        for (int l = 0; l < kMaxFusedLat; ++l)
+            if (l < f.n_lat) {
+#pragma unroll
+                for (int j = 0; j < 2 * R; ++j)
+                    if ((own >> j) & 1u) {
+                        const int64_t p =
+                            (int64_t)(oi + r0 + j / 2) * f.nj + gj0 + (j & 1);
+                        if (f.lat[l].activated[p]) lat_act |= 1u << (l * 8 + j);
+                    }
+            }
+
+        // ---- sub-steps ----
+        for (int s = 0; s < f.ksteps; ++s) {
+            const int64_t n = f.n0 + s;
+            float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
+            float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;
+
+            if ((f.stim_on >> s) & 1u) {
+                for (int i = 0; i < f.n_stims; ++i) {
+                    const FStim &F = f.stims[i];
+                    if (!((F.on >> s) & 1u)) continue;
+#pragma unroll
+                    for (int j = 0; j < 2 * R; ++j) {
+                        if (!((myo_bits >> j) & 1u)) continue;
+                        const int lr = r0 + j / 2, gi = oi + lr, gj = gj0 + (j & 1);
+                        if (gj < F.lo1 || gj >= F.hi1) continue;
+                        if (gi < F.lo0 || gi >= F.hi0) continue;
+                        if (F.mask && !F.mask[(int64_t)gi * f.nj + gj]) continue;
+                        float x = cur[lr + 1][cx + (j & 1)];
+                        if (F.kind == FW_STIM_VOLTAGE) {
+                            x = F.value;
+                        } else {
+                            x = x + F.value;
+                            if (F.has_umax && x > F.u_max) x = F.u_max;
+                        }
+                        cur[lr + 1][cx + (j & 1)] = x;
+                    }
+                }
+                __syncthreads();
+            }
+
+            // window rows r0 - 1 .. r0 + R: a = column c0 - 1, (m0, m1) =
+            // columns c0, c0 + 1, b = column c0 + 2
+            float a[R + 2], m0[R + 2], m1[R + 2], b[R + 2];
+#pragma unroll
+            for (int i = 0; i < R + 2; ++i) {
+                a[i] = cur[r0 + i][cx - 1];
+                const float2 mm = *reinterpret_cast<const float2 *>(&cur[r0 + i][cx]);
+                m0[i] = mm.x;
+                m1[i] = mm.y;
+                b[i] = cur[r0 + i][cx + 2];
+            }
+
+            if (own) {
+                float mx = fmaxf(fmaxf(m0[1], m1[1]), fmaxf(m0[2], m1[2]));
+#pragma unroll
+                for (int aa = 0; aa < kMaxFusedAt; ++aa) {
+                    if (aa >= f.n_at || !((f.at[aa].on >> s) & 1u)) continue;
+                    // (fmaxf skips NaN nodes, which never cross)
+                    if (!(mx > f.at[aa].thr)) continue;
+                    const float thr = f.at[aa].thr;
+                    uint32_t hit = (m0[1] > thr ? 1u : 0u) | (m1[1] > thr ? 2u : 0u) |
+                                   (m0[2] > thr ? 4u : 0u) | (m1[2] > thr ? 8u : 0u);
+                    hit &= own & ~(at_done >> (aa * 8));
+                    if (hit) {
+#pragma unroll
+                        for (int j = 0; j < 2 * R; ++j) {
+                            if (!((hit >> j) & 1u)) continue;
+                            // first crossing: unsigned minimum, "never" = -1
+                            // (activation_time_2d_tracker.py:61-63)
+                            const int64_t p =
+                                (int64_t)(oi + r0 + j / 2) * f.nj + gj0 + (j & 1);
+                            atomicMin(reinterpret_cast<unsigned *>(f.at[aa].act) + p,
+                                      (unsigned)n);
+                        }
+                        at_done |= hit << (aa * 8);
+                    }
+                }
+#pragma unroll
+                for (int l = 0; l < kMaxFusedLat; ++l) {
+                    if (l >= f.n_lat || !((f.lat[l].on >> s) & 1u)) continue;
+                    // (local_activation_time_2d_tracker.py:71-89)
+                    const float thr = f.lat[l].thr;
+                    const uint32_t ge = (m0[1] >= thr ? 1u : 0u) |
+                                        (m1[1] >= thr ? 2u : 0u) |
+                                        (m0[2] >= thr ? 4u : 0u) |
+                                        (m1[2] >= thr ? 8u : 0u);
+                    const uint32_t lt = (m0[1] < thr ? 1u : 0u) |
+                                        (m1[1] < thr ? 2u : 0u) |
+                                        (m0[2] < thr ? 4u : 0u) |
+                                        (m1[2] < thr ? 8u : 0u);
+                    const uint32_t was = (lat_act >> (l * 8)) & 0xffu;
+                    const uint32_t rise = ge & own & ~was;
+                    const uint32_t fall = lt & own & was;
+                    lat_act ^= (rise | fall) << (l * 8);
+                    if (rise) {
+#pragma unroll
+                        for (int j = 0; j < 2 * R; ++j)
+                            if ((rise >> j) & 1u)
+                                lat_record(f.lat[l],
+                                           (int64_t)(oi + r0 + j / 2) * f.nj + gj0 +
+                                               (j & 1),
+                                           f.n, n, f.status);
+                    }
+                }
+            }
+
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int lr = r0 + r;
+                const float4 wa0 = G.wa[lr][cp], wa1 = G.wa[lr][HW + cp];
+                float4 wb0 = wa0, wb1 = wa1;
+                if constexpr (NWO == 8) {
+                    wb0 = G.wb[lr][cp];
+                    wb1 = G.wb[lr][HW + cp];
+                }
+                const float un0 = stencil_fma<ST>(wcen[2 * r], m0[r + 1], wa0, wb0,
+                                                  a[r], m0[r], m1[r], a[r + 1],
+                                                  m1[r + 1], a[r + 2], m0[r + 2],
+                                                  m1[r + 2]);
+                const float un1 = stencil_fma<ST>(wcen[2 * r + 1], m1[r + 1], wa1, wb1,
+                                                  m0[r], m1[r], b[r], m0[r + 1],
+                                                  b[r + 1], m0[r + 2], m1[r + 2],
+                                                  b[r + 2]);
+                const float uu0 =
+                    M::template update<float>(m0[r + 1], un0, st[2 * r], P, dt);
+                const float uu1 =
+                    M::template update<float>(m1[r + 1], un1, st[2 * r + 1], P, dt);
+                float2 o;
+                o.x = ((upd >> (2 * r)) & 1u) ? uu0 : m0[r + 1];
+                o.y = ((upd >> (2 * r + 1)) & 1u) ? uu1 : m1[r + 1];
+                *reinterpret_cast<float2 *>(&nxt[lr + 1][cx]) = o;
+            }
+            // probes: u after the stimuli, the state after the update
+            if (probe_mine && ((f.probe_on >> s) & 1u)) {
+#pragma unroll
+                for (int j = 0; j < 2 * R; ++j)
+                    if ((probe_mine >> j) & 1u)
+                        write_probes<M>(f, S.probe_list, S.probe_count, r0 + j / 2,
+                                        c0 + (j & 1), s,
+                                        (j & 1) ? m1[j / 2 + 1] : m0[j / 2 + 1], st[j],
+                                        ((myo_bits >> j) & 1u) != 0,
+                                        (int64_t)(oi + r0 + j / 2) * f.nj + gj0 +
+                                            (j & 1));
+            }
+            __syncthreads();
+        }
+
+        // ---- write the interior back ----
+        float(*fin)[kBoxF] = (f.ksteps & 1) ? S.u1 : G.u;
+#pragma unroll
+        for (int j = 0; j < 2 * R; ++j) {
+            if (!((own >> j) & 1u)) continue;
+            const int lr = r0 + j / 2;
+            const int64_t p = (int64_t)(oi + lr) * f.nj + gj0 + (j & 1);
+            if ((myo_bits >> j) & 1u) {
+                const float uo = fin[lr + 1][cx + (j & 1)];
+                f.u_out[p] = uo;
+                if (!isfinite(uo) && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
+                M::template store<float>(f.state, p, st[j]);
+            }
+#pragma unroll
+            for (int l = 0; l < kMaxFusedLat; ++l)
+                if (l < f.n_lat)
+                    f.lat[l].activated[p] = (lat_act >> (l * 8 + j)) & 1u;
+        }
+        __syncthreads();
+    }
+}
+
 // ---- host side -------------------------------------------------------------------
 
 inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
@@ -500,6 +877,24 @@ inline bool encode_weights(CUtensorMap *m, const void *base, int nwo, int64_t nj
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The same packed weights viewed as (q, column pair, column parity, row):
+// a box of 32 pairs x 2 parities lands as [row][parity][pair] float4s.
+inline bool encode_weights_pairs(CUtensorMap *m, const void *base, int nwo,
+                                 int64_t nj, int64_t ni, int bh)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[4] = {(cuuint64_t)nwo, (cuuint64_t)(nj / 2), 2, (cuuint64_t)ni};
+    cuuint64_t strides[3] = {(cuuint64_t)(2 * nwo * 4), (cuuint64_t)(nwo * 4),
+                             (cuuint64_t)(nj * nwo * 4)};
+    cuuint32_t box[4] = {4, (cuuint32_t)(kTW / 2), 2, (cuuint32_t)bh};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void *>(base), dims,
+               strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 inline int sm_count()
 {
     int dev = 0, n = 0;
@@ -517,15 +912,20 @@ inline bool tma_usable(const fw_step_args *a)
            a->nj < (1 << 30) && tensor_map_encoder() != nullptr;
 }
 
-template <class M, int ST, int KMAX, int LH, int R>
+// PAIRS: the column-pair kernel k_fused_tma2 (R is then 2, fixed by it).
+template <class M, int ST, int KMAX, int LH, int R, bool PAIRS = false>
 int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                      cudaStream_t stream)
 {
     constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
-    constexpr int NT = kTW * (LH / R);
+    constexpr int NT = PAIRS ? (kTW / 2) * (LH / 2) : kTW * (LH / R);
     constexpr int NWO = Stencil2D<ST>::NWO;
     constexpr size_t SMEM = sizeof(TmaSmem<LH, M::NS, NWO>) + 1024;
-    auto kern = k_fused_tma<M, ST, KMAX, LH, R>;
+    void (*kern)(const TmaK);
+    if constexpr (PAIRS)
+        kern = k_fused_tma2<M, ST, KMAX, LH>;
+    else
+        kern = k_fused_tma<M, ST, KMAX, LH, R>;
     FW_CUDA_CHECK(cudaFuncSetAttribute(
         kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM));
     if (a->n_lat > kMaxFusedLat) {
@@ -535,7 +935,10 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     }
     TmaK k;  // kernel argument, copied at each launch
     memset(&k, 0, sizeof k);
-    bool ok = encode_weights(&k.maps.w, a->weights_packed, NWO, a->nj, a->ni, LH) &&
+    bool ok = (PAIRS ? encode_weights_pairs(&k.maps.w, a->weights_packed, NWO, a->nj,
+                                            a->ni, LH)
+                     : encode_weights(&k.maps.w, a->weights_packed, NWO, a->nj, a->ni,
+                                      LH)) &&
               encode_2d(&k.maps.myo, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a->myo,
                         a->nj, a->ni, kBoxB, LH) &&
               encode_2d(&k.maps.u[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->u[0],
@@ -602,7 +1005,8 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 //   1: cp.async staging, 64 x 32 regions, 256 threads, two CTAs per SM;
 //   2: cp.async staging, 64 x 64 regions, 512 threads, one CTA per SM;
 //   3: TMA pipeline: persistent CTAs, 64 x 32 regions, 512 threads with
-//      4-node strips, two stages in shared memory.
+//      4-node strips, two stages in shared memory;
+//   4: the TMA pipeline with 2 x 2 node blocks per thread (even K only).
 // KMAX (fused_k) in {2, 4, 8} time steps per launch.
 template <class M, int ST>
 int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
@@ -611,7 +1015,7 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     const int k = a->fused_k ? a->fused_k : 4;
     int v = a->fused_variant;
     if (v == 0) v = tma_usable(a) ? 3 : 1;
-    if (v == 3 && !tma_usable(a)) {
+    if ((v == 3 || v == 4) && !tma_usable(a)) {
         set_error("fw_step (fused): the TMA kernel needs packed weights and "
                   "nj %% 16 == 0");
         return FW_ERR_UNSUPPORTED;
@@ -620,6 +1024,8 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     return launch_fused<M, ST, KK, 64, LH, 8, MINB>(a, n_begin, n_steps, stream)
 #define FW_TMA_CASE(KK)                                                        \
     return launch_fused_tma<M, ST, KK, 32, 4>(a, n_begin, n_steps, stream)
+#define FW_TMA2_CASE(KK)                                                       \
+    return launch_fused_tma<M, ST, KK, 32, 2, true>(a, n_begin, n_steps, stream)
     if (v == 1) {
         if (k == 2) FW_CP_CASE(2, 32, 2);
         if (k == 4) FW_CP_CASE(4, 32, 2);
@@ -633,11 +1039,16 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         if (k == 3) FW_TMA_CASE(3);
         if (k == 4) FW_TMA_CASE(4);
         if (k == 8) FW_TMA_CASE(8);
+    } else if (v == 4) {
+        if (k == 2) FW_TMA2_CASE(2);
+        if (k == 4) FW_TMA2_CASE(4);
+        if (k == 8) FW_TMA2_CASE(8);
     }
 #undef FW_CP_CASE
 #undef FW_TMA_CASE
+#undef FW_TMA2_CASE
     set_error("fw_step (fused): no kernel for fused_k=%d fused_variant=%d "
-              "(k in 2, 4, 8; variant in 0..3)", k, a->fused_variant);
+              "(k in 2, 3, 4, 8; variant in 0..4, variant 4 with even k)", k, a->fused_variant);
     return FW_ERR_UNSUPPORTED;
 }
 

@@ -209,23 +209,13 @@ def test_f32_close_to_f64(gc, form):
     assert np.abs(mv["v"] - g["mv_v"]).max() < 5e-3
 
 
-@pytest.mark.parametrize("name", ["ap", "ms", "fk"])
-@pytest.mark.parametrize("aniso", [False, True])
-@pytest.mark.parametrize("k", [2, 4, 8])
-@pytest.mark.parametrize("variant,nj", [(1, 140), (2, 140), (3, 144)])
-def test_fused_matches_plain_f32(gc, name, aniso, k, variant, nj):
-    """Fused temporal blocking vs the plain FP32 form on a grid of several
-    tiles (150 x nj), S1 plus a cross-field S2, 777 steps (an odd count, not
-    a multiple of k): same activation steps within one step, fields within
-    a tolerance that covers FMA-vs-no-FMA rounding.  Variants 1 and 2 stage
-    with cp.async; variant 3 is the persistent TMA pipeline (rows of a
-    multiple of 16 nodes)."""
+def _fused_case(name, aniso, nj):
     rng = np.random.default_rng(11)
     ni = 150
     mesh = np.where(rng.random((ni, nj)) < 0.15, 2, 1).astype(np.int8)
     ang = rng.uniform(-np.pi, np.pi, (ni, nj))
     fibers = np.stack([np.cos(ang), np.sin(ang)], -1)
-    case = dict(model=name, mesh=mesh, dt=0.01, dr=0.25, t_max=7.77,
+    return dict(model=name, mesh=mesh, dt=0.01, dr=0.25, t_max=7.77,
                 stencil="aniso9" if aniso else "iso5", fibers=fibers,
                 stims=[dict(kind="voltage", t=0, value=1.0,
                             box=[(0, ni), (1, 5)]),
@@ -235,6 +225,20 @@ def test_fused_matches_plain_f32(gc, name, aniso, k, variant, nj):
                           dict(kind="probe", cells=[[3, 3], [75, 70],
                                                     [149, 139], [56, 56]],
                                vars=cases.MODEL_VARS[name], step=3)])
+
+
+@pytest.mark.parametrize("name", ["ap", "ms", "fk"])
+@pytest.mark.parametrize("aniso", [False, True])
+@pytest.mark.parametrize("k", [2, 4, 8])
+@pytest.mark.parametrize("variant,nj", [(1, 140), (2, 140), (3, 144), (4, 144)])
+def test_fused_matches_plain_f32(gc, name, aniso, k, variant, nj):
+    """Fused temporal blocking vs the plain FP32 form on a grid of several
+    tiles (150 x nj), S1 plus a cross-field S2, 777 steps (an odd count, not
+    a multiple of k): same activation steps within one step, fields within
+    a tolerance that covers FMA-vs-no-FMA rounding.  Variants 1 and 2 stage
+    with cp.async; variants 3 and 4 are the persistent TMA pipeline (rows of
+    a multiple of 16 nodes) with 4 x 1 and 2 x 2 nodes per thread."""
+    case = _fused_case(name, aniso, nj)
     ref = gc.run(case, npfloat="float32", form="plain")
     r = gc.run(case, npfloat="float32", form="fused", fused_k=k,
                fused_variant=variant)
@@ -245,6 +249,25 @@ def test_fused_matches_plain_f32(gc, name, aniso, k, variant, nj):
         np.testing.assert_allclose(r[v], ref[v], rtol=0, atol=2e-3)
         np.testing.assert_allclose(r["trackers"][1][v], ref["trackers"][1][v],
                                    rtol=0, atol=2e-3)
+
+
+@pytest.mark.parametrize("name", ["ap", "ms", "fk"])
+@pytest.mark.parametrize("aniso", [False, True])
+@pytest.mark.parametrize("k", [2, 4, 8])
+def test_tma_pair_kernel_equals_strip_kernel(gc, name, aniso, k):
+    """The 2 x 2-block TMA kernel (variant 4) does each node's arithmetic in
+    the strip kernel's (variant 3) order, so fields, state, activation times
+    and probe traces agree bitwise."""
+    case = _fused_case(name, aniso, 144)
+    r3 = gc.run(case, npfloat="float32", form="fused", fused_k=k,
+                fused_variant=3)
+    r4 = gc.run(case, npfloat="float32", form="fused", fused_k=k,
+                fused_variant=4)
+    assert int(r4["model"]._status.item()) == 0
+    for v in cases.MODEL_VARS[name]:
+        assert np.array_equal(r4[v], r3[v]), v
+        assert np.array_equal(r4["trackers"][1][v], r3["trackers"][1][v]), v
+    assert np.array_equal(r4["trackers"][0], r3["trackers"][0])
 
 
 def test_fused_trackers_cable(gc):
