@@ -208,7 +208,16 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
     const int tid = threadIdx.x;
     const int col = tid % LW;
     const int r0 = (tid / LW) * R;
-    const bool col_interior = col >= KMAX && col < KMAX + TJ;
+    // rows of the strip in the region's interior / off its ring: the same
+    // for every tile
+    uint32_t own_c = 0, ring_c = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int lr = r0 + r;
+        if (col >= KMAX && col < KMAX + TJ && lr >= KMAX && lr < KMAX + TI)
+            own_c |= 1u << r;
+        if (col > 0 && col < LW - 1 && lr > 0 && lr < LH - 1) ring_c |= 1u << r;
+    }
 
     if (tid == 0) {
         mbar_init(&S.bar[0], 1);
@@ -258,24 +267,24 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
         const int xo = oj - floor_to(oj - 1, 4);   // 1..4
         const int xo8 = oj - floor_to(oj, 16);     // 0..15
         const int gj = oj + col;
-        const bool col_in = gj >= 0 && gj < f.nj;
+        const bool col_in = (unsigned)gj < (unsigned)f.nj;
 
         // per-thread flags and state of the strip
         typename M::template St<float> st[R];
-        uint32_t myo_bits = 0, own = 0, upd = 0;
+        uint32_t myo_bits = 0, inb = 0;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const int lr = r0 + r, gi = oi + lr;
-            const bool in = col_in && gi >= 0 && gi < f.ni;
-            if (in && G.myo[lr][col + xo8]) myo_bits |= 1u << r;
-            if (in && col_interior && lr >= KMAX && lr < KMAX + TI) own |= 1u << r;
-            if (col > 0 && col < LW - 1 && lr > 0 && lr < LH - 1) upd |= 1u << r;
+            const int lr = r0 + r;
+            if (col_in && (unsigned)(oi + lr) < (unsigned)f.ni) inb |= 1u << r;
+            if (G.myo[lr][col + xo8]) myo_bits |= 1u << r;
             float sv[kMaxTmaState];
 #pragma unroll
             for (int q = 0; q < NS; ++q) sv[q] = G.s[q][lr][col + xo];
             st[r] = M::template from_array<float>(sv);
         }
-        upd &= myo_bits;
+        myo_bits &= inb;
+        const uint32_t own = own_c & inb;
+        const uint32_t upd = ring_c & myo_bits;
         // centre weights of the strip (the stored plane); the sub-steps form
         // the reference's sum  w_c u + sum_k w_k u_k  as one FMA chain
         float wcen[R];
@@ -450,6 +459,7 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
 
         // ---- write the interior back ----
         float(*fin)[kBoxF] = (f.ksteps & 1) ? S.u1 : G.u;
+        bool nonfinite = false;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             if (!((own >> r) & 1u)) continue;
@@ -458,8 +468,7 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             if ((myo_bits >> r) & 1u) {
                 const float uo = fin[lr + 1][col + xo];
                 f.u_out[p] = uo;
-                if (!isfinite(uo) && f.status)
-                    atomicOr(f.status, FW_DEV_NONFINITE);
+                nonfinite |= !isfinite(uo);
                 M::template store<float>(f.state, p, st[r]);
             }
 #pragma unroll
@@ -467,6 +476,7 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
                 if (l < f.n_lat)
                     f.lat[l].activated[p] = (lat_act >> (l * 8 + r)) & 1u;
         }
+        if (nonfinite && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
         __syncthreads();
     }
 }
@@ -811,6 +821,7 @@ __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
 
         // ---- write the interior back ----
         float(*fin)[kBoxF] = (f.ksteps & 1) ? S.u1 : G.u;
+        bool nonfinite = false;
 #pragma unroll
         for (int j = 0; j < 2 * R; ++j) {
             if (!((own >> j) & 1u)) continue;
@@ -819,7 +830,7 @@ __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
             if ((myo_bits >> j) & 1u) {
                 const float uo = fin[lr + 1][cx + (j & 1)];
                 f.u_out[p] = uo;
-                if (!isfinite(uo) && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
+                nonfinite |= !isfinite(uo);
                 M::template store<float>(f.state, p, st[j]);
             }
 #pragma unroll
@@ -827,6 +838,7 @@ __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
                 if (l < f.n_lat)
                     f.lat[l].activated[p] = (lat_act >> (l * 8 + j)) & 1u;
         }
+        if (nonfinite && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
         __syncthreads();
     }
 }
