@@ -167,6 +167,7 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
         }
     }
     typename M::template St<float> st[R];
+    float wcen[R];
     uint32_t myo_bits = 0, own = 0;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -175,6 +176,7 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
         const int64_t p = in ? (int64_t)gi * T.nj + gj : 0;
         const int8_t m = T.myo[p];
         st[r] = M::template load<float>(T.state, p);
+        wcen[r] = T.w[(int64_t)CEN * T.n + p];
         if (in && m) myo_bits |= 1u << r;
         if (in && col_interior && lr >= KMAX && lr < KMAX + TI) own |= 1u << r;
     }
@@ -294,19 +296,12 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
         for (int r = 0; r < R; ++r) {
             const float b1 = wc[r + 1];
             const int lr = r0 + r;
-            float d;
             const float4 wa = S.w[0][lr][col];
-            if constexpr (ST == FW_STENCIL_ISO5) {
-                d = wa.x * (wc[r] - b1) + wa.y * (wl[r + 1] - b1) +
-                    wa.z * (wr[r + 1] - b1) + wa.w * (wc[r + 2] - b1);
-            } else {
-                const float4 wb = S.w[1][lr][col];
-                d = wa.x * (wl[r] - b1) + wa.y * (wc[r] - b1) +
-                    wa.z * (wr[r] - b1) + wa.w * (wl[r + 1] - b1) +
-                    wb.x * (wr[r + 1] - b1) + wb.y * (wl[r + 2] - b1) +
-                    wb.z * (wc[r + 2] - b1) + wb.w * (wr[r + 2] - b1);
-            }
-            const float uu = M::template update<float>(b1, b1 + d, st[r], P, dt);
+            const float4 wb = NWO == 8 ? S.w[1][lr][col] : wa;
+            const float un = fused::stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r],
+                                                    wr[r], wl[r + 1], wr[r + 1],
+                                                    wl[r + 2], wc[r + 2], wr[r + 2]);
+            const float uu = M::template update<float>(b1, un, st[r], P, dt);
             nxt[lr + 1][col + 1] = ((upd >> r) & 1u) ? uu : b1;
         }
         __syncthreads();

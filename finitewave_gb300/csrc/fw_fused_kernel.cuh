@@ -149,6 +149,36 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.wait_group 0;\n" ::);
 }
 
+// The diffusion sum of one node, w_c u + sum_k w_k u_k, as one FMA chain in
+// the reference's term order (isotropic_stencil_2d.py:98-132,
+// asymmetric_stencil_2d.py:165-201): rows above (ul, uc, ur), the node's own
+// row (ml, mr) and below (dl, dc, dr).  Every fused kernel forms it this way
+// from the stored weights, so they agree bitwise node by node.
+template <int ST>
+__device__ __forceinline__ float stencil_fma(float wcen, float c, const float4 &wa,
+                                             const float4 &wb, float ul, float uc,
+                                             float ur, float ml, float mr, float dl,
+                                             float dc, float dr)
+{
+    float un = wcen * c;
+    if constexpr (ST == FW_STENCIL_ISO5) {
+        un = fmaf(wa.x, uc, un);
+        un = fmaf(wa.y, ml, un);
+        un = fmaf(wa.z, mr, un);
+        un = fmaf(wa.w, dc, un);
+    } else {
+        un = fmaf(wa.x, ul, un);
+        un = fmaf(wa.y, uc, un);
+        un = fmaf(wa.z, ur, un);
+        un = fmaf(wa.w, ml, un);
+        un = fmaf(wb.x, mr, un);
+        un = fmaf(wb.y, dl, un);
+        un = fmaf(wb.z, dc, un);
+        un = fmaf(wb.w, dr, un);
+    }
+    return un;
+}
+
 // Rows r < R of a strip (potential x[r + 1]) that compare with a threshold,
 // as bit masks: the trackers test whole strips without a branch per row and
 // branch only on the rare rows that record something.  Each comparison is
@@ -277,8 +307,9 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
                           wbase[q] + p, in);
         }
     }
-    // state and myocyte flags of the nodes this thread owns
+    // state, centre weights and myocyte flags of the nodes this thread owns
     typename M::template St<float> st[R];
+    float wcen[R];
     uint32_t myo_bits = 0, own = 0;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -287,6 +318,7 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
         const int64_t p = in ? (int64_t)gi * k.nj + gj : 0;
         const int8_t m = k.myo[p];
         st[r] = M::template load<float>(k.state, p);
+        wcen[r] = k.w[(int64_t)CEN * k.n + p];
         if (in && m) myo_bits |= 1u << r;
         if (in && col_interior && lr >= KMAX && lr < KMAX + TI) own |= 1u << r;
     }
@@ -466,19 +498,12 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
         for (int r = 0; r < R; ++r) {
             const float b1 = wc[r + 1];
             const int lr = r0 + r;
-            float d;
             const float4 wa = S.w[0][lr][col];
-            if constexpr (ST == FW_STENCIL_ISO5) {
-                d = wa.x * (wc[r] - b1) + wa.y * (wl[r + 1] - b1) +
-                    wa.z * (wr[r + 1] - b1) + wa.w * (wc[r + 2] - b1);
-            } else {
-                const float4 wb = S.w[1][lr][col];
-                d = wa.x * (wl[r] - b1) + wa.y * (wc[r] - b1) +
-                    wa.z * (wr[r] - b1) + wa.w * (wl[r + 1] - b1) +
-                    wb.x * (wr[r + 1] - b1) + wb.y * (wl[r + 2] - b1) +
-                    wb.z * (wc[r + 2] - b1) + wb.w * (wr[r + 2] - b1);
-            }
-            const float uu = M::template update<float>(b1, b1 + d, st[r], P, dt);
+            const float4 wb = NWO == 8 ? S.w[NWO / 4 - 1][lr][col] : wa;
+            const float un = stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r], wr[r],
+                                             wl[r + 1], wr[r + 1], wl[r + 2],
+                                             wc[r + 2], wr[r + 2]);
+            const float uu = M::template update<float>(b1, un, st[r], P, dt);
             nxt[lr + 1][col + 1] = ((upd >> r) & 1u) ? uu : b1;
         }
         // probes: u after the stimuli, the state after the update

@@ -423,24 +423,11 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             for (int r = 0; r < R; ++r) {
                 const float b1 = wc[r + 1];
                 const int lr = r0 + r;
-                float un = wcen[r] * b1;
                 const float4 wa = G.wa[lr][col];
-                if constexpr (ST == FW_STENCIL_ISO5) {
-                    un = fmaf(wa.x, wc[r], un);
-                    un = fmaf(wa.y, wl[r + 1], un);
-                    un = fmaf(wa.z, wr[r + 1], un);
-                    un = fmaf(wa.w, wc[r + 2], un);
-                } else {
-                    const float4 wb = G.wb[lr][col];
-                    un = fmaf(wa.x, wl[r], un);
-                    un = fmaf(wa.y, wc[r], un);
-                    un = fmaf(wa.z, wr[r], un);
-                    un = fmaf(wa.w, wl[r + 1], un);
-                    un = fmaf(wb.x, wr[r + 1], un);
-                    un = fmaf(wb.y, wl[r + 2], un);
-                    un = fmaf(wb.z, wc[r + 2], un);
-                    un = fmaf(wb.w, wr[r + 2], un);
-                }
+                const float4 wb = NWO == 8 ? G.wb[NWO == 8 ? lr : 0][col] : wa;
+                const float un = stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r],
+                                                 wr[r], wl[r + 1], wr[r + 1],
+                                                 wl[r + 2], wc[r + 2], wr[r + 2]);
                 const float uu = M::template update<float>(b1, un, st[r], P, dt);
                 nxt[lr + 1][col + xo] = ((upd >> r) & 1u) ? uu : b1;
             }
@@ -493,33 +480,6 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
 // float4s.  Each node's arithmetic is k_fused_tma's, in the same order.
 // Needs an even region origin (even KMAX), which makes the float2 offsets
 // 8-byte aligned.
-
-// w_c u + sum_k w_k u_k in k_fused_tma's order: rows above (ul, uc, ur),
-// the node's own row (ml, mr) and below (dl, dc, dr).
-template <int ST>
-__device__ __forceinline__ float stencil_fma(float wcen, float c, const float4 &wa,
-                                             const float4 &wb, float ul, float uc,
-                                             float ur, float ml, float mr, float dl,
-                                             float dc, float dr)
-{
-    float un = wcen * c;
-    if constexpr (ST == FW_STENCIL_ISO5) {
-        un = fmaf(wa.x, uc, un);
-        un = fmaf(wa.y, ml, un);
-        un = fmaf(wa.z, mr, un);
-        un = fmaf(wa.w, dc, un);
-    } else {
-        un = fmaf(wa.x, ul, un);
-        un = fmaf(wa.y, uc, un);
-        un = fmaf(wa.z, ur, un);
-        un = fmaf(wa.w, ml, un);
-        un = fmaf(wb.x, mr, un);
-        un = fmaf(wb.y, dl, un);
-        un = fmaf(wb.z, dc, un);
-        un = fmaf(wb.w, dr, un);
-    }
-    return un;
-}
 
 template <class M, int ST, int KMAX, int LH>
 __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
