@@ -242,17 +242,22 @@ typedef struct fw_step_args {
     fw_probe_tracker probe[FW_MAX_PROBE];
     int32_t *status;  /* device int32 status word (may be NULL)             */
     int32_t fused_k;  /* FW_FORM_FUSED time steps per launch: 2, 4 or 8
-                         (0 = 4)                                            */
+                         (0 = 4); 3 also for variant 3                      */
     int32_t fused_variant; /* FW_FORM_FUSED kernel: 0 = automatic (the TMA
                               pipeline when weights_packed is given and
                               nj % 16 == 0, else 1); 1 = cp.async staging,
                               64x32-node regions, two CTAs per SM; 2 = same,
                               64x64 regions; 3 = TMA pipeline (persistent
-                              CTAs, double-buffered 64x32 regions)          */
+                              CTAs, double-buffered 64x32 regions, 4 x 1
+                              nodes per thread); 4 = the TMA pipeline with
+                              2 x 2 nodes per thread (even fused_k).  All
+                              variants give bitwise the same results        */
     const void *weights_packed; /* FW_FORM_FUSED: off-centre float32 weights
                                    node-major, (N, 4) for ISO5 or (N, 8)
                                    for ANISO9, from fw_pack_weights; NULL
-                                   when not available                       */
+                                   when not available.  The TMA variants
+                                   also read the centre plane of `weights`
+                                   (16-byte aligned)                        */
     int32_t n_ecg;
     int32_t n_tip;
     fw_ecg_tracker ecg[FW_MAX_ECG];
