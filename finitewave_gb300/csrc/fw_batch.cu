@@ -14,8 +14,9 @@
 //
 // A tile is the fused form's region (fw_fused_kernel.cuh): the off-centre
 // weights and the potential staged with cp.async into shared memory, the
-// ionic state of each thread's strip in registers, K sub-steps on chip, the
-// interior written back.  Stimulus and tracker windows are evaluated on the
+// ionic state and centre weights of each thread's strip in registers, K
+// sub-steps on chip with the fused kernels' FMA chain (so a batched tissue
+// is bitwise the same as the tissue run alone), the interior written back.  Stimulus and tracker windows are evaluated on the
 // device from each tissue's step windows, so a launch needs no per-launch
 // host data beyond the step offset.  Per sub-step, in the reference's order
 // (core/model/cardiac_model.py:164-178): stimuli, activation / local

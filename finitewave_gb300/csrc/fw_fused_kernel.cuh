@@ -16,10 +16,11 @@
 // updates its R nodes into the other buffer, so no shared load waits behind a
 // shared store.
 //
-// The centre weight is not read: every stencil row sums to one (each major
-// flux moves weight between a neighbour and the centre, each six-point minor
-// flux sums to zero -- asymmetric_stencil_2d.py:204-288 -- and the centre gets
-// +1), so  sum_k w_k u_k = u + sum_{k != c} w_k (u_k - u).
+// The diffusion sum  w_c u + sum_k w_k u_k  is one FMA chain (stencil_fma)
+// over the stored weights: the off-centre ones from shared memory, each
+// node's centre weight from its plane into registers with the state.  The
+// TMA kernels and the batched kernel form it the same way, so every fused
+// kernel gives bitwise the same node values.
 //
 // Inside each sub-step (global step n), in the reference's order
 // (core/model/cardiac_model.py:164-178): stimuli on u (every node of the

@@ -9,11 +9,11 @@
 //   * two stages: while the CTA computes tile i from one stage, the TMA
 //     fills the other with tile i + 1, so HBM traffic overlaps compute.
 // Every wait on an mbarrier is bounded; a timeout sets FW_DEV_TIMEOUT in the
-// status word and the CTA returns.  Unlike the cp.async kernel, the sub-steps
-// form the diffusion sum as  w_c u + sum_k w_k u_k  in one FMA chain, with
-// the centre weight w_c staged from the weights' own centre plane beside the
-// packed off-centre weights (9 FMA per node and sub-step instead of 17
-// operations for  u + sum_k w_k (u_k - u)).
+// status word and the CTA returns.  The sub-steps form the diffusion sum as
+// w_c u + sum_k w_k u_k  in one FMA chain (stencil_fma, shared with the
+// cp.async and batched kernels), with the centre weight w_c staged from the
+// weights' own centre plane beside the packed off-centre weights (9 FMA per
+// node and sub-step instead of 17 operations for  u + sum_k w_k (u_k - u)).
 //
 // Layout requirements (checked by the host): nj % 16 == 0 (TMA row strides
 // and the int8 myocyte rows) and the packed weight array of fw_pack_weights.
