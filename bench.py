@@ -66,6 +66,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+WORKLOAD = ("Aliev-Panfilov 2D 4096x4096, AsymmetricStencil2D (D_al 1, "
+            "D_ac 0.111), 20% diffuse fibrosis, smooth fibers, S1-S2, "
+            "activation tracker")
 METRIC = ("node-steps/s: batched FP32 vs plain FP64 GPU at LAT err≤1 "
           "step; p50/p99 latency")
 UNIT = "myocyte-steps/s"
@@ -893,9 +896,7 @@ def run_gb300(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded fibrosis and fibers)",
             "config": {
-                "workload": "Aliev-Panfilov 2D 4096x4096, AsymmetricStencil2D "
-                            "(D_al 1, D_ac 0.111), 20% diffuse fibrosis, "
-                            "smooth fibers, S1-S2, activation tracker",
+                "workload": WORKLOAD,
                 "grid": [N, N], "myocytes": myo,
                 "time_steps_per_bench_step": chunk, "form": form32 or "auto",
                 "l2": "state larger than L2 (no flush needed)",
@@ -999,12 +1000,19 @@ def run_reference(args):
     line = {
         "metric": METRIC, "value": cpu["value"], "unit": UNIT,
         "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "warmup": args.warmup,
+        # one bench step (args.chunk time steps of the whole grid) at the
+        # rate the bounded sample measured
+        "ms_per_step": (int((mesh == 1).sum()) * args.chunk / cpu["value"] * 1e3
+                        if cpu and cpu.get("value") else None),
+        "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded fibrosis and fibers)",
-        "config": {"workload": "Aliev-Panfilov 2D 4096x4096, "
-                               "AsymmetricStencil2D, 20% fibrosis",
-                   "grid": [N, N]},
+        "config": {"workload": WORKLOAD, "grid": [N, N],
+                   "myocytes": int((mesh == 1).sum()),
+                   "time_steps_per_bench_step": args.chunk,
+                   "form": "float64 CPU restatement (OpenMP)",
+                   "parallelism": "rank 0 host cores"},
         "impl": "reference",
         "cpu_baseline": cpu,
         "e2e": {"value": cpu["value"], "unit": UNIT,
