@@ -288,8 +288,12 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
         // centre weights of the strip (the stored plane); the sub-steps form
         // the reference's sum  w_c u + sum_k w_k u_k  as one FMA chain
         float wcen[R];
+        float4 wreg[R];   // the first four off-centre weights, kept for the tile
 #pragma unroll
-        for (int r = 0; r < R; ++r) wcen[r] = G.wc[r0 + r][col + xo];
+        for (int r = 0; r < R; ++r) {
+            wcen[r] = G.wc[r0 + r][col + xo];
+            wreg[r] = G.wa[r0 + r][col];
+        }
 
         // probe cells of this tile
         uint32_t probe_mine = 0;
@@ -423,7 +427,7 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             for (int r = 0; r < R; ++r) {
                 const float b1 = wc[r + 1];
                 const int lr = r0 + r;
-                const float4 wa = G.wa[lr][col];
+                const float4 wa = wreg[r];
                 const float4 wb = NWO == 8 ? G.wb[NWO == 8 ? lr : 0][col] : wa;
                 const float un = stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r],
                                                  wr[r], wl[r + 1], wr[r + 1],
