@@ -992,8 +992,8 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     int v = a->fused_variant;
     if (v == 0) v = tma_usable(a) ? 3 : 1;
     if ((v == 3 || v == 4) && !tma_usable(a)) {
-        set_error("fw_step (fused): the TMA kernel needs packed weights and "
-                  "nj %% 16 == 0");
+        set_error("fw_step (fused): the TMA kernels need packed weights, "
+                  "16-byte aligned float32 weights and nj %% 16 == 0");
         return FW_ERR_UNSUPPORTED;
     }
 #define FW_CP_CASE(KK, LH, MINB)                                               \
