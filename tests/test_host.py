@@ -291,3 +291,61 @@ def test_device_footprint():
     m3.cardiac_tissue = t3
     assert fg.device_footprint(m3) == 10 * 12 * 14 * (
         2 * 4 + 2 + 5 * 8 + 14 * 4 + 7 * 4)
+
+
+def test_autotune_cache_logic(tmp_path, monkeypatch):
+    """The autotuner's cache without a GPU: the key names the GPU, model
+    class, stencil, dimension and size class; a configuration is timed once,
+    then served from memory, then from the JSON file; an unreadable file
+    means a re-tune, not an error."""
+    import json
+    import torch
+    from finitewave_gb300 import autotune
+
+    path = tmp_path / "tune.json"
+    monkeypatch.setenv("FWGPU_AUTOTUNE_CACHE", str(path))
+    monkeypatch.setattr(torch.cuda, "get_device_name", lambda dev=None: "GPU-X")
+    calls = []
+
+    def fake_tune(model, steps=96):
+        calls.append(model)
+        return {"variant": 3, "k": 4, "ms": {"3/4": 1.0}, "steps": steps}
+
+    monkeypatch.setattr(autotune, "tune", fake_tune)
+
+    class _Stencil:
+        kind = 2
+
+    class AlievPanfilov2D:
+        stencil = _Stencil()
+
+        def __init__(self, shape):
+            self.shape = shape
+
+        def _shape(self):
+            return self.shape
+
+        def _device(self):
+            return 0
+
+    m = AlievPanfilov2D((4096, 4096))
+    assert autotune.key(m) == "GPU-X|AlievPanfilov2D|2|2D|2^24"
+    # the size class is the power of two of the node count
+    assert autotune.key(AlievPanfilov2D((4000, 4000))).endswith("|2^23")
+    assert autotune.key(AlievPanfilov2D((64, 64, 64))).endswith("|3D|2^18")
+
+    autotune._memo.clear()
+    assert autotune.choose(m) == (3, 4) and len(calls) == 1
+    assert autotune.choose(m) == (3, 4) and len(calls) == 1       # memory
+    table = json.loads(path.read_text())
+    assert table[autotune.key(m)]["variant"] == 3
+    autotune._memo.clear()
+    assert autotune.choose(m) == (3, 4) and len(calls) == 1       # file
+    path.write_text("{ not json")
+    autotune._memo.clear()
+    assert autotune.choose(m) == (3, 4) and len(calls) == 2       # re-tuned
+    assert json.loads(path.read_text())[autotune.key(m)]["k"] == 4
+    autotune._memo.clear()
+    # TMA candidates (variants 3 and 4) come first, cp.async ones after
+    assert {v for v, _ in autotune._TMA} == {3, 4}
+    assert all(k % 2 == 0 for v, k in autotune._TMA if v == 4)
