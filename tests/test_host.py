@@ -349,3 +349,40 @@ def test_autotune_cache_logic(tmp_path, monkeypatch):
     # TMA candidates (variants 3 and 4) come first, cp.async ones after
     assert {v for v, _ in autotune._TMA} == {3, 4}
     assert all(k % 2 == 0 for v, k in autotune._TMA if v == 4)
+
+
+def _fmaf(a, b, c):
+    """float32 fused multiply-add: the exact product (fits float64) plus c,
+    rounded to float32 (double rounding at most half an ulp off fmaf)."""
+    return (a.astype(np.float64) * b + c).astype(np.float32)
+
+
+def test_ap_float32_update_rearrangement():
+    """The float32 Aliev-Panfilov update of the fused kernels (u - a - 1
+    formed once, the cubic as ((u - (a + 1)) u + a) u, FMAs) against the
+    reference's expression in float64 (aliev_panfilov_2d.py:133-202) on a
+    grid of (u, v, diffusion) values over the model's range: the new v and
+    u agree within float32 rounding."""
+    f32 = np.float32
+    a, k, eap, mu1, mu2 = 0.1, 8.0, 0.01, 0.2, 0.3
+    dt = 0.01
+    u, v, un = np.meshgrid(np.linspace(-0.1, 1.1, 121),
+                           np.linspace(0.0, 2.5, 101),
+                           np.array([-0.05, 0.0, 0.3]), indexing="ij")
+    # reference, float64
+    v64 = v + (-dt) * (eap + (mu1 * v) / (mu2 + u)) * (v + k * u * (u - a - 1.0))
+    u64 = (u + un) + dt * ((-k) * u * (u - a) * (u - 1.0) - u * v64)
+    # the float32 form
+    U, V, UN = (x.astype(f32) for x in (u, v, u + un))
+    A, K, EAP, MU1, MU2, DT = (f32(x) for x in (a, k, eap, mu1, mu2, dt))
+    ua1 = U - (A + f32(1.0))
+    q = (MU1 * V) / (MU2 + U)
+    g = _fmaf(K * U, ua1, V)
+    V32 = _fmaf((-DT) * (EAP + q), g, V)
+    cub = _fmaf(ua1, U, A) * U
+    U32 = _fmaf(np.full_like(U, DT), _fmaf(np.full_like(U, -K), cub, -(U * V32)), UN)
+    scale_v = np.maximum(np.abs(v64), 1.0)
+    scale_u = np.maximum(np.abs(u64), 1.0)
+    # about one float32 ulp measured (1.1e-7); two allowed
+    assert np.max(np.abs(V32 - v64) / scale_v) < 2.5e-7
+    assert np.max(np.abs(U32 - u64) / scale_u) < 2.5e-7
