@@ -386,3 +386,95 @@ def test_ap_float32_update_rearrangement():
     # about one float32 ulp measured (1.1e-7); two allowed
     assert np.max(np.abs(V32 - v64) / scale_v) < 2.5e-7
     assert np.max(np.abs(U32 - u64) / scale_u) < 2.5e-7
+
+
+class _HostModel:
+    """Stand-in for a model on the host side of commands and checkpoints."""
+    state_vars = ["u", "v"]
+
+    def __init__(self, t_max=10.0):
+        self.t = 0.0
+        self.t_max = t_max
+        self.u = np.arange(6.0).reshape(2, 3)
+        self.v = -np.arange(6.0).reshape(2, 3)
+
+
+def test_command_sequence_runs_each_command_once_when_due():
+    """core/command/command_sequence.py: a command runs at the first check
+    with t >= its time, once; initialize re-arms every command."""
+    from finitewave_gb300.command import Command, CommandSequence
+
+    ran = []
+
+    class Mark(Command):
+        def execute(self, model):
+            ran.append((self.t, model.t))
+
+    m = _HostModel()
+    seq = CommandSequence()
+    for t in (1.0, 2.0, 3.0):
+        seq.add_command(Mark(t))
+    seq.initialize(m)
+    m.t = 0.5
+    seq.execute_next()
+    assert ran == []
+    m.t = 2.0
+    seq.execute_next()
+    seq.execute_next()
+    assert ran == [(1.0, 2.0), (2.0, 2.0)]
+    m.t = 7.0
+    seq.execute_next()
+    assert [c for c, _ in ran] == [1.0, 2.0, 3.0]
+    seq.initialize(m)
+    seq.execute_next()
+    assert len(ran) == 6
+    seq.remove_commands()
+    assert seq.sequence == []
+
+
+def test_state_saver_and_loader_round_trip(tmp_path):
+    """core/state/state_saver.py, state_loader.py: one <var>.npy per state
+    variable, written once t reaches the saver's time (or t_max for a
+    negative time), read back by the loader; an empty path disables both and
+    a missing directory is a FileNotFoundError."""
+    from finitewave_gb300.state import (StateLoader, StateSaver,
+                                        StateSaverCollection)
+
+    m = _HostModel(t_max=5.0)
+    end = StateSaver(str(tmp_path / "end"))          # time -1: at the end
+    at3 = StateSaver(str(tmp_path / "at3"), time=3.0)
+    coll = StateSaverCollection()
+    coll.savers = [end, at3]
+    coll.initialize(m)
+    m.t = 2.0
+    coll.save()
+    assert not (tmp_path / "end").exists() and not (tmp_path / "at3").exists()
+    m.t = 3.0
+    coll.save()
+    assert (tmp_path / "at3" / "u.npy").exists() and at3.passed
+    m.u = m.u + 100.0                                  # later state
+    coll.save()                                        # at3 does not re-save
+    assert np.array_equal(np.load(tmp_path / "at3" / "u.npy"),
+                          np.arange(6.0).reshape(2, 3))
+    m.t = 5.0
+    coll.save()
+    assert np.array_equal(np.load(tmp_path / "end" / "u.npy"), m.u)
+
+    off = StateSaver("")
+    off.initialize(m)
+    off.save()
+    assert off.passed
+
+    m2 = _HostModel()
+    m2.u = np.zeros((2, 3))
+    m2.v = np.zeros((2, 3))
+    loader = StateLoader(str(tmp_path / "at3"))
+    loader.initialize(m2)
+    loader.load()
+    assert np.array_equal(m2.u, np.arange(6.0).reshape(2, 3))
+    assert np.array_equal(m2.v, -np.arange(6.0).reshape(2, 3))
+    m2.u = None
+    loader.load()                                      # once only
+    assert m2.u is None
+    with pytest.raises(FileNotFoundError):
+        StateLoader(str(tmp_path / "missing")).initialize(m2)
