@@ -478,3 +478,35 @@ def test_state_saver_and_loader_round_trip(tmp_path):
     assert m2.u is None
     with pytest.raises(FileNotFoundError):
         StateLoader(str(tmp_path / "missing")).initialize(m2)
+
+
+def test_tissue_mesh_rules():
+    """core/tissue/cardiac_tissue.py and the 2D/3D tissues: assigning a mesh
+    zeroes its outer ring, a mesh of the wrong dimension is a ValueError,
+    myocyte indices are the flat indices of code 1 outside special
+    boundaries, clean() turns fibrosis back into myocytes, clone() copies."""
+    import finitewave_gb300 as fg
+
+    t = fg.CardiacTissue2D((5, 6))
+    mesh = np.full((5, 6), 1, dtype=np.int8)
+    mesh[2, 3] = 2
+    t.mesh = mesh
+    ring = np.ones((5, 6), bool)
+    ring[1:-1, 1:-1] = False
+    assert (t.mesh[ring] == 0).all() and t.mesh[2, 3] == 2
+    t.compute_myo_indexes()
+    want = np.flatnonzero(t.mesh == 1)
+    assert np.array_equal(t.myo_indexes, want) and len(want) == 3 * 4 - 1
+    t.special_boundaries = np.zeros((5, 6), np.int8)
+    t.special_boundaries[1, 1] = 1
+    t.compute_myo_indexes()
+    assert 1 * 6 + 1 not in t.myo_indexes and len(t.myo_indexes) == 10
+    c = t.clone()
+    c.clean()
+    assert c.mesh[2, 3] == 1 and t.mesh[2, 3] == 2
+    with pytest.raises(ValueError):
+        t.mesh = np.ones((5, 6, 2), np.int8)
+
+    t3 = fg.CardiacTissue3D((4, 5, 6))
+    assert t3.mesh.sum() == 2 * 3 * 4
+    assert (t3.mesh[0] == 0).all() and (t3.mesh[:, :, -1] == 0).all()
