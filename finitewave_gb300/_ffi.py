@@ -24,6 +24,8 @@ FW_DEV_TIMEOUT = 8
 FW_DEV_TIP_OVERFLOW = 16
 FW_DEV_NONFINITE = 32
 
+FW_DEBUG_FORCE_TIMEOUT = 1
+
 MODEL_AP, MODEL_MS, MODEL_FK, MODEL_TP06, MODEL_CRN = 1, 2, 3, 4, 5
 MODEL_BK, MODEL_BO, MODEL_LR91 = 6, 7, 8
 ISO5, ANISO9, ISO7, ANISO19, SYM9 = 1, 2, 3, 4, 5
@@ -106,7 +108,8 @@ class StepArgs(ctypes.Structure):
                 ("fused_variant", _i32), ("weights_packed", _vp),
                 ("n_ecg", _i32), ("n_tip", _i32),
                 ("ecg", EcgTracker * MAX_ECG),
-                ("tip", TipTracker * MAX_TIP)]
+                ("tip", TipTracker * MAX_TIP),
+                ("debug_flags", _i32), ("reserved2", _i32)]
 
 
 class Batch(ctypes.Structure):

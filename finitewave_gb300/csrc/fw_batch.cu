@@ -328,8 +328,8 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
 // exhausted; the last CTA to leave (counted in scratch[1]) zeroes both.
 __global__ void __launch_bounds__(NT, 2)
     k_batch(const BTissue *__restrict__ tissues, const BTile *__restrict__ tiles,
-            int32_t n_tiles, int64_t offset, int32_t ks, int32_t in_buf,
-            uint32_t *scratch)
+            int32_t n_tiles, int32_t n_tissues, int64_t offset, int32_t ks,
+            int32_t in_buf, uint32_t *scratch)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BSmem &S = *reinterpret_cast<BSmem *>(smem_raw);
@@ -340,6 +340,14 @@ __global__ void __launch_bounds__(NT, 2)
         const int t = S.next;
         if (t >= n_tiles) break;
         const BTile bt = tiles[t];
+        if (bt.tissue < 0 || bt.tissue >= n_tissues) {
+            // a corrupted plan: report it on the first tissue's status word
+            // and skip the tile
+            if (tid == 0 && tissues[0].h.status)
+                atomicOr(tissues[0].h.status, FW_DEV_BATCH_FAULT);
+            __syncthreads();
+            continue;
+        }
         const BTissue *Tg = tissues + bt.tissue;
         {
             // stage the tissue's head into shared memory
@@ -396,7 +404,9 @@ __global__ void __launch_bounds__(NT, 2)
             run_tile<ModelFK, FW_STENCIL_ANISO9>(stims, bt.tile, n0, ks, in_buf, S);
             break;
         default:
-            break;  // rejected by the plan
+            // rejected by the plan; reached only through a corrupted one
+            if (tid == 0 && T.status) atomicOr(T.status, FW_DEV_BATCH_FAULT);
+            break;
         }
         __syncthreads();
     }
@@ -657,8 +667,8 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
         if (ks > KMAX) ks = KMAX;
         const int in_buf = (int)((offset + li) & 1);
         k_batch<<<b->grid, NT, kSmem, stream>>>(desc, tl, b->n_tiles,
-                                               offset + done, (int32_t)ks,
-                                               in_buf, scratch);
+                                               b->n_tissues, offset + done,
+                                               (int32_t)ks, in_buf, scratch);
         FW_CHECK_LAUNCH("k_batch");
         done += ks;
     }
@@ -687,13 +697,22 @@ uint32_t *g_noalloc_ptr[kNoallocMaxDevices];  // device address, per device
 
 }  // namespace
 
+// The batch's scratch (the tile counters) has a fixed size, so the limit is
+// checked when the library is compiled: a batch kernel needing more than the
+// fixed array holds does not build.
+static_assert(kBatchScratchBytes <= kNoallocScratchBytes,
+              "fw_batch_run_noalloc: the batch scratch exceeds the fixed array");
+
 int batch_run_noalloc(const fw_batch *b, int64_t offset, int64_t n_steps,
                       cudaStream_t stream)
 {
-    if (kBatchScratchBytes > kNoallocScratchBytes) {
-        set_error("fw_batch_run_noalloc: the batch needs %lld bytes of "
-                  "scratch, the library's fixed scratch holds %d",
-                  (long long)kBatchScratchBytes, kNoallocScratchBytes);
+    // the argument checks of batch_run, before the one-time set-up
+    if (!b || !b->plan || b->n_tissues <= 0 || b->grid <= 0) {
+        set_error("fw_batch_run_noalloc: empty plan");
+        return FW_ERR_ARG;
+    }
+    if (offset < 0 || n_steps < 0) {
+        set_error("fw_batch_run_noalloc: negative offset or step count");
         return FW_ERR_ARG;
     }
     int dev = 0;

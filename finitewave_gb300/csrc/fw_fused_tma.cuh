@@ -9,7 +9,8 @@
 //   * two stages: while the CTA computes tile i from one stage, the TMA
 //     fills the other with tile i + 1, so HBM traffic overlaps compute.
 // Every wait on an mbarrier is bounded; a timeout sets FW_DEV_TIMEOUT in the
-// status word and the CTA returns.  The sub-steps form the diffusion sum as
+// status word and the CTA returns once its copies in flight have landed
+// (again a bounded wait).  The sub-steps form the diffusion sum as
 // w_c u + sum_k w_k u_k  in one FMA chain (stencil_fma, shared with the
 // cp.async and batched kernels), with the centre weight w_c staged from the
 // weights' own centre plane beside the packed off-centre weights (9 FMA per
@@ -68,6 +69,8 @@ struct TmaK {
     FusedK f;
     int32_t in_buf;     // potential buffer holding step n0
     int32_t tiles;
+    int32_t force_timeout;  // testing: report every wait as timed out after
+                            // its copy has arrived (FW_DEBUG_FORCE_TIMEOUT)
 };
 
 // ---- PTX wrappers ------------------------------------------------------------
@@ -149,6 +152,21 @@ __device__ __forceinline__ void tma_4d(void *dst, const CUtensorMap *map, int x,
         "bytes [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_u32(dst)),
         "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
         : "memory");
+}
+
+// A CTA giving up on its pipeline: set FW_DEV_TIMEOUT, then wait (bounded)
+// for the bulk copies it still has in flight -- the one into stage sg when
+// its wait did not see it arrive, and the prefetch into the other stage when
+// one was issued -- so that no copy lands in shared memory after the CTA
+// has exited.  Called by thread 0 only.
+template <class TK>
+__device__ __noinline__ void tma_abandon(const TK &k, uint64_t *bar, int sg,
+                                         unsigned ph, unsigned parity,
+                                         bool arrived, int next)
+{
+    if (k.f.status) atomicOr(k.f.status, FW_DEV_TIMEOUT);
+    if (!arrived) mbar_wait(&bar[sg], ph);
+    if (next < k.tiles) mbar_wait(&bar[sg ^ 1], (parity >> (sg ^ 1)) & 1u);
 }
 
 __device__ __forceinline__ int floor_to(int x, int m)
@@ -254,10 +272,11 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             fence_proxy_async();
             issue_tile<KMAX>(k, S.stage[sg ^ 1], &S.bar[sg ^ 1], ni_, nj_);
         }
-        const bool ok = mbar_wait(&S.bar[sg], (parity >> sg) & 1u);
+        const unsigned ph = (parity >> sg) & 1u;
+        const bool arrived = mbar_wait(&S.bar[sg], ph);
         parity ^= 1u << sg;
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0 && f.status) atomicOr(f.status, FW_DEV_TIMEOUT);
+        if (__syncthreads_or(!arrived || k.force_timeout)) {
+            if (tid == 0) tma_abandon(k, S.bar, sg, ph, parity, arrived, next);
             return;
         }
 
@@ -555,10 +574,11 @@ __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
             issue_tile<KMAX, LH, NS, NWO, true>(k, S.stage[sg ^ 1], &S.bar[sg ^ 1],
                                                 ni_, nj_);
         }
-        const bool ok = mbar_wait(&S.bar[sg], (parity >> sg) & 1u);
+        const unsigned ph = (parity >> sg) & 1u;
+        const bool arrived = mbar_wait(&S.bar[sg], ph);
         parity ^= 1u << sg;
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0 && f.status) atomicOr(f.status, FW_DEV_TIMEOUT);
+        if (__syncthreads_or(!arrived || k.force_timeout)) {
+            if (tid == 0) tma_abandon(k, S.bar, sg, ph, parity, arrived, next);
             return;
         }
 
@@ -880,12 +900,19 @@ inline int sm_count()
     return n;
 }
 
-// True when the TMA form can run this configuration.
-inline bool tma_usable(const fw_step_args *a)
+inline bool aligned16(const void *p) { return p && ((uintptr_t)p & 15) == 0; }
+
+// True when the TMA form can run this configuration: every array it reads
+// through a tensor map (packed weights, the weights' centre plane, both
+// potential buffers, the myocyte flags and the model's `ns` state arrays)
+// starts on a 16-byte boundary, and rows are a multiple of 16 nodes.
+inline bool tma_usable(const fw_step_args *a, int ns)
 {
-    return a->weights_packed && a->weights && ((uintptr_t)a->weights & 15) == 0 &&
-           a->nj % 16 == 0 && a->ni < (1 << 30) &&
-           a->nj < (1 << 30) && tensor_map_encoder() != nullptr;
+    bool ok = aligned16(a->weights_packed) && aligned16(a->weights) &&
+              aligned16(a->u[0]) && aligned16(a->u[1]) && aligned16(a->myo) &&
+              a->nj % 16 == 0 && a->ni < (1 << 30) && a->nj < (1 << 30);
+    for (int q = 0; q < ns && ok; ++q) ok = aligned16(a->state[q]);
+    return ok && tensor_map_encoder() != nullptr;
 }
 
 // PAIRS: the column-pair kernel k_fused_tma2 (R is then 2, fixed by it).
@@ -911,6 +938,7 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     }
     TmaK k;  // kernel argument, copied at each launch
     memset(&k, 0, sizeof k);
+    k.force_timeout = (a->debug_flags & FW_DEBUG_FORCE_TIMEOUT) ? 1 : 0;
     bool ok = (PAIRS ? encode_weights_pairs(&k.maps.w, a->weights_packed, NWO, a->nj,
                                             a->ni, LH)
                      : encode_weights(&k.maps.w, a->weights_packed, NWO, a->nj, a->ni,
@@ -990,10 +1018,11 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 {
     const int k = a->fused_k ? a->fused_k : 4;
     int v = a->fused_variant;
-    if (v == 0) v = tma_usable(a) ? 3 : 1;
-    if ((v == 3 || v == 4) && !tma_usable(a)) {
+    if (v == 0) v = tma_usable(a, M::NS) ? 3 : 1;
+    if ((v == 3 || v == 4) && !tma_usable(a, M::NS)) {
         set_error("fw_step (fused): the TMA kernels need packed weights, "
-                  "16-byte aligned float32 weights and nj %% 16 == 0");
+                  "16-byte aligned weights, potential, state and myocyte "
+                  "arrays and nj %% 16 == 0");
         return FW_ERR_UNSUPPORTED;
     }
 #define FW_CP_CASE(KK, LH, MINB)                                               \

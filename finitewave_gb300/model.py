@@ -24,10 +24,10 @@ import torch
 from . import _ffi
 from .stencil import (AsymmetricStencil2D, AsymmetricStencil3D,
                       IsotropicStencil2D, IsotropicStencil3D)
-from .stimulation import Stim
+from . import stimulation, tracker as _tracker
 from .tracker import (ActivationTime2DTracker, ECG2DTracker,
                       LocalActivationTime2DTracker, SpiralWaveCore2DTracker,
-                      _ProbeTracker)
+                      Tracker, _ProbeTracker)
 
 _NP = {"float64": np.float64, "float32": np.float32}
 _MAX_SEGMENT = 1 << 20
@@ -333,11 +333,17 @@ class CardiacModel:
         if self.state_loader:
             self.state_loader.load()
         self._nonmyo_equal = None
+        host_stims, host_trs = self._host_plugins()
         iters = int(np.ceil((self.t_max - self.t) / self.dt))
         remaining = iters
         while remaining > 0:
-            n_seg = self._run_segment(min(remaining, _MAX_SEGMENT),
-                                      sync=False)
+            limit = min(remaining, _MAX_SEGMENT)
+            if host_stims or host_trs:
+                k = self._steps_before_host(limit, host_stims, host_trs)
+                n_seg = self._host_step(host_stims, host_trs) if k == 0 \
+                    else self._run_segment(k, sync=False)
+            else:
+                n_seg = self._run_segment(limit, sync=False)
             remaining -= n_seg
             if self.command_sequence:
                 self.command_sequence.execute_next()
@@ -349,14 +355,84 @@ class CardiacModel:
                 break
         self._check_status()
 
+    def _times(self, limit):
+        """Times t_n of the next `limit` steps and the time after them (the
+        float64 accumulation t += dt)."""
+        acc = np.empty(limit + 1)
+        acc[0] = self.t
+        acc[1:] = self.dt
+        return np.add.accumulate(acc)
+
+    # ------------------------------------------- host round-trip plug-ins
+    def _host_plugins(self):
+        """Stimuli and trackers the kernels do not apply themselves: user
+        subclasses written against the reference's plug-in interface
+        (``Stim.stimulate``, ``Tracker._track`` / ``track``)."""
+        stims = [s for s in (self.stim_sequence.sequence
+                             if self.stim_sequence else [])
+                 if not stimulation.is_native(s)]
+        trs = [t for t in (self.tracker_sequence.sequence
+                           if self.tracker_sequence else [])
+               if not _tracker.is_native(t)]
+        return stims, trs
+
+    def _steps_before_host(self, limit, stims, trs):
+        """Steps (at most `limit`) before the next step on which a host
+        stimulus or tracker is due: a stimulus on steps with t >= stim.t
+        while it has not passed (stim_sequence.py:65-77), a tracker on the
+        steps of Tracker.track (tracker.py:70-83), or on every step when a
+        subclass replaces ``track``."""
+        ts = self._times(limit)[:limit]
+        ns = self.step + np.arange(limit, dtype=np.int64)
+        due = np.zeros(limit, dtype=bool)
+        for s in stims:
+            if not s.passed:
+                due |= ts >= s.t
+        for tr in trs:
+            if isinstance(tr, Tracker) and type(tr).track is not Tracker.track:
+                return 0
+            due |= ((tr.start_time <= ts) & (ts <= tr.end_time) &
+                    (ns % int(tr.step) == 0))
+        return int(np.argmax(due)) if due.any() else limit
+
+    def _host_step(self, stims, trs):
+        """One step with host plug-ins, in the reference's order
+        (cardiac_model.py:164-178).  When a host stimulus is due, every
+        stimulus of the step runs on the host in the sequence's order
+        (this package's own through ``Stim.stimulate`` on the device
+        array); then one plain-form step on the device, with this package's
+        trackers inside it; then the host trackers, which see the state as
+        the reference's do: ``model.u`` after the stimuli, ``model.u_new``
+        and the state variables after the update, ``model.t`` and
+        ``model.step`` of this step."""
+        host_stim = any(self.t >= s.t and not s.passed for s in stims)
+        if host_stim:
+            for s in self.stim_sequence.sequence:
+                if self.t >= s.t and not s.passed:
+                    s.stimulate(self)
+                    s.update_status(self)
+        form = self.form
+        self.form = "plain"
+        try:
+            seg = self._prepare_segment(1, skip_stims=host_stim)
+        finally:
+            self.form = form
+        stream = torch.cuda.current_stream().cuda_stream
+        _ffi.call("fw_step", ctypes.byref(seg.args), seg.n0, seg.n_seg,
+                  stream)
+        if trs:
+            with _HostView(self):
+                for tr in self.tracker_sequence.sequence:
+                    if any(tr is h for h in trs):
+                        tr.track()
+        self._finish_segment(seg)
+        return seg.n_seg
+
     def _segment_times(self, limit):
         """Times t_n of the next `limit` steps and the segment length: the
         first step after which a command, a state save or termination is
         due ends the segment."""
-        acc = np.empty(limit + 1)
-        acc[0] = self.t
-        acc[1:] = self.dt
-        ts_all = np.add.accumulate(acc)
+        ts_all = self._times(limit)
         after = ts_all[1:]
         steps_after = self.step + 1 + np.arange(limit)
         stop = (after > self.t_max) | (steps_after >
@@ -415,6 +491,14 @@ class CardiacModel:
 
     def _check_status(self):
         st = int(self._status.item())
+        if st & _ffi.FW_DEV_TIMEOUT:
+            raise RuntimeError(f"{type(self).__name__}: a bounded on-chip "
+                               "wait of the fused kernel gave up; the state "
+                               "after this run is not defined")
+        if st & _ffi.FW_DEV_BATCH_FAULT:
+            raise RuntimeError(f"{type(self).__name__}: a batch tile "
+                               "descriptor was out of range; the state after "
+                               "this run is not defined")
         if st & _ffi.FW_DEV_NONFINITE:
             # the reference carries on with NaN silently; keep its results
             # and say so
@@ -468,6 +552,7 @@ class CardiacModel:
         a.form = self._form()
         a.fused_k = int(self.fused_k)
         a.fused_variant = int(self.fused_variant)
+        a.debug_flags = int(getattr(self, "_debug_flags", 0))
         if (a.form == _ffi.FORM_FUSED and not a.fused_k and
                 not a.fused_variant and self.autotune):
             from . import autotune
@@ -476,9 +561,11 @@ class CardiacModel:
             if a.form == _ffi.FORM_FUSED else None
         return a
 
-    def _prepare_segment(self, limit):
+    def _prepare_segment(self, limit, skip_stims=False):
         """The fw_step_args of the next segment of at most `limit` steps
-        (stimulus and tracker windows in global step indices)."""
+        (stimulus and tracker windows in global step indices).  Stimuli and
+        trackers that run on the host are left out, and so are all stimuli
+        with skip_stims (a host step that has applied them already)."""
         a = self._bare_args()
         ts, t_end, n_seg = self._segment_times(limit)
         n0 = int(self.step)
@@ -487,11 +574,10 @@ class CardiacModel:
 
         # stimuli (stim_sequence.py:65-77)
         n_st = 0
-        if self.stim_sequence:
+        if self.stim_sequence and not skip_stims:
             for stim in self.stim_sequence.sequence:
-                if not isinstance(stim, Stim) or not hasattr(stim, "_region"):
-                    raise TypeError(f"{type(stim).__name__} is not a "
-                                    "finitewave_gb300 stimulus")
+                if not stimulation.is_native(stim):
+                    continue
                 wins = stim._windows(ts, n0)
                 if not wins:
                     continue
@@ -518,6 +604,8 @@ class CardiacModel:
         n_at = n_lat = n_pr = n_ecg = n_tip = 0
         if self.tracker_sequence:
             for tr in self.tracker_sequence.sequence:
+                if not _tracker.is_native(tr):
+                    continue
                 win = tr._window(ts, n0)
                 if win is None:
                     continue
@@ -601,6 +689,29 @@ class CardiacModel:
                                                   self._dev["u"])
         self.t = seg.t_end
         self.step = seg.n0 + seg.n_seg
+
+
+class _HostView:
+    """While host trackers run: host copies of the state variables also in
+    ``model.__dict__``, where the reference's trackers may read them
+    (``model.__dict__[var]``, multi_variable_2d_tracker.py:54,68); removed
+    afterwards.  Attribute access (``model.u``) reads the device arrays
+    through the state-variable descriptors either way."""
+
+    def __init__(self, model):
+        self.model = model
+        self.names = ["u", "u_new"] + list(model._state_names)
+
+    def __enter__(self):
+        d = self.model.__dict__
+        for n in self.names:
+            d[n] = self.model._dev[n].cpu().numpy()
+        return self
+
+    def __exit__(self, *exc):
+        for n in self.names:
+            self.model.__dict__.pop(n, None)
+        return False
 
 
 class _Segment:

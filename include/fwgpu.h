@@ -52,6 +52,13 @@ extern "C" {
 #define FW_DEV_TIP_OVERFLOW 16  /* more spiral tips than the tracker holds  */
 #define FW_DEV_NONFINITE 32     /* a myocyte's potential became inf or NaN  */
 
+/* fw_step_args.debug_flags (testing the error paths without a fault):
+ * FW_DEBUG_FORCE_TIMEOUT makes the TMA kernels treat their first pipeline
+ * wait as timed out after the awaited copy has in fact arrived, so the
+ * timeout exit (status bit, waits for copies in flight, early return) runs
+ * on a healthy GPU.  The results of such a call are not defined. */
+#define FW_DEBUG_FORCE_TIMEOUT 1
+
 /* ------------------------------------------------------------ enumerations */
 enum fw_model {
     FW_MODEL_AP = 1,   /* Aliev-Panfilov       cpuwave2D/model/aliev_panfilov_2d.py  */
@@ -262,6 +269,8 @@ typedef struct fw_step_args {
     int32_t n_tip;
     fw_ecg_tracker ecg[FW_MAX_ECG];
     fw_tip_tracker tip[FW_MAX_TIP];
+    int32_t debug_flags; /* 0 in normal use; FW_DEBUG_* bits for tests      */
+    int32_t reserved2;
 } fw_step_args;
 
 /* A planned batch of tissues (fw_batch_plan).  Host-side handle; the
@@ -398,8 +407,10 @@ FW_API int fw_batch_run(const fw_batch *b, void *scratch, int64_t offset,
  * arrays and the plan buffer from another runtime and has no allocator of
  * its own for the device, or a program that fixes its device memory at
  * set-up.  The tile counters then live in a fixed array inside the library
- * (256 bytes per device; a batch needing more scratch is rejected with
- * FW_ERR_ARG).  The call allocates nothing.  The first call on a device does
+ * (256 bytes per device).  A batch's scratch has a fixed size
+ * (fw_batch_scratch_size), so the limit is checked when the library is
+ * compiled; a NULL or empty plan and a negative offset or step count are
+ * rejected with FW_ERR_ARG.  The call allocates nothing.  The first call on a device does
  * a one-time set-up (looks up the array's device address and zeroes it on
  * `stream`), so make that first call before any stream capture.  All calls
  * on one device share the array: calls whose launches may overlap (other

@@ -15,10 +15,9 @@ import cases
 
 pytestmark = pytest.mark.gpu
 
-# Both entry points launch the same kernel on the same inputs, so the results
-# are expected to be identical; the tolerance only allows for nothing more
-# than float32 rounding noise.
-ATOL = 1e-6
+# Both entry points launch the same kernel on the same plan, so the results
+# must be identical bit for bit: a tile counter left non-zero by an earlier
+# call would shift the tiles and show up here.
 
 
 @pytest.fixture(scope="module")
@@ -99,9 +98,37 @@ def test_noalloc_matches_scratch_entry(env):
     for (mr, objs_r), (mg, objs_g) in zip(ref, got):
         assert mr.step == mg.step == 2 * sum(steps)
         for name in ["u"] + list(mr._state_names):
-            np.testing.assert_allclose(getattr(mg, name), getattr(mr, name),
-                                       rtol=0, atol=ATOL, err_msg=name)
+            assert np.array_equal(getattr(mg, name), getattr(mr, name)), name
         for tr, tg in zip(objs_r, objs_g):
-            np.testing.assert_allclose(tg.output, tr.output, rtol=0,
-                                       atol=ATOL)
+            assert np.array_equal(tg.output, tr.output)
         assert np.any(getattr(mg, "u") != 0)
+
+
+def test_noalloc_rejects_bad_arguments(env):
+    """A NULL or empty plan and negative offsets or step counts come back
+    as FW_ERR_ARG with a message, before any device work.  (The scratch a
+    batch needs has a fixed size, which the library checks against the
+    fixed array when it is compiled, so no call can ask for more.)"""
+    _ffi, _ = env
+    lib = _ffi.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    assert lib.fw_batch_run_noalloc(None, 0, 4, ctypes.c_void_p(stream)) == -1
+    assert b"empty plan" in lib.fw_last_error()
+    b = _ffi.Batch()
+    assert lib.fw_batch_run_noalloc(ctypes.byref(b), 0, 4,
+                                    ctypes.c_void_p(stream)) == -1
+    ref = _build(env[1])[:1]
+    seg = ref[0][0]._prepare_segment(8)
+    ptrs = (ctypes.c_void_p * 1)(ctypes.addressof(seg.args))
+    n_begin = (ctypes.c_int64 * 1)(seg.n0)
+    size = ctypes.c_int64()
+    _ffi.call("fw_batch_plan_size", ptrs, 1, ctypes.byref(size))
+    plan = torch.empty(size.value, dtype=torch.uint8, device="cuda")
+    _ffi.call("fw_batch_plan", ptrs, 1, n_begin, plan.data_ptr(), size.value,
+              ctypes.byref(b), stream)
+    assert lib.fw_batch_run_noalloc(ctypes.byref(b), -1, 4,
+                                    ctypes.c_void_p(stream)) == -1
+    assert lib.fw_batch_run_noalloc(ctypes.byref(b), 0, -4,
+                                    ctypes.c_void_p(stream)) == -1
+    assert b"negative" in lib.fw_last_error()
+    torch.cuda.synchronize()
