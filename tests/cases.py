@@ -254,3 +254,30 @@ def models_extra(name, dim):
     gold["act_t"] = g[f"{name}{dim}_act_t"]
     gold.update({f"mv_{v}": g[f"{name}{dim}_mv_{v}"] for v in ["u", var]})
     return case, gold
+
+
+def detailed_long(name, dim):
+    """TP06 ('tp06') or Courtemanche ('crn') on the 10 x 10 anisotropic
+    fibrotic sheet (2D) or the 6 x 6 x 5 anisotropic block (3D), current S1
+    on the first columns, 10^4 steps (t = 100 ms) through the upstroke into
+    the plateau; u at two cells every 100 steps."""
+    g = load("detailed_long")
+    if dim == 2:
+        case = dict(model=name, mesh=g["mesh2"], fibers=g["fib2"],
+                    stencil="aniso9", dt=0.01, dr=0.25, t_max=100,
+                    stims=[dict(kind="current", t=0, value=80, duration=1.0,
+                                box=[(0, 10), (0, 3)])],
+                    trackers=[dict(kind="probe", cells=[[4, 4], [7, 6]],
+                                   vars=["u"], step=100)])
+    else:
+        case = dict(model=name, mesh=g["mesh3"], fibers=g["fib3"],
+                    stencil="aniso19", dt=0.01, dr=0.25, t_max=100,
+                    stims=[dict(kind="current", t=0, value=80, duration=1.0,
+                                box=[(0, 6), (0, 3), (0, 5)])],
+                    trackers=[dict(kind="probe", cells=[[3, 3, 2], [4, 2, 3]],
+                                   vars=["u"], step=100)])
+    key = f"{name}{dim}"
+    gold = {v: g[f"{key}_{v}"] for v in MODEL_VARS[name]}
+    gold["mv_u"] = g[f"{key}_mv_u"]
+    gold["step"] = int(g[f"{key}_step"])
+    return case, gold

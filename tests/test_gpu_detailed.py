@@ -63,6 +63,27 @@ def test_detailed_f64_vs_reference(gc, name, dim):
         assert np.all(r["cai"] == 0.00007)   # frozen in the reference
 
 
+# The gate for float64 on the potential: max |dV| <= 1e-9 mV after 10^4
+# steps through an action potential, absolute, everywhere in the tissue.
+LONG_U_ATOL = 1e-9
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("name", ["tp06", "crn"])
+def test_detailed_f64_long_absolute(gc, name, dim):
+    case, g = cases.detailed_long(name, dim)
+    r = gc.run(case)
+    assert r["step"] == g["step"] == 10000
+    du = float(np.max(np.abs(r["u"] - g["u"])))
+    dmv = float(np.max(np.abs(r["trackers"][0]["u"] - g["mv_u"])))
+    print(f"{name} {dim}D float64, 10^4 steps: max|dV| {du:.3e} mV "
+          f"(field), {dmv:.3e} mV (probes)")
+    assert du <= LONG_U_ATOL, du
+    assert dmv <= LONG_U_ATOL, dmv
+    for v in cases.MODEL_VARS[name][1:]:
+        assert _rel_err(r[v], g[v]) < F64_RTOL, v
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("name", ["tp06", "crn"])
 def test_detailed_f32_close_to_f64(gc, name, dim):

@@ -147,6 +147,29 @@ def test_detailed_models(oracle, name, dim):
         assert np.all(r["cai"] == 0.00007)
 
 
+# The absolute gate on the potential for float64 runs of the detailed
+# models: max |dV| <= 1e-9 mV after 10^4 steps through an action potential.
+LONG_U_ATOL = 1e-9
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("name", ["tp06", "crn"])
+def test_detailed_models_long(oracle, name, dim):
+    """10^4 steps through the upstroke: the oracle's potential stays within
+    1e-9 mV of the reference's everywhere, and every state variable within
+    1e-9 relative."""
+    case, g = cases.detailed_long(name, dim)
+    r = oracle.run(case)
+    assert r["step"] == g["step"] == 10000
+    assert g["u"].max() > 0, "the case must fire an action potential"
+    du = float(np.max(np.abs(r["u"] - g["u"])))
+    assert du <= LONG_U_ATOL, du
+    dmv = float(np.max(np.abs(r["trackers"][0]["u"] - g["mv_u"])))
+    assert dmv <= LONG_U_ATOL, dmv
+    for v in cases.MODEL_VARS[name][1:]:
+        assert _rel_err(r[v], g[v]) < DETAILED_RTOL, v
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 def test_ecg_bitwise(oracle, dim):
     """compute_ecg after the diffusion kernel, every tracked step."""
