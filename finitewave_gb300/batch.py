@@ -18,7 +18,7 @@ import ctypes
 import numpy as np
 import torch
 
-from . import _ffi
+from . import _ffi, stimulation, tracker
 from .model import _MAX_SEGMENT
 from .tracker import (ActivationTime2DTracker, LocalActivationTime2DTracker)
 
@@ -63,10 +63,16 @@ class TissueBatch:
             else []
         n_at = sum(isinstance(t, ActivationTime2DTracker) for t in trs)
         n_lat = sum(isinstance(t, LocalActivationTime2DTracker) for t in trs)
-        if n_at > 1 or n_lat > 1 or n_at + n_lat != len(trs):
+        if (n_at > 1 or n_lat > 1 or n_at + n_lat != len(trs) or
+                not all(tracker.is_native(t) for t in trs)):
             raise ValueError(f"{name}: a batched tissue takes at most one "
                              "activation-time and one local-activation-time "
                              "tracker, and no probe trackers")
+        stims = model.stim_sequence.sequence if model.stim_sequence else []
+        if not all(stimulation.is_native(s) for s in stims):
+            raise ValueError(f"{name}: a batched tissue takes only this "
+                             "package's stimulus classes (a stimulus with "
+                             "its own stimulate() needs model.run())")
         if not model._fused_ok():
             raise ValueError(f"{name}: u and u_new must be equal at the "
                              "non-myocyte nodes")

@@ -29,6 +29,38 @@ class Stim:
     def update_status(self, model):
         self.passed = model.t >= (self.t + self.duration)
 
+    def stimulate(self, model):
+        """Apply this stimulus once to ``model.u`` on the device (the
+        reference's ``Stim.stimulate``).  The run loop calls it only on the
+        steps whose stimuli run on the host, in the sequence's order, because
+        a stimulus of another kind (a user subclass with its own
+        ``stimulate``) is due on that step; on every other step the stimulus
+        is applied inside the kernels.  Same arithmetic as the kernels:
+        nodes of the region with mesh == 1, u = value (voltage) or
+        u = min(u + dt * current, u_max) (current)."""
+        lo, hi, mask = self._region(model)
+        kind, value, has_umax, u_max = self._kind_value(
+            model, self._host_application())
+        if any(b <= a for a, b in zip(lo, hi)):
+            return
+        box = tuple(slice(a, b) for a, b in zip(lo, hi))
+        u = model._dev["u"][box]
+        sel = model._mesh_d[box] == 1
+        if mask is not None:
+            sel &= mask[box] != 0
+        if kind == _ffi.STIM_VOLTAGE:
+            u.masked_fill_(sel, value)
+        else:
+            x = u + value
+            if has_umax:
+                x = torch.where(x > u_max, torch.full_like(x, u_max), x)
+            u.copy_(torch.where(sel, x, u))
+        model._nonmyo_equal = None
+
+    def _host_application(self):
+        """Index of the application made by a host-side ``stimulate``."""
+        return 0
+
     # -- lowering -------------------------------------------------------
     def _region(self, model):
         """(lo, hi, mask_tensor_or_None) in grid coordinates."""
@@ -81,6 +113,16 @@ class StimCurrent(Stim):
         return (_ffi.STIM_CURRENT, float(model.dt * self.curr_value),
                 int(u_max is not None),
                 float(u_max) if u_max is not None else 0.0)
+
+
+def is_native(stim):
+    """True when the kernels apply `stim` themselves: one of this package's
+    stimulus classes whose region and value the library understands, and
+    whose ``stimulate`` is not replaced by a subclass.  Any other object
+    with the reference's interface (``t``, ``passed``, ``initialize``,
+    ``stimulate``, ``update_status``) runs on the host."""
+    return (isinstance(stim, Stim) and type(stim)._region is not Stim._region
+            and type(stim).stimulate is Stim.stimulate)
 
 
 class StimSequence:
@@ -272,6 +314,11 @@ class StimVoltageListMatrix3D(StimVoltage):
 
     def _kind_value(self, model, k):
         return _ffi.STIM_VOLTAGE, float(self.volt_value[k]), 0, 0.0
+
+    def _host_application(self):
+        k = self.step
+        self.step += 1
+        return k
 
     def _windows(self, ts, n0):
         out = []

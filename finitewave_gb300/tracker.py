@@ -32,6 +32,22 @@ class Tracker:
     def initialize(self, model):
         raise NotImplementedError
 
+    def _track(self):
+        """Record one sample (the reference's abstract ``Tracker._track``).
+        This package's own trackers record inside the kernels instead; a
+        user subclass that implements ``_track`` runs on the host."""
+        raise NotImplementedError
+
+    def track(self):
+        """Call ``_track`` on the steps where the tracker is active
+        (core/tracker/tracker.py:70-83): start_time <= t <= end_time and
+        step % self.step == 0."""
+        if self.start_time > self.model.t or self.model.t > self.end_time:
+            return
+        if self.model.step % self.step != 0:
+            return
+        self._track()
+
     def clone(self):
         return copy.deepcopy(self)
 
@@ -507,3 +523,18 @@ class Period2DTracker(LocalActivationTime2DTracker):
 
 class Period3DTracker(Period2DTracker):
     """(cpuwave3D/tracker/period_3d_tracker.py)"""
+
+
+_NATIVE = (ActivationTime2DTracker, LocalActivationTime2DTracker,
+           _ProbeTracker, ECG2DTracker, SpiralWaveCore2DTracker)
+
+
+def is_native(tracker):
+    """True when the kernels record `tracker` themselves: one of this
+    package's tracker classes, with neither ``track`` nor ``_track``
+    replaced by a subclass.  Any other tracker with the reference's
+    interface (``initialize``, ``track`` / ``_track``, ``start_time``,
+    ``end_time``, ``step``) runs on the host."""
+    return (isinstance(tracker, _NATIVE) and
+            type(tracker)._track is Tracker._track and
+            type(tracker).track is Tracker.track)

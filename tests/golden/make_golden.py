@@ -461,6 +461,127 @@ def case_courtemanche(fw):
     return out
 
 
+def case_detailed_long(fw):
+    """TP06 and Courtemanche, 2D and 3D, 10^4 steps (t = 0 .. 100 ms at
+    dt = 0.01) from a current S1 through the upstroke into the plateau, on
+    small fibrotic anisotropic tissues; the whole u field and every state
+    variable at the end, and u at two cells every 100 steps."""
+    out = {}
+    rng = np.random.default_rng(909)
+    mesh2 = _fibrosis(rng, (10, 10), 0.1)
+    fib2 = _seeded_fibers_2d(rng, (10, 10))
+    mesh3 = _fibrosis(rng, (6, 6, 5), 0.1)
+    fib3 = _seeded_fibers_3d(rng, (6, 6, 5))
+    out["mesh2"], out["fib2"], out["mesh3"], out["fib3"] = (mesh2, fib2,
+                                                           mesh3, fib3)
+    for name in ("tp06", "crn"):
+        for dim in (2, 3):
+            cls = {("tp06", 2): fw.TP062D, ("tp06", 3): fw.TP063D,
+                   ("crn", 2): fw.Courtemanche2D,
+                   ("crn", 3): fw.Courtemanche3D}[(name, dim)]
+            model = cls()
+            ss = fw.StimSequence()
+            if dim == 2:
+                tissue = fw.CardiacTissue2D((10, 10))
+                tissue.mesh = mesh2.copy()
+                tissue.fibers = fib2
+                ss.add_stim(fw.StimCurrentCoord2D(0, 80, 1.0, 0, 10, 0, 3))
+            else:
+                tissue = fw.CardiacTissue3D((6, 6, 5))
+                tissue.mesh = mesh3.copy()
+                tissue.fibers = fib3
+                ss.add_stim(fw.StimCurrentCoord3D(0, 80, 1.0, 0, 6, 0, 3,
+                                                  0, 5))
+            model.dt, model.dr, model.t_max = 0.01, 0.25, 100
+            model.prog_bar = False
+            model.cardiac_tissue = tissue
+            model.stim_sequence = ss
+            tr = (fw.MultiVariable2DTracker() if dim == 2
+                  else fw.MultiVariable3DTracker())
+            tr.cell_ind = ([[4, 4], [7, 6]] if dim == 2
+                           else [[3, 3, 2], [4, 2, 3]])
+            tr.var_list = ["u"]
+            tr.step = 100
+            for var in tr.var_list:  # see case_tp06
+                if var not in model.__dict__:
+                    setattr(model, var, None)
+            _attach(fw, model, [tr])
+            model.run()
+            key = f"{name}{dim}"
+            for var in model.state_vars:
+                out[f"{key}_{var}"] = getattr(model, var)
+            out[f"{key}_mv_u"] = tr.output["u"]
+            out[f"{key}_step"] = model.step
+    return out
+
+
+def plugin_classes(Stim, Tracker):
+    """A user stimulus and a user tracker written against the reference's
+    plug-in interface (Stim.stimulate, Tracker._track), built on the given
+    base classes, so that the test can define the same two classes on the
+    GPU package's bases."""
+
+    class RestimulateWhenQuiet(Stim):
+        """While active: u = 1 on rows 1..3 whenever node (15, 15) is
+        below 0.1; counts its firings."""
+
+        def __init__(self, time, duration):
+            super().__init__(time, duration)
+            self.count = 0
+
+        def initialize(self, model):
+            self.count = 0
+
+        def stimulate(self, model):
+            if model.u[15, 15] < 0.1:
+                model.u[1:4, 1:-1] = 1.0
+                self.count += 1
+
+    class PatchTracker(Tracker):
+        """Per active step: step, t, the sums of u and u_new over a 3 x 3
+        patch, and v at one node read through the model's __dict__."""
+
+        def initialize(self, model):
+            self.model = model
+            self.output = []
+
+        def _track(self):
+            m = self.model
+            self.output.append([m.step, m.t, float(m.u[3:6, 3:6].sum()),
+                                float(m.u_new[3:6, 3:6].sum()),
+                                float(m.__dict__["v"][4, 4])])
+
+    return RestimulateWhenQuiet, PatchTracker
+
+
+def case_plugins(fw):
+    """Aliev-Panfilov 2D, 32 x 32 isotropic, float64: a planar S1, the user
+    stimulus above from t = 30 for 2 time units, the user tracker every 50
+    steps from t = 5 and an activation-time tracker; t = 60."""
+    Restim, Patch = plugin_classes(fw.Stim, fw.Tracker)
+    n = 32
+    tissue = fw.CardiacTissue2D((n, n))
+    model = fw.AlievPanfilov2D()
+    model.dt, model.dr, model.t_max = 0.01, 0.25, 60
+    model.prog_bar = False
+    model.cardiac_tissue = tissue
+    ss = fw.StimSequence()
+    ss.add_stim(fw.StimVoltageCoord2D(0, 1.0, 0, n, 1, 5))
+    rs = Restim(30, 2.0)
+    ss.add_stim(rs)
+    model.stim_sequence = ss
+    pt = Patch()
+    pt.start_time = 5
+    pt.step = 50
+    at = fw.ActivationTime2DTracker()
+    at.threshold = 0.5
+    _attach(fw, model, [pt, at])
+    model.run()
+    return {"u": model.u, "v": model.v, "act_t": at.output,
+            "patch": np.asarray(pt.output, dtype=np.float64),
+            "restim_count": rs.count, "step": model.step}
+
+
 def case_fibrosis(fw):
     """Seeded diffuse fibrosis patterns, 2D and 3D, whole mesh and boxes."""
     out = {}
@@ -659,6 +780,8 @@ CASES = {
     "stimuli": case_stimuli,
     "tp06": case_tp06,
     "courtemanche": case_courtemanche,
+    "detailed_long": case_detailed_long,
+    "plugins": case_plugins,
     "fibrosis": case_fibrosis,
     "ecg": case_ecg,
     "tips": case_tips,

@@ -510,3 +510,67 @@ def test_tissue_mesh_rules():
     t3 = fg.CardiacTissue3D((4, 5, 6))
     assert t3.mesh.sum() == 2 * 3 * 4
     assert (t3.mesh[0] == 0).all() and (t3.mesh[:, :, -1] == 0).all()
+
+
+def test_plugin_classification_and_host_steps():
+    """User subclasses with their own ``stimulate`` / ``_track`` / ``track``
+    run on the host; this package's classes run in the kernels.  The run
+    loop finds the next step on which a host plug-in is due with the
+    reference's rules (stim_sequence.py:65-77, tracker.py:70-83)."""
+    import finitewave_gb300 as fg
+    from finitewave_gb300 import stimulation, tracker
+
+    class MyStim(fg.Stim):
+        def initialize(self, model):
+            pass
+
+        def stimulate(self, model):
+            pass
+
+    class MyCoord(fg.StimVoltageCoord2D):
+        def stimulate(self, model):
+            pass
+
+    class MyTracker(fg.Tracker):
+        def initialize(self, model):
+            self.model = model
+
+        def _track(self):
+            pass
+
+    class MyAT(fg.ActivationTime2DTracker):
+        def _track(self):
+            pass
+
+    class EveryStep(fg.Tracker):
+        def initialize(self, model):
+            self.model = model
+
+        def track(self):
+            pass
+
+    assert stimulation.is_native(fg.StimVoltageCoord2D(0, 1, 0, 5, 0, 5))
+    assert stimulation.is_native(fg.StimCurrentMatrix2D(0, 1, 1,
+                                                        np.ones((4, 4))))
+    assert not stimulation.is_native(MyStim(1.0))
+    assert not stimulation.is_native(MyCoord(0, 1, 0, 5, 0, 5))
+    assert tracker.is_native(fg.ActivationTime2DTracker())
+    assert tracker.is_native(fg.MultiVariable2DTracker())
+    assert tracker.is_native(fg.Period2DTracker())
+    assert not tracker.is_native(MyTracker())
+    assert not tracker.is_native(MyAT())
+    assert not tracker.is_native(EveryStep())
+
+    m = fg.AlievPanfilov2D()
+    m.dt, m.t, m.step = 0.01, 0.0, 0
+    s = MyStim(0.5, 0.1)
+    assert m._steps_before_host(200, [s], []) == 50
+    s.passed = True
+    assert m._steps_before_host(200, [s], []) == 200
+    tr = MyTracker()
+    tr.start_time, tr.step = 0.3, 7
+    # first step n with t_n >= 0.3 and n % 7 == 0: t_35 = 0.35 (t_28 < 0.3)
+    assert m._steps_before_host(200, [], [tr]) == 35
+    m.step, m.t = 35, 0.35
+    assert m._steps_before_host(200, [], [tr]) == 0
+    assert m._steps_before_host(200, [], [EveryStep()]) == 0
