@@ -32,16 +32,27 @@ rotating -60..+60 degrees through the depth, AsymmetricStencil3D, S1-S2,
 16 probes), plain form, float32 with float64 ion concentrations next to
 float64.
 
-``serving``: a trace of simulation requests (Poisson arrivals at 50/s;
-TP06 / Courtemanche; 2D tissues and 3D left-ventricle shells; float32 with
-float64 concentrations) served in real time by SimulationServer under an HBM
-budget: p50 / p99 latency, queueing and service times, myocyte-steps/s.
+``serving``: a trace of 40 simulation requests (Poisson arrivals at 50/s;
+TP06 / Courtemanche; 2D tissues of side 256-2048 and 3D left-ventricle
+shells on 128^3-256^3 grids; float32 with float64 concentrations; 20-80 ms
+of simulated time each, 1/25 of the configuration's 500-2000 ms, which
+``--serving-full`` serves) in real time by SimulationServer under an HBM
+budget, the requests' chunks on several streams at once: p50 / p99
+latency, queueing and service times, myocyte-steps/s and the overlap of
+the requests on the device.
 
 ``accuracy_f32_vs_f64``: the float32 forms against the float64 plain form
-on an Aliev-Panfilov 1024^2 S1-S2 run (the 4096^2 generator, t = 120) and a
-TP06 192^2 run through one action potential (350 ms): max |dV|, activation
-and local-activation time errors in steps, APD90 error at 16 probes,
-conduction-velocity error in percent.
+on the headline 4096^2 S1-S2 workload past the S2 into the re-entry
+(t = 200 by default, ``--accuracy-tmax``), on the TP06 slab's generator at
+128 x 128 x 16 through one beat (450 ms) and on a TP06 192^2 sheet through
+one action potential (350 ms): max |dV|, activation and local-activation
+time errors in steps, APD90 error at 16 probes, conduction-velocity error in
+percent, and whether the thresholds (activation within one step on 99.9 %
+of the myocytes, APD90 within 0.5 ms) hold.
+
+The timed window of the headline starts after an untimed lead-in of 3200
+steps (``--lead-in``), so it runs after the S2 (step 3100) with both waves
+in the tissue.
 
 ``--impl reference`` times the reference's algorithm on the host cores: the
 C restatement of its numba kernels (oracle/fw_oracle.c, OpenMP over all
@@ -169,7 +180,7 @@ def run_batched(args, fg, torch, reps):
     myo = [int(m._myo_d.sum().item()) for m in models]
     b_alg = sum(B_ALG_BATCH[(s["model"], "aniso9" if s["aniso"] else "iso5")]
                 * k for s, k in zip(specs, myo)) / sum(myo)
-    batch = fg.TissueBatch(models)
+    batch = fg.TissueBatch(models, kernel=args.batch_kernel)
     chunk = args.chunk
 
     def advance(steps):
@@ -208,6 +219,7 @@ def run_batched(args, fg, torch, reps):
     kms = e0.elapsed_time(e1)
     kl = L.fw_launch_count() - kl0
     kernel_value = reps.whole_job(sum(myo) * chunk, kms / 1e3)
+    batch_kernel = batch._batch.kernel
     del batch, models
     torch.cuda.empty_cache()
 
@@ -235,7 +247,9 @@ def run_batched(args, fg, torch, reps):
             "myocytes": sum(myo), "time_steps_per_bench_step": chunk,
             "bench_steps": k_b, "launches": int(launches),
             "ms_per_step": 1e3 * el / k_b,
-            "kernel": {"name": "k_batch", "value": kernel_value,
+            "kernel": {"name": ("k_batch_tma" if batch_kernel == 2
+                                else "k_batch"),
+                       "value": kernel_value,
                        "ms_per_launch": kms / max(1, kl),
                        "time_steps_per_launch": chunk / max(1, kl)},
             "fp64_plain": {"value": fp64_value, "unit": UNIT,
@@ -346,7 +360,8 @@ def run_tp06_slab(args, fg, torch, reps):
 # serving trace: Poisson arrivals of TP06 / Courtemanche requests
 SERVE_RATE = 50.0          # requests per second
 SERVE_REQUESTS = 40
-SERVE_MS = (5.0, 20.0)     # simulated time per request (ms), scaled down
+SERVE_MS = (20.0, 80.0)    # simulated time per request (ms): 1/25 of the
+SERVE_MS_FULL = (500.0, 2000.0)  # configuration's 500-2000 ms
 
 
 def lv_shell(n, wall, rng):
@@ -377,29 +392,30 @@ def lv_shell(n, wall, rng):
     return mesh, fib
 
 
-def serving_trace(fg, n_requests=SERVE_REQUESTS, seed=SEED):
-    """The serving configuration, scaled to finish in seconds: Poisson
-    arrivals at 50 requests/s; 70 % 2D tissues with side U[256, 2048], 30 %
-    3D left-ventricle shells on 64^3..128^3 grids (wall 8-16 nodes, fibers
-    rotating +-60 deg transmurally); model TP06 or Courtemanche; 5-20 ms of
-    simulated time each (the full configuration's 500-2000 ms is two orders
-    of magnitude more work than one GPU serves in minutes); float32 state
-    with float64 concentrations; a current stimulus at t = 0 and an
-    activation-time tracker (threshold -20 mV)."""
+def serving_trace(fg, n_requests=SERVE_REQUESTS, seed=SEED, ms=SERVE_MS):
+    """The serving configuration: Poisson arrivals at 50 requests/s; 70 % 2D
+    tissues with side U[256, 2048], 30 % 3D left-ventricle shells on
+    128^3..256^3 grids (wall 8-16 nodes, fibers rotating +-60 deg
+    transmurally); model TP06 or Courtemanche; simulated time per request
+    uniform in `ms` (by default 20-80 ms, 1/25 of the configuration's
+    500-2000 ms, so that the trace is served in seconds; ``--serving-full``
+    serves the configuration's own durations); float32 state with float64
+    concentrations; a current stimulus at t = 0 and an activation-time
+    tracker (threshold -20 mV)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     reqs = []
     for i in range(n_requests):
         t += rng.exponential(1.0 / SERVE_RATE)
         tp06 = bool(rng.integers(2))
-        dur = float(rng.uniform(*SERVE_MS))
+        dur = float(rng.uniform(*ms))
         if rng.random() < 0.7:
             side = int(rng.integers(256, 2049))
             tissue = fg.CardiacTissue2D((side, side))
             model = fg.TP062D() if tp06 else fg.Courtemanche2D()
             stim = fg.StimCurrentCoord2D(0, 100, 1.0, 0, side, 1, 6)
         else:
-            n = int(rng.integers(64, 129))
+            n = int(rng.integers(128, 257))
             wall = int(rng.integers(8, 17))
             mesh, fib = lv_shell(n, wall, rng)
             tissue = fg.CardiacTissue3D((n, n, n))
@@ -429,7 +445,8 @@ def serving_trace(fg, n_requests=SERVE_REQUESTS, seed=SEED):
 
 def run_serving(args, fg, torch, reps):
     """The serving trace through SimulationServer in real time."""
-    reqs = serving_trace(fg, args.serving_requests)
+    ms = SERVE_MS_FULL if args.serving_full else SERVE_MS
+    reqs = serving_trace(fg, args.serving_requests, ms=ms)
     server = fg.SimulationServer(chunk=args.serving_chunk)
     server.serve(reqs, realtime=True)
     torch.cuda.synchronize()
@@ -438,7 +455,7 @@ def run_serving(args, fg, torch, reps):
              for r in reqs)
     st.update({"unit": UNIT, "requests": len(reqs), "requests_2d": n2,
                "arrival_rate_per_s": SERVE_RATE,
-               "simulated_ms_per_request": list(SERVE_MS),
+               "simulated_ms_per_request": list(ms),
                "chunk_steps": args.serving_chunk,
                "value_note": "myocyte-steps of the completed requests / "
                              "(last finish - first arrival)"})
@@ -497,16 +514,19 @@ def _accuracy_pair(fg, build, probes_at):
     return out
 
 
-def accuracy_ap(fg, n=1024, t_max=120.0):
-    """Aliev-Panfilov 2D n x n, the 4096^2 configuration's generator
-    (fibrosis 0.2, fibers smoothed with sigma = n / 64), S1-S2, to t_max."""
+def accuracy_ap(fg, n=N, t_max=200.0):
+    """Aliev-Panfilov 2D n x n with the headline configuration's generator
+    (fibrosis 0.2, fibers smoothed with sigma = n / 64), S1 at t = 0 and S2
+    on the lower-left quadrant at t = 31, to t_max (past the S2 into the
+    re-entry it induces); activation, local activation (every crossing) and
+    u at 16 seeded myocytes every step."""
     mesh, fibers = workload_inputs(n, sigma=n / 64.0)
 
     def build(prec):
         model, at = build_model(fg, mesh, fibers, prec, None, init=False)
         model.t_max = t_max
         lat = fg.LocalActivationTime2DTracker()
-        lat.threshold, lat.capacity = 0.5, 8
+        lat.threshold, lat.capacity = 0.5, int(t_max // 20) + 4
         model.tracker_sequence.add_tracker(lat)
         pr = fg.MultiVariable2DTracker()
         cells = np.argwhere(mesh == 1)
@@ -561,6 +581,44 @@ def accuracy_tp06(fg, n=192, t_max=350.0):
     return build
 
 
+def accuracy_slab(fg, shape=(128, 128, 16), t_max=450.0):
+    """The TP06 slab configuration's generator (10 % fibrosis, fibers
+    rotating -60..+60 degrees through the depth, AsymmetricStencil3D) at a
+    reduced lateral size, through one beat: the S1 on the first interior
+    layers at 0 ms and no S2, to t_max; activation and local activation at
+    -20 mV and u at the generator's 16 seeded probe myocytes every step."""
+
+    def build(prec):
+        model = tp06_slab(fg, prec, shape)
+        model.t_max = t_max
+        model.stim_sequence.sequence = model.stim_sequence.sequence[:1]
+        pr = model.tracker_sequence.sequence[0]
+        pr.step = 1
+        at = fg.ActivationTime3DTracker()
+        at.threshold = -20.0
+        lat = fg.LocalActivationTime3DTracker()
+        lat.threshold, lat.capacity = -20.0, 4
+        model.tracker_sequence.add_tracker(at)
+        model.tracker_sequence.add_tracker(lat)
+        return model, at, lat, pr
+    return build
+
+
+# north-star accuracy thresholds of the float32 forms against float64
+ACC_AT_FRACTION = 0.999     # activation within one step on this fraction
+ACC_APD90_MS = 0.5          # APD90 error (ms; model time units for AP)
+
+
+def _verdict(r):
+    """Whether an accuracy record meets the thresholds."""
+    ok = r["at_within_1_step"] >= ACC_AT_FRACTION
+    if "lat_within_1_step" in r:
+        ok &= r["lat_within_1_step"] >= ACC_AT_FRACTION
+    if r.get("apd90_max_err") is not None:
+        ok &= r["apd90_max_err"] <= ACC_APD90_MS
+    return bool(ok)
+
+
 def accuracy_batched(fg, torch, n_tissues=16, steps=2000):
     """Local activation times of the batched float32 form (TissueBatch, one
     persistent launch over all tissues) against each tissue's float64 plain
@@ -604,13 +662,26 @@ def run_accuracy(args, fg, torch, reps):
     and local activation time errors in steps, APD90 error at 16 probes,
     conduction-velocity error in percent; and the batched form's local
     activation times against the float64 plain form."""
-    return {"aliev_panfilov_2d_1024": dict(
-                units="normalised u; time in model units",
-                **_accuracy_pair(fg, accuracy_ap(fg), None)),
-            "tp06_2d_192": dict(
-                units="mV; ms",
-                **_accuracy_pair(fg, accuracy_tp06(fg), None)),
-            "batched_16_tissues": accuracy_batched(fg, torch)}
+    out = {"cfg2_4096": dict(
+               grid=[args.grid, args.grid], t_max=args.accuracy_tmax,
+               units="normalised u; time in model units",
+               **_accuracy_pair(fg, accuracy_ap(fg, args.grid,
+                                                args.accuracy_tmax), None)),
+           "cfg3_slab": dict(
+               grid=[128, 128, 16], t_max=450.0, units="mV; ms",
+               note="the 512x512x64 slab's generator at 128x128x16, S1 only "
+                    "(one beat); float64 of the full slab for one beat is "
+                    "~45 min of GPU time",
+               **_accuracy_pair(fg, accuracy_slab(fg), None)),
+           "tp06_2d_192": dict(
+               units="mV; ms",
+               **_accuracy_pair(fg, accuracy_tp06(fg), None)),
+           "batched_16_tissues": accuracy_batched(fg, torch)}
+    for k in ("cfg2_4096", "cfg3_slab", "tp06_2d_192"):
+        out[k]["meets_thresholds"] = _verdict(out[k])
+    out["thresholds"] = {"at_within_1_step_fraction": ACC_AT_FRACTION,
+                         "apd90_max_err_ms": ACC_APD90_MS}
+    return out
 
 
 def peaks():
@@ -791,6 +862,11 @@ def run_gb300(args):
     model, at = build_model(fg, mesh, fibers, "float32", form32)
     model.fused_k = args.fused_k
     model.fused_variant = args.fused_variant
+    # lead-in past the S2 (t = 31), so that the timed steps run the
+    # induced re-entry with both waves in the tissue
+    lead = args.lead_in
+    while lead > 0:
+        lead -= model._run_segment(min(lead, 1000), sync=False)
     for _ in range(W):
         model._run_segment(chunk, sync=False)
     barrier()
@@ -859,6 +935,9 @@ def run_gb300(args):
 
     # --- float64 plain form, same workload ----------------------------------
     m64, _ = build_model(fg, mesh, fibers, "float64", "plain")
+    lead = args.lead_in
+    while lead > 0:
+        lead -= m64._run_segment(min(lead, 1000), sync=False)
     for _ in range(max(1, W // 2)):
         m64._run_segment(chunk, sync=False)
     barrier()
@@ -899,6 +978,7 @@ def run_gb300(args):
                 "workload": WORKLOAD,
                 "grid": [N, N], "myocytes": myo,
                 "time_steps_per_bench_step": chunk, "form": form32 or "auto",
+                "timed_from_step": args.lead_in + W * chunk,
                 "l2": "state larger than L2 (no flush needed)",
                 "parallelism": f"replicas x{world}"},
             "fp64_plain": {"value": fp64_value, "unit": UNIT,
@@ -1040,14 +1120,23 @@ def main():
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched many-tissue measurement")
     ap.add_argument("--batched-tissues", type=int, default=N_TISSUES)
+    ap.add_argument("--batch-kernel", default="tma",
+                    choices=["tma", "cp.async"])
     ap.add_argument("--no-tp06", action="store_true",
                     help="skip the TP06 slab measurement")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the float32 vs float64 accuracy runs")
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the serving trace")
+    ap.add_argument("--accuracy-tmax", type=float, default=200.0,
+                    help="model time of the 4096^2 float32-vs-float64 run")
+    ap.add_argument("--lead-in", type=int, default=3200,
+                    help="untimed time steps before the warm-up: the timed "
+                         "window starts after the S2 (step 3100)")
     ap.add_argument("--serving-requests", type=int, default=SERVE_REQUESTS)
     ap.add_argument("--serving-chunk", type=int, default=500)
+    ap.add_argument("--serving-full", action="store_true",
+                    help="serve the configuration's 500-2000 ms per request")
     ap.add_argument("--only", default=None,
                     choices=[None, "tp06", "batched", "serving",
                              "accuracy"],

@@ -109,12 +109,14 @@ class StepArgs(ctypes.Structure):
                 ("n_ecg", _i32), ("n_tip", _i32),
                 ("ecg", EcgTracker * MAX_ECG),
                 ("tip", TipTracker * MAX_TIP),
-                ("debug_flags", _i32), ("reserved2", _i32)]
+                ("debug_flags", _i32), ("reserved2", _i32),
+                ("pitch", _i64)]
 
 
 class Batch(ctypes.Structure):
     _fields_ = [("plan", _vp), ("n_tissues", _i32), ("n_tiles", _i32),
-                ("ksteps", _i32), ("grid", _i32)]
+                ("ksteps", _i32), ("grid", _i32), ("kernel", _i32),
+                ("reserved", _i32)]
 
 
 class FwError(RuntimeError):
@@ -136,6 +138,7 @@ _SIGS = {
     "fw_model_info": ([_i32, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
                       _i32),
     "fw_state_is_f64": ([_i32, _i32, _i32], _i32),
+    "fw_state_is_pair": ([_i32, _i32, _i32], _i32),
     "fw_build_weights": ([_i32, _i32, _vp, _vp, _f64, _vp, _f64, _f64, _f64,
                           _f64, _f64, _i64, _i64, _i64, _vp, _vp], _i32),
     "fw_diffuse": ([_i32, _i32, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _i64,
@@ -206,3 +209,9 @@ def model_info(model):
 
 def state_is_f64(model, precision, index):
     return bool(load().fw_state_is_f64(model, precision, index))
+
+
+def state_is_pair(model, precision, index):
+    """True when the state variable is a compensated float32 pair (hi, lo)
+    per node."""
+    return bool(load().fw_state_is_pair(model, precision, index))

@@ -25,6 +25,70 @@ from .tracker import (ActivationTime2DTracker, LocalActivationTime2DTracker)
 _BATCH_MODELS = (_ffi.MODEL_AP, _ffi.MODEL_MS, _ffi.MODEL_FK)
 
 
+class _Mirror:
+    """Copies of one model's arrays that the TMA form of the batched kernel
+    reads through tensor maps -- the two potential buffers, the state
+    variables, the myocyte flags and the weights (plus their node-major
+    packing) -- with rows padded to a multiple of 16 nodes (the row pitch a
+    tensor map needs).  The padding columns are non-myocytes holding zero
+    in both potential buffers.  The batch advances the copies; `sync_in`
+    and `sync_out` move the model's state between them and the model's own
+    arrays, and `swap` follows the model's u / u_new exchange."""
+
+    def __init__(self, m):
+        ni, nj = m._shape()
+        self.model, self.nj = m, nj
+        self.pitch = -(-nj // 16) * 16
+        self.weights_src = m.weights
+        dev = m._device()
+        f32 = torch.float32
+        nw = m.weights.shape[0]
+        self.w = torch.zeros((nw, ni, self.pitch), dtype=f32, device=dev)
+        self.w[:, :, :nj] = m.weights.view(nw, ni, nj)
+        nwo = 4 if m.stencil.kind == _ffi.ISO5 else 8
+        self.wpack = torch.empty(ni * self.pitch * nwo, dtype=f32, device=dev)
+        _ffi.call("fw_pack_weights", m.stencil.kind, self.w.data_ptr(),
+                  ni * self.pitch, self.wpack.data_ptr(),
+                  torch.cuda.current_stream(dev).cuda_stream)
+        self.myo = torch.zeros((ni, self.pitch), dtype=torch.int8, device=dev)
+        self.myo[:, :nj] = m._myo_d
+        self.u = [torch.zeros((ni, self.pitch), dtype=f32, device=dev)
+                  for _ in range(2)]
+        self.state = [torch.zeros((ni, self.pitch), dtype=f32, device=dev)
+                      for _ in m._state_names]
+
+    def valid_for(self, m):
+        return m is self.model and m.weights is self.weights_src
+
+    def sync_in(self):
+        m, nj = self.model, self.nj
+        self.u[0][:, :nj].copy_(m._dev["u"])
+        self.u[1][:, :nj].copy_(m._dev["u_new"])
+        for t, name in zip(self.state, m._state_names):
+            t[:, :nj].copy_(m._dev[name])
+
+    def sync_out(self):
+        m, nj = self.model, self.nj
+        m._dev["u"].copy_(self.u[0][:, :nj])
+        m._dev["u_new"].copy_(self.u[1][:, :nj])
+        for t, name in zip(self.state, m._state_names):
+            m._dev[name].copy_(t[:, :nj])
+
+    def swap(self):
+        self.u.reverse()
+
+    def apply(self, a):
+        """Point a tissue's fw_step_args at the copies."""
+        a.u[0], a.u[1] = self.u[0].data_ptr(), self.u[1].data_ptr()
+        for i, t in enumerate(self.state):
+            a.state[i] = t.data_ptr()
+        a.myo = self.myo.data_ptr()
+        a.weights = self.w.data_ptr()
+        a.weights_packed = self.wpack.data_ptr()
+        a.pitch = self.pitch
+        a.fused_variant = 0
+
+
 class TissueBatch:
     """A batch of models run together (see the module docstring).
 
@@ -33,16 +97,32 @@ class TissueBatch:
     a captured CUDA graph -- the launches of a chunk depend only on its
     length and on the plan and scratch buffers (each chunk is planned at
     offset 0 into the same plan buffer), so equal chunks replay one graph
-    and the per-launch host cost disappears."""
+    and the per-launch host cost disappears.  kernel: "tma" (default) runs
+    the TMA pipeline over row-padded copies of the tissues' arrays (made
+    once per model and kept by the batch, about 90 bytes per node), state
+    copied in at the start of run() and out at its end and around host-side
+    commands and state savers; "cp.async" runs the kernel that stages with
+    4-byte asynchronous copies straight from the models' arrays."""
 
-    def __init__(self, models=(), chunk=None, graphs=True):
+    def __init__(self, models=(), chunk=None, graphs=True, kernel="tma"):
+        if kernel not in ("tma", "cp.async"):
+            raise ValueError("kernel must be 'tma' or 'cp.async'")
         self.models = list(models)
         self.chunk = chunk
         self.graphs = graphs
+        self.kernel = kernel
         self._plan = None
         self._scratch = None
         self._batch = None   # the last plan's fw_batch handle
         self._graphs = {}
+        self._mirrors = {}
+
+    def _mirror(self, m):
+        mir = self._mirrors.get(id(m))
+        if mir is None or not mir.valid_for(m):
+            mir = _Mirror(m)
+            self._mirrors[id(m)] = mir
+        return mir
 
     def add(self, model):
         self.models.append(model)
@@ -138,12 +218,22 @@ class TissueBatch:
         remaining = [int(np.ceil((m.t_max - m.t) / m.dt)) for m in ms]
         active = [i for i in range(len(ms)) if remaining[i] > 0]
         stream = torch.cuda.current_stream(dev).cuda_stream
+        tma = self.kernel == "tma"
+        mirrors = [self._mirror(m) for m in ms] if tma else None
+        if tma:
+            for mir in mirrors:
+                mir.sync_in()
         while active:
             limit = min(_MAX_SEGMENT, min(remaining[i] for i in active))
             if self.chunk:
                 limit = min(limit, int(self.chunk))
             n = min(ms[i]._segment_times(limit)[2] for i in active)
             segs = [ms[i]._prepare_segment(n) for i in active]
+            for i, seg in zip(active, segs):
+                if tma:
+                    mirrors[i].apply(seg.args)
+                else:
+                    seg.args.fused_variant = 1
             k = len(segs)
             ptrs = (ctypes.c_void_p * k)(
                 *[ctypes.addressof(s.args) for s in segs])
@@ -160,11 +250,18 @@ class TissueBatch:
             for i, seg in zip(active, segs):
                 m = ms[i]
                 m._finish_segment(seg)
+                if tma and seg.n_seg % 2 == 1:
+                    mirrors[i].swap()
                 remaining[i] -= n
+                host = tma and (m.command_sequence or m.state_saver)
+                if host:
+                    mirrors[i].sync_out()
                 if m.command_sequence:
                     m.command_sequence.execute_next()
                 if m.state_saver:
                     m.state_saver.save()
+                if host:
+                    mirrors[i].sync_in()
                 if m.check_termination():
                     if m.state_saver:
                         m.state_saver.save()
@@ -172,5 +269,8 @@ class TissueBatch:
                 if remaining[i] > 0:
                     still.append(i)
             active = still
+        if tma:
+            for mir in mirrors:
+                mir.sync_out()
         for m in ms:
             m._check_status()

@@ -28,7 +28,7 @@
 #include <mutex>
 #include <vector>
 
-#include "fw_fused_kernel.cuh"
+#include "fw_fused_tma.cuh"
 
 namespace fw {
 namespace batch {
@@ -489,6 +489,379 @@ int64_t tissue_tiles(const fw_step_args *a)
     return ((a->ni + TI - 1) / TI) * ((a->nj + TJ - 1) / TJ);
 }
 
+// ---- the TMA form of the batch (kernel 2) ------------------------------------
+//
+// The single-tissue TMA pipeline (fw_fused_tma.cuh) over the ragged tile
+// list: one persistent 512-thread CTA per SM, two shared-memory stages, the
+// tile computed by the fused kernels' tile code (tma_tile), so a tissue
+// advanced here is bitwise the same as when run alone by k_fused_tma.
+// Everything a tile needs arrives asynchronously: thread 0 issues, for the
+// tile after the current one, one bulk copy of its tissue's launch
+// description (a FusedK kept in the plan, whose per-launch fields
+// k_batch_events fills before each launch) and the TMA copies of its region
+// through the tissue's own tensor maps (also in the plan), all completing
+// on the stage's mbarrier.  Thread 0 takes tile indices from the counter two
+// tiles ahead and reads their list entries one tile ahead, so none of its
+// loads is waited for on the way.  Tissues need rows of a multiple of 16
+// nodes, which the caller provides as a row pitch (fw_step_args.pitch) on
+// copies of the TMA-read arrays.
+
+constexpr int kTmaR = 4;                           // rows per thread
+constexpr int kTmaNT = fused::kTW * (LH / kTmaR);  // 512 threads
+
+struct alignas(128) BTissueT {
+    fused::TmaMaps maps;   // 64-byte aligned tensor maps of this tissue
+    fused::FusedK f;       // launch description (static part from the plan)
+    BWin stim_win[FW_MAX_STIMS];
+    BWin at_win[fused::kMaxFusedAt];
+    BWin lat_win[fused::kMaxFusedLat];
+    float *u[2];
+    int64_t step_base;
+};
+
+// One entry of the TMA form's tile list.
+struct BTileT {
+    int32_t tissue;
+    int32_t key;           // model * 8 + stencil
+    int32_t oi, oj;        // region origin
+};
+
+struct BatchTmaSmem {
+    fused::TmaSmem<LH, 2, 8> t;
+    fused::FusedK f[2];    // launch description of each stage's tile
+    int tile[2];           // the stage's tile index (>= n_tiles: none)
+    int oi[2], oj[2];      // its region origin
+    int key[2];            // model * 8 + stencil, -1 for a skipped tile
+};
+
+// The per-launch fields of every tissue's launch description: step window
+// masks of the stimuli and trackers, first step, step count and the
+// potential buffers.  One warp per tissue.
+__global__ void k_batch_events(BTissueT *__restrict__ tissues, int32_t n,
+                               int64_t koff, int32_t ks, int32_t in_buf)
+{
+    const int i = blockIdx.x * blockDim.y + threadIdx.y;
+    if (i >= n) return;
+    BTissueT &T = tissues[i];
+    fused::FusedK &F = T.f;
+    const int lane = threadIdx.x;
+    const int64_t n0 = T.step_base + koff;
+    if (lane < F.n_stims)
+        F.stims[lane].on =
+            window_bits(n0, ks, T.stim_win[lane].first, T.stim_win[lane].last, 1);
+    if (lane >= 16 && lane - 16 < F.n_at) {
+        const BWin &w = T.at_win[lane - 16];
+        F.at[lane - 16].on = window_bits(n0, ks, w.first, w.last, w.stride);
+    }
+    if (lane >= 24 && lane - 24 < F.n_lat) {
+        const BWin &w = T.lat_win[lane - 24];
+        F.lat[lane - 24].on = window_bits(n0, ks, w.first, w.last, w.stride);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        uint32_t any = 0;
+        for (int s = 0; s < F.n_stims; ++s) any |= F.stims[s].on;
+        F.stim_on = any;
+        F.n0 = n0;
+        F.ksteps = ks;
+        F.u_in = T.u[in_buf];
+        F.u_out = T.u[in_buf ^ 1];
+    }
+}
+
+__device__ __forceinline__ void tensormap_acquire(const void *map)
+{
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes,
+                                          uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1], %2, [%3];\n" ::"r"(fused::smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(fused::smem_u32(bar))
+        : "memory");
+}
+
+// Thread 0: stage tile t (list entry bt) into stage sg.
+__device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
+                                         int32_t n_tiles, int32_t n_tissues,
+                                         int32_t in_buf, BatchTmaSmem &S, int sg,
+                                         int t, BTileT bt)
+{
+    S.tile[sg] = t;
+    if (t >= n_tiles) return;
+    uint64_t *bar = &S.t.bar[sg];
+    fused::fence_proxy_async();
+    if (bt.tissue < 0 || bt.tissue >= n_tissues) {
+        // a corrupted plan: flag it and complete the stage's phase without
+        // data, so that the tile is skipped
+        S.key[sg] = -1;
+        if (tissues[0].f.status) atomicOr(tissues[0].f.status, FW_DEV_BATCH_FAULT);
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(
+                         fused::smem_u32(bar))
+                     : "memory");
+        return;
+    }
+    const BTissueT &T = tissues[bt.tissue];
+    S.key[sg] = bt.key;
+    S.oi[sg] = bt.oi;
+    S.oj[sg] = bt.oj;
+    const fused::TmaMaps &M = T.maps;
+    tensormap_acquire(&M.w);
+    tensormap_acquire(&M.myo);
+    tensormap_acquire(&M.u[in_buf]);
+    tensormap_acquire(&M.s[0]);
+    tensormap_acquire(&M.s[1]);
+    tensormap_acquire(&M.wc);
+    // one arrive on the stage's barrier announces the region's bytes and
+    // the launch description's, which rides on the same barrier
+    constexpr unsigned kF = (unsigned)sizeof(fused::FusedK);
+    auto &G = S.t.stage[sg];
+    switch (bt.key) {
+    case FW_MODEL_AP * 8 + FW_STENCIL_ISO5:
+    case FW_MODEL_MS * 8 + FW_STENCIL_ISO5:
+        fused::issue_region<KMAX, 1, 4>(M, in_buf, G, bar, bt.oi, bt.oj, kF);
+        break;
+    case FW_MODEL_AP * 8 + FW_STENCIL_ANISO9:
+    case FW_MODEL_MS * 8 + FW_STENCIL_ANISO9:
+        fused::issue_region<KMAX, 1, 8>(M, in_buf, G, bar, bt.oi, bt.oj, kF);
+        break;
+    case FW_MODEL_FK * 8 + FW_STENCIL_ISO5:
+        fused::issue_region<KMAX, 2, 4>(M, in_buf, G, bar, bt.oi, bt.oj, kF);
+        break;
+    default:  // FK, ANISO9 (the plan admits no other key)
+        fused::issue_region<KMAX, 2, 8>(M, in_buf, G, bar, bt.oi, bt.oj, kF);
+        break;
+    }
+    bulk_copy(&S.f[sg], &T.f, kF, bar);
+}
+
+template <class M, int ST>
+__device__ __forceinline__ void batch_tile(BatchTmaSmem &S, int sg, uint32_t own_c,
+                                           uint32_t ring_c)
+{
+    const fused::FusedK &f = S.f[sg];
+    Params<float, M::NP> P;
+#pragma unroll
+    for (int i = 0; i < M::NP; ++i) P.v[i] = f.params[i];
+    fused::tma_tile<M, ST, KMAX, LH, kTmaR>(f, S.t.stage[sg], S.t, S.oi[sg], S.oj[sg],
+                                           own_c, ring_c, P);
+}
+
+__global__ void __launch_bounds__(kTmaNT, 1)
+    k_batch_tma(const BTissueT *__restrict__ tissues, const BTileT *__restrict__ tiles,
+                int32_t n_tiles, int32_t n_tissues, int32_t in_buf, uint32_t *scratch)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned mis = fused::smem_u32(smem_raw) & 127u;
+    BatchTmaSmem &S =
+        *reinterpret_cast<BatchTmaSmem *>(smem_raw + (mis ? 128u - mis : 0u));
+    const int tid = threadIdx.x;
+    uint32_t own_c, ring_c;
+    fused::strip_masks<KMAX, LH, kTmaR>(tid % fused::kTW, (tid / fused::kTW) * kTmaR,
+                                        own_c, ring_c);
+    const BTileT none{-1, -1, 0, 0};
+    // thread 0's look-ahead: tile i + 1 (index and entry) and tile i + 2
+    // (index) while tile i is computed
+    int t_next = n_tiles, t_after = n_tiles;
+    BTileT b_next = none;
+    if (tid == 0) {
+        fused::mbar_init(&S.t.bar[0], 1);
+        fused::mbar_init(&S.t.bar[1], 1);
+        fused::mbar_fence_init();
+        const int t0 = (int)atomicAdd(&scratch[0], 1u);
+        if (t0 < n_tiles) {
+            t_next = (int)atomicAdd(&scratch[0], 1u);
+            if (t_next < n_tiles) t_after = (int)atomicAdd(&scratch[0], 1u);
+        }
+        batch_issue(tissues, n_tiles, n_tissues, in_buf, S, 0, t0,
+                    t0 < n_tiles ? tiles[t0] : none);
+        if (t_next < n_tiles) b_next = tiles[t_next];
+    }
+    __syncthreads();
+    unsigned parity = 0u;
+    for (int it = 0;; ++it) {
+        const int sg = it & 1;
+        if (S.tile[sg] >= n_tiles) break;
+        if (tid == 0) {
+            // the other stage's readers finished at the barrier that closed
+            // the previous iteration
+            batch_issue(tissues, n_tiles, n_tissues, in_buf, S, sg ^ 1, t_next,
+                        b_next);
+            t_next = t_after;
+            b_next = t_next < n_tiles ? tiles[t_next] : none;
+            t_after = t_next < n_tiles ? (int)atomicAdd(&scratch[0], 1u) : n_tiles;
+        }
+        const unsigned ph = (parity >> sg) & 1u;
+        const bool arrived = fused::mbar_wait(&S.t.bar[sg], ph);
+        parity ^= 1u << sg;
+        if (__syncthreads_or(!arrived)) {
+            if (tid == 0) {
+                // flag it, then wait (bounded) for the copies in flight
+                if (tissues[0].f.status) atomicOr(tissues[0].f.status, FW_DEV_TIMEOUT);
+                if (!arrived) fused::mbar_wait(&S.t.bar[sg], ph);
+                if (S.tile[sg ^ 1] < n_tiles)
+                    fused::mbar_wait(&S.t.bar[sg ^ 1], (parity >> (sg ^ 1)) & 1u);
+            }
+            break;
+        }
+        switch (S.key[sg]) {
+        case FW_MODEL_AP * 8 + FW_STENCIL_ISO5:
+            batch_tile<ModelAP, FW_STENCIL_ISO5>(S, sg, own_c, ring_c);
+            break;
+        case FW_MODEL_AP * 8 + FW_STENCIL_ANISO9:
+            batch_tile<ModelAP, FW_STENCIL_ANISO9>(S, sg, own_c, ring_c);
+            break;
+        case FW_MODEL_MS * 8 + FW_STENCIL_ISO5:
+            batch_tile<ModelMS, FW_STENCIL_ISO5>(S, sg, own_c, ring_c);
+            break;
+        case FW_MODEL_MS * 8 + FW_STENCIL_ANISO9:
+            batch_tile<ModelMS, FW_STENCIL_ANISO9>(S, sg, own_c, ring_c);
+            break;
+        case FW_MODEL_FK * 8 + FW_STENCIL_ISO5:
+            batch_tile<ModelFK, FW_STENCIL_ISO5>(S, sg, own_c, ring_c);
+            break;
+        case FW_MODEL_FK * 8 + FW_STENCIL_ANISO9:
+            batch_tile<ModelFK, FW_STENCIL_ANISO9>(S, sg, own_c, ring_c);
+            break;
+        default:
+            break;  // skipped (flagged when it was taken)
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&scratch[1], 1u) == gridDim.x - 1) {
+            atomicExch(&scratch[0], 0u);
+            atomicExch(&scratch[1], 0u);
+        }
+    }
+}
+
+constexpr size_t kTmaSmem = sizeof(BatchTmaSmem) + 128;
+static_assert(kTmaSmem <= 232448, "the batched TMA stages exceed 227 KB");
+static_assert(sizeof(fused::FusedK) % 16 == 0 && offsetof(BTissueT, f) % 16 == 0,
+              "the launch description moves as one bulk copy");
+
+inline bool aligned16(const void *p) { return p && ((uintptr_t)p & 15) == 0; }
+
+// The TMA form can take this tissue: rows (the pitch) a multiple of 16
+// nodes, every TMA-read array 16-byte aligned, packed weights.
+bool tma_tissue_ok(const fw_step_args *a)
+{
+    const int64_t pitch = a->pitch ? a->pitch : a->nj;
+    if (pitch < a->nj || pitch % 16 || pitch >= (1 << 30)) return false;
+    if (!aligned16(a->weights_packed) || !aligned16(a->weights) ||
+        !aligned16(a->u[0]) || !aligned16(a->u[1]) || !aligned16(a->myo))
+        return false;
+    int ns = 0, np = 0;
+    fw_model_info(a->model, &ns, &np);
+    for (int q = 0; q < ns; ++q)
+        if (!aligned16(a->state[q])) return false;
+    return fused::tensor_map_encoder() != nullptr;
+}
+
+// Fill one tissue's descriptor of the TMA form.
+int fill_tma_tissue(const fw_step_args *a, int64_t n_begin, BTissueT &T)
+{
+    using namespace fused;
+    const int64_t pitch = a->pitch ? a->pitch : a->nj;
+    const int nwo = a->stencil == FW_STENCIL_ISO5 ? 4 : 8;
+    const int cen = a->stencil == FW_STENCIL_ISO5 ? 2 : 4;
+    int ns = 0, np = 0;
+    fw_model_info(a->model, &ns, &np);
+    bool ok = encode_weights(&T.maps.w, a->weights_packed, nwo, a->nj, a->ni, LH,
+                             pitch) &&
+              encode_2d(&T.maps.myo, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a->myo, a->nj,
+                        a->ni, kBoxB, LH, pitch) &&
+              encode_2d(&T.maps.u[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->u[0],
+                        a->nj, a->ni, kBoxF, LH + 2, pitch) &&
+              encode_2d(&T.maps.u[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->u[1],
+                        a->nj, a->ni, kBoxF, LH + 2, pitch) &&
+              encode_2d(&T.maps.wc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                        (const float *)a->weights + (int64_t)cen * a->ni * pitch,
+                        a->nj, a->ni, kBoxF, LH, pitch);
+    // the map of a second state array exists for every tissue (the kernel
+    // acquires it); models with one state variable map the first twice
+    for (int q = 0; q < 2 && ok; ++q)
+        ok = encode_2d(&T.maps.s[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                       a->state[q < ns ? q : 0], a->nj, a->ni, kBoxF, LH, pitch);
+    if (!ok) {
+        set_error("fw_batch_plan: tensor map encoding failed");
+        return FW_ERR_UNSUPPORTED;
+    }
+    FusedK &f = T.f;
+    f.w = nullptr;
+    f.myo = a->myo;
+    for (int i = 0; i < FW_MAX_STATE; ++i) f.state[i] = a->state[i];
+    for (int i = 0; i < FW_MAX_PARAMS; ++i) f.params[i] = (float)a->params[i];
+    f.dt = (float)a->dt;
+    f.ni = (int32_t)a->ni;
+    f.nj = (int32_t)a->nj;
+    f.pitch = (int32_t)pitch;
+    f.n = a->ni * a->nj;
+    f.tiles_j = (int32_t)((a->nj + TJ - 1) / TJ);
+    f.status = a->status;
+    f.n_stims = a->n_stims;
+    for (int i = 0; i < a->n_stims; ++i) {
+        const fw_stim &St = a->stims[i];
+        FStim &F = f.stims[i];
+        F.on = 0;
+        F.kind = St.kind;
+        F.has_umax = St.has_umax;
+        F.value = (float)St.value;
+        F.u_max = (float)St.u_max;
+        F.lo0 = (int32_t)(St.lo[0] < 0 ? 0 : St.lo[0]);
+        F.hi0 = (int32_t)(St.hi[0] > a->ni ? a->ni : St.hi[0]);
+        F.lo1 = (int32_t)(St.lo[1] < 0 ? 0 : St.lo[1]);
+        F.hi1 = (int32_t)(St.hi[1] > a->nj ? a->nj : St.hi[1]);
+        F.mask = St.mask;
+        T.stim_win[i] = BWin{St.first, St.last, 1};
+    }
+    f.n_at = a->n_at;
+    for (int i = 0; i < a->n_at; ++i) {
+        f.at[i] = FAt{0u, (float)a->at[i].threshold, a->at[i].act_step};
+        T.at_win[i] = BWin{a->at[i].win.first, a->at[i].win.last, a->at[i].win.stride};
+    }
+    f.n_lat = a->n_lat;
+    for (int i = 0; i < a->n_lat; ++i) {
+        const fw_lat_tracker &L = a->lat[i];
+        f.lat[i] = FLat{0u, (float)L.threshold, L.activated, L.cross_steps,
+                        L.cross_count, L.capacity};
+        T.lat_win[i] = BWin{L.win.first, L.win.last, L.win.stride};
+    }
+    f.n_probe = 0;
+    T.u[0] = (float *)a->u[0];
+    T.u[1] = (float *)a->u[1];
+    T.step_base = n_begin;
+    return FW_OK;
+}
+
+// Kernel of a batch: 2 (TMA) when every tissue can take it, unless every
+// tissue asks for cp.async staging (fused_variant 1 or 2); else 1.  A row
+// pitch other than nj needs the TMA kernel.
+int choose_kernel(const fw_step_args *const *tissues, int32_t n, int *kernel)
+{
+    bool tma = true, cp = true, pitched = false;
+    for (int i = 0; i < n; ++i) {
+        const fw_step_args *a = tissues[i];
+        tma &= tma_tissue_ok(a);
+        cp &= a->fused_variant == 1 || a->fused_variant == 2;
+        pitched |= a->pitch != 0 && a->pitch != a->nj;
+    }
+    if (pitched && (!tma || cp)) {
+        set_error("fw_batch: a row pitch other than nj needs the TMA kernel "
+                  "(pitch a multiple of 16 nodes, 16-byte aligned arrays, "
+                  "packed weights)");
+        return FW_ERR_UNSUPPORTED;
+    }
+    *kernel = tma && !cp ? 2 : 1;
+    return FW_OK;
+}
+
 }  // namespace batch
 
 int batch_plan_size(const fw_step_args *const *tissues, int32_t n,
@@ -509,8 +882,14 @@ int batch_plan_size(const fw_step_args *const *tissues, int32_t n,
         set_error("fw_batch_plan_size: too many tiles");
         return FW_ERR_ARG;
     }
-    *bytes = (int64_t)(align_up(sizeof(BTissue) * n, 256) +
-                       sizeof(BTile) * (size_t)n_tiles);
+    int kernel = 0;
+    {
+        int rc = choose_kernel(tissues, n, &kernel);
+        if (rc) return rc;
+    }
+    const size_t desc = kernel == 2 ? sizeof(BTissueT) : sizeof(BTissue);
+    const size_t tile = kernel == 2 ? sizeof(BTileT) : sizeof(BTile);
+    *bytes = (int64_t)(align_up(desc * n, 256) + tile * (size_t)n_tiles);
     return FW_OK;
 }
 
@@ -531,68 +910,82 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
                   (long long)plan_bytes, (long long)need);
         return FW_ERR_ARG;
     }
-    if (((uintptr_t)plan & 15) != 0) {
-        set_error("fw_batch_plan: plan must be 16-byte aligned");
+    int kernel = 1;
+    rc = choose_kernel(tissues, n, &kernel);
+    if (rc) return rc;
+    if (((uintptr_t)plan & (kernel == 2 ? 127 : 15)) != 0) {
+        set_error("fw_batch_plan: plan must be %d-byte aligned",
+                  kernel == 2 ? 128 : 16);
         return FW_ERR_ARG;
     }
-    std::vector<unsigned char> host((size_t)need, 0);
-    BTissue *desc = reinterpret_cast<BTissue *>(host.data());
-    BTile *tl = reinterpret_cast<BTile *>(
-        host.data() + align_up(sizeof(BTissue) * n, 256));
-    int32_t t_count = 0;
-    for (int i = 0; i < n; ++i) {
-        const fw_step_args *a = tissues[i];
-        BHead &T = desc[i].h;
-        T.w = (const float *)a->weights;
-        T.myo = a->myo;
-        T.u[0] = (float *)a->u[0];
-        T.u[1] = (float *)a->u[1];
-        int ns = 0, np = 0;
-        fw_model_info(a->model, &ns, &np);
-        for (int s = 0; s < kMaxState; ++s) T.state[s] = s < ns ? a->state[s] : nullptr;
-        for (int p = 0; p < kMaxParams; ++p) T.params[p] = p < np ? (float)a->params[p] : 0.f;
-        T.dt = (float)a->dt;
-        T.model = a->model;
-        T.stencil = a->stencil;
-        T.ni = (int32_t)a->ni;
-        T.nj = (int32_t)a->nj;
-        T.tiles_j = (int32_t)((a->nj + TJ - 1) / TJ);
-        T.n = a->ni * a->nj;
-        T.step_base = n_begin[i];
-        T.n_stims = a->n_stims;
-        for (int s = 0; s < a->n_stims; ++s) {
-            const fw_stim &S = a->stims[s];
-            BStim &B = desc[i].stims[s];
-            B.first = S.first;
-            B.last = S.last;
-            B.kind = S.kind;
-            B.has_umax = S.has_umax;
-            B.value = (float)S.value;
-            B.u_max = (float)S.u_max;
-            B.lo0 = (int32_t)(S.lo[0] < 0 ? 0 : S.lo[0]);
-            B.hi0 = (int32_t)(S.hi[0] > a->ni ? a->ni : S.hi[0]);
-            B.lo1 = (int32_t)(S.lo[1] < 0 ? 0 : S.lo[1]);
-            B.hi1 = (int32_t)(S.hi[1] > a->nj ? a->nj : S.hi[1]);
-            B.mask = S.mask;
+    // host staging, 128-byte aligned like the device plan (the descriptors
+    // of the TMA form hold 64-byte aligned tensor maps)
+    std::vector<unsigned char> raw((size_t)need + 128, 0);
+    unsigned char *host = raw.data() + ((128 - ((uintptr_t)raw.data() & 127)) & 127);
+    const size_t desc_bytes = kernel == 2 ? sizeof(BTissueT) : sizeof(BTissue);
+    unsigned char *tiles_host = host + align_up(desc_bytes * n, 256);
+    if (kernel == 2) {
+        BTissueT *desc = reinterpret_cast<BTissueT *>(host);
+        for (int i = 0; i < n; ++i) {
+            rc = fill_tma_tissue(tissues[i], n_begin[i], desc[i]);
+            if (rc) return rc;
         }
-        T.has_at = a->n_at;
-        if (a->n_at) {
-            T.at_win = BWin{a->at[0].win.first, a->at[0].win.last,
-                            a->at[0].win.stride};
-            T.at_thr = (float)a->at[0].threshold;
-            T.at_act = a->at[0].act_step;
+    } else {
+        BTissue *desc = reinterpret_cast<BTissue *>(host);
+        for (int i = 0; i < n; ++i) {
+            const fw_step_args *a = tissues[i];
+            BHead &T = desc[i].h;
+            T.w = (const float *)a->weights;
+            T.myo = a->myo;
+            T.u[0] = (float *)a->u[0];
+            T.u[1] = (float *)a->u[1];
+            int ns = 0, np = 0;
+            fw_model_info(a->model, &ns, &np);
+            for (int s = 0; s < kMaxState; ++s) T.state[s] = s < ns ? a->state[s] : nullptr;
+            for (int p = 0; p < kMaxParams; ++p) T.params[p] = p < np ? (float)a->params[p] : 0.f;
+            T.dt = (float)a->dt;
+            T.model = a->model;
+            T.stencil = a->stencil;
+            T.ni = (int32_t)a->ni;
+            T.nj = (int32_t)a->nj;
+            T.tiles_j = (int32_t)((a->nj + TJ - 1) / TJ);
+            T.n = a->ni * a->nj;
+            T.step_base = n_begin[i];
+            T.n_stims = a->n_stims;
+            for (int s = 0; s < a->n_stims; ++s) {
+                const fw_stim &S = a->stims[s];
+                BStim &B = desc[i].stims[s];
+                B.first = S.first;
+                B.last = S.last;
+                B.kind = S.kind;
+                B.has_umax = S.has_umax;
+                B.value = (float)S.value;
+                B.u_max = (float)S.u_max;
+                B.lo0 = (int32_t)(S.lo[0] < 0 ? 0 : S.lo[0]);
+                B.hi0 = (int32_t)(S.hi[0] > a->ni ? a->ni : S.hi[0]);
+                B.lo1 = (int32_t)(S.lo[1] < 0 ? 0 : S.lo[1]);
+                B.hi1 = (int32_t)(S.hi[1] > a->nj ? a->nj : S.hi[1]);
+                B.mask = S.mask;
+            }
+            T.has_at = a->n_at;
+            if (a->n_at) {
+                T.at_win = BWin{a->at[0].win.first, a->at[0].win.last,
+                                a->at[0].win.stride};
+                T.at_thr = (float)a->at[0].threshold;
+                T.at_act = a->at[0].act_step;
+            }
+            T.has_lat = a->n_lat;
+            if (a->n_lat) {
+                const fw_lat_tracker &L = a->lat[0];
+                T.lat_win = BWin{L.win.first, L.win.last, L.win.stride};
+                T.lat_thr = (float)L.threshold;
+                T.lat_cap = L.capacity;
+                T.lat_activated = L.activated;
+                T.lat_steps = L.cross_steps;
+                T.lat_count = L.cross_count;
+            }
+            T.status = a->status;
         }
-        T.has_lat = a->n_lat;
-        if (a->n_lat) {
-            const fw_lat_tracker &L = a->lat[0];
-            T.lat_win = BWin{L.win.first, L.win.last, L.win.stride};
-            T.lat_thr = (float)L.threshold;
-            T.lat_cap = L.capacity;
-            T.lat_activated = L.activated;
-            T.lat_steps = L.cross_steps;
-            T.lat_count = L.cross_count;
-        }
-        T.status = a->status;
     }
     // tile list grouped by (model, stencil): CTAs taking consecutive tiles
     // then run the same specialisation of the tile code (one of six inlined
@@ -604,12 +997,23 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
         const int ky = tissues[y]->model * 8 + tissues[y]->stencil;
         return kx < ky;
     });
+    int32_t t_count = 0;
     for (int i : order) {
-        const int32_t nt = (int32_t)tissue_tiles(tissues[i]);
-        for (int32_t k = 0; k < nt; ++k) tl[t_count + k] = BTile{i, k};
+        const fw_step_args *a = tissues[i];
+        const int32_t nt = (int32_t)tissue_tiles(a);
+        if (kernel == 2) {
+            BTileT *tl = reinterpret_cast<BTileT *>(tiles_host);
+            const int32_t tj = (int32_t)((a->nj + TJ - 1) / TJ);
+            for (int32_t k = 0; k < nt; ++k)
+                tl[t_count + k] = BTileT{i, a->model * 8 + a->stencil,
+                                         (k / tj) * TI - KMAX, (k % tj) * TJ - KMAX};
+        } else {
+            BTile *tl = reinterpret_cast<BTile *>(tiles_host);
+            for (int32_t k = 0; k < nt; ++k) tl[t_count + k] = BTile{i, k};
+        }
         t_count += nt;
     }
-    FW_CUDA_CHECK(cudaMemcpyAsync(plan, host.data(), (size_t)need,
+    FW_CUDA_CHECK(cudaMemcpyAsync(plan, host, (size_t)need,
                                   cudaMemcpyHostToDevice, stream));
     // the host staging buffer is released on return
     FW_CUDA_CHECK(cudaStreamSynchronize(stream));
@@ -617,10 +1021,17 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     int dev = 0, sms = 0, per_sm = 0;
     FW_CUDA_CHECK(cudaGetDevice(&dev));
     FW_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    FW_CUDA_CHECK(cudaFuncSetAttribute(
-        k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
-    FW_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, k_batch, NT, kSmem));
+    if (kernel == 2) {
+        FW_CUDA_CHECK(cudaFuncSetAttribute(
+            k_batch_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaSmem));
+        FW_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_batch_tma, kTmaNT, kTmaSmem));
+    } else {
+        FW_CUDA_CHECK(cudaFuncSetAttribute(
+            k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
+        FW_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_batch, NT, kSmem));
+    }
     if (per_sm < 1) per_sm = 1;
     int64_t grid = (int64_t)sms * per_sm;
     if (grid > t_count) grid = t_count;
@@ -629,6 +1040,8 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     out->n_tiles = t_count;
     out->ksteps = KMAX;
     out->grid = (int32_t)grid;
+    out->kernel = kernel;
+    out->reserved = 0;
     return FW_OK;
 }
 
@@ -636,7 +1049,8 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
               int64_t n_steps, cudaStream_t stream)
 {
     using namespace batch;
-    if (!b || !b->plan || !scratch || b->n_tissues <= 0 || b->grid <= 0) {
+    if (!b || !b->plan || !scratch || b->n_tissues <= 0 || b->grid <= 0 ||
+        (b->kernel != 1 && b->kernel != 2)) {
         set_error("fw_batch_run: empty plan or NULL scratch");
         return FW_ERR_ARG;
     }
@@ -648,14 +1062,25 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
     // the plan set the shared-memory attribute on this device; set it again
     // unless the stream is being captured into a CUDA graph (the launches
     // alone are recorded then)
+    const bool tma = b->kernel == 2;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     FW_CUDA_CHECK(cudaStreamIsCapturing(stream, &cap));
-    if (cap == cudaStreamCaptureStatusNone)
-        FW_CUDA_CHECK(cudaFuncSetAttribute(
-            k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
+    if (cap == cudaStreamCaptureStatusNone) {
+        if (tma)
+            FW_CUDA_CHECK(cudaFuncSetAttribute(k_batch_tma,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kTmaSmem));
+        else
+            FW_CUDA_CHECK(cudaFuncSetAttribute(
+                k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
+    }
+    const size_t desc_bytes = tma ? sizeof(BTissueT) : sizeof(BTissue);
     const BTissue *desc = reinterpret_cast<const BTissue *>(b->plan);
-    const BTile *tl = reinterpret_cast<const BTile *>(
-        (const unsigned char *)b->plan + align_up(sizeof(BTissue) * b->n_tissues, 256));
+    BTissueT *desc_t = reinterpret_cast<BTissueT *>(b->plan);
+    const unsigned char *tiles_dev =
+        (const unsigned char *)b->plan + align_up(desc_bytes * b->n_tissues, 256);
+    const BTile *tl = reinterpret_cast<const BTile *>(tiles_dev);
+    const BTileT *tl_t = reinterpret_cast<const BTileT *>(tiles_dev);
     // L launches of <= KMAX steps with L == n_steps (mod 2): the result ends
     // in u[(offset + n_steps) & 1], as after the same steps of the plain form
     int64_t L = (n_steps + KMAX - 1) / KMAX;
@@ -666,10 +1091,20 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
         int64_t ks = (left + launches_left - 1) / launches_left;
         if (ks > KMAX) ks = KMAX;
         const int in_buf = (int)((offset + li) & 1);
-        k_batch<<<b->grid, NT, kSmem, stream>>>(desc, tl, b->n_tiles,
-                                               b->n_tissues, offset + done,
-                                               (int32_t)ks, in_buf, scratch);
-        FW_CHECK_LAUNCH("k_batch");
+        if (tma) {
+            const dim3 eb(32, 4);
+            k_batch_events<<<(unsigned)((b->n_tissues + 3) / 4), eb, 0, stream>>>(
+                desc_t, b->n_tissues, offset + done, (int32_t)ks, in_buf);
+            FW_CHECK_LAUNCH("k_batch_events");
+            k_batch_tma<<<b->grid, kTmaNT, kTmaSmem, stream>>>(
+                desc_t, tl_t, b->n_tiles, b->n_tissues, in_buf, scratch);
+            FW_CHECK_LAUNCH("k_batch_tma");
+        } else {
+            k_batch<<<b->grid, NT, kSmem, stream>>>(desc, tl, b->n_tiles,
+                                                   b->n_tissues, offset + done,
+                                                   (int32_t)ks, in_buf, scratch);
+            FW_CHECK_LAUNCH("k_batch");
+        }
         done += ks;
     }
     return FW_OK;
@@ -707,7 +1142,8 @@ int batch_run_noalloc(const fw_batch *b, int64_t offset, int64_t n_steps,
                       cudaStream_t stream)
 {
     // the argument checks of batch_run, before the one-time set-up
-    if (!b || !b->plan || b->n_tissues <= 0 || b->grid <= 0) {
+    if (!b || !b->plan || b->n_tissues <= 0 || b->grid <= 0 ||
+        (b->kernel != 1 && b->kernel != 2)) {
         set_error("fw_batch_run_noalloc: empty plan");
         return FW_ERR_ARG;
     }

@@ -91,6 +91,10 @@ int check_step_args(const fw_step_args *a, int64_t n_steps)
         set_error("fw_step: n_steps %lld out of range", (long long)n_steps);
         return FW_ERR_ARG;
     }
+    if (a->pitch != 0 && a->pitch != a->nj) {
+        set_error("fw_step: a row pitch other than nj is for batches only");
+        return FW_ERR_UNSUPPORTED;
+    }
     if (!a->mesh || !a->myo || !a->weights || !a->u[0] || !a->u[1] ||
         a->u[0] == a->u[1]) {
         set_error("fw_step: mesh/myo/weights/u buffers missing or aliased");
@@ -219,7 +223,14 @@ int fw_model_info(int32_t model, int32_t *n_state, int32_t *n_params)
 
 int fw_state_is_f64(int32_t model, int32_t precision, int32_t index)
 {
-    if (precision == FW_F64) return 1;
+    (void)model;
+    (void)index;
+    return precision == FW_F64 ? 1 : 0;
+}
+
+int fw_state_is_pair(int32_t model, int32_t precision, int32_t index)
+{
+    if (precision != FW_F32) return 0;
     switch (model) {
     case FW_MODEL_TP06: return fw::ModelTP06::is_conc(index) ? 1 : 0;
     case FW_MODEL_CRN: return fw::ModelCRN::is_conc(index) ? 1 : 0;

@@ -45,7 +45,7 @@
 namespace fw {
 namespace fused {
 
-constexpr int kMaxFusedStims = 8;
+constexpr int kMaxFusedStims = FW_MAX_STIMS;
 constexpr int kMaxFusedProbeEntries = 128;
 // trackers evaluated in the fused kernel (more -> the host uses the plain
 // form); kept small so that their state stays in registers
@@ -85,7 +85,9 @@ struct FProbe {
     int32_t var_ids[FW_MAX_PROBE_VARS];
 };
 
-struct FusedK {
+// (16-byte aligned and sized: the batched TMA kernel moves it with one
+// bulk copy)
+struct alignas(16) FusedK {
     const float *w;
     const int8_t *myo;
     const float *u_in;
@@ -96,6 +98,7 @@ struct FusedK {
     float params[FW_MAX_PARAMS];
     float dt;
     int32_t ni, nj;
+    int32_t pitch;   // row pitch (nodes) of u_out, state and myo (TMA forms)
     int64_t n;
     int64_t n0;
     int32_t ksteps;

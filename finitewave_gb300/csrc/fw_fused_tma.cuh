@@ -176,31 +176,292 @@ __device__ __forceinline__ int floor_to(int x, int m)
 
 // ---- kernel ----------------------------------------------------------------------
 
+// Copy one tile's region into a stage: packed weights, potential, the
+// model's NS state arrays, myocyte flags and centre weights, all completing
+// on `bar`.  NS and NWO are the model's and the stencil's; the stage may be
+// laid out for more (the batched kernel's stages hold the largest model).
 // PAIRS: the weight map is the column-pair view of encode_weights_pairs, and
 // the weights land as [row][column parity][column pair] (k_fused_tma2).
+// The barrier has an arrival count of one: this is the stage's only
+// arrive, and it announces the region's bytes plus `extra` bytes of other
+// copies the caller issues on the same barrier.
+template <int KMAX, int NS, int NWO, bool PAIRS = false, class Stage>
+__device__ __forceinline__ void issue_region(const TmaMaps &maps, int in_buf,
+                                             Stage &G, uint64_t *bar, int oi,
+                                             int oj, unsigned extra = 0)
+{
+    const int x4 = floor_to(oj - 1, 4), x16 = floor_to(oj, 16);
+    const unsigned bytes = (unsigned)(sizeof(G.wa) * (NWO == 8 ? 2 : 1) +
+                                      sizeof(G.u) + NS * sizeof(G.s[0]) +
+                                      sizeof(G.myo) + sizeof(G.wc));
+    mbar_expect_tx(bar, bytes + extra);
+    if constexpr (PAIRS) {
+        tma_4d(&G.wa[0][0], &maps.w, 0, oj / 2, 0, oi, bar);
+        if constexpr (NWO == 8) tma_4d(&G.wb[0][0], &maps.w, 4, oj / 2, 0, oi, bar);
+    } else {
+        tma_3d(&G.wa[0][0], &maps.w, 0, oj, oi, bar);
+        if constexpr (NWO == 8) tma_3d(&G.wb[0][0], &maps.w, 4, oj, oi, bar);
+    }
+    tma_2d(&G.u[0][0], &maps.u[in_buf], x4, oi - 1, bar);
+#pragma unroll
+    for (int q = 0; q < NS; ++q) tma_2d(&G.s[q][0][0], &maps.s[q], x4, oi, bar);
+    tma_2d(&G.myo[0][0], &maps.myo, x16, oi, bar);
+    tma_2d(&G.wc[0][0], &maps.wc, x4, oi, bar);
+}
+
 template <int KMAX, int LH, int NS, int NWO, bool PAIRS = false>
 __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> &G,
                                            uint64_t *bar, int bi, int bj)
 {
     constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
-    const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
-    const int x4 = floor_to(oj - 1, 4), x16 = floor_to(oj, 16);
-    constexpr unsigned bytes =
-        sizeof(G.wa) + (NWO == 8 ? sizeof(G.wb) : 0) + sizeof(G.u) +
-        sizeof(G.s) + sizeof(G.myo) + sizeof(G.wc);
-    mbar_expect_tx(bar, bytes);
-    if constexpr (PAIRS) {
-        tma_4d(&G.wa[0][0], &k.maps.w, 0, oj / 2, 0, oi, bar);
-        if constexpr (NWO == 8) tma_4d(&G.wb[0][0], &k.maps.w, 4, oj / 2, 0, oi, bar);
-    } else {
-        tma_3d(&G.wa[0][0], &k.maps.w, 0, oj, oi, bar);
-        if constexpr (NWO == 8) tma_3d(&G.wb[0][0], &k.maps.w, 4, oj, oi, bar);
-    }
-    tma_2d(&G.u[0][0], &k.maps.u[k.in_buf], x4, oi - 1, bar);
+    issue_region<KMAX, NS, NWO, PAIRS>(k.maps, k.in_buf, G, bar, bi * TI - KMAX,
+                                       bj * TJ - KMAX);
+}
+
+// Rows r < R of the strip of thread (col, r0) inside the region's interior
+// (own) and off its outer ring (ring): the same for every tile.
+template <int KMAX, int LH, int R>
+__device__ __forceinline__ void strip_masks(int col, int r0, uint32_t &own_c,
+                                            uint32_t &ring_c)
+{
+    constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
+    own_c = ring_c = 0;
 #pragma unroll
-    for (int q = 0; q < NS; ++q) tma_2d(&G.s[q][0][0], &k.maps.s[q], x4, oi, bar);
-    tma_2d(&G.myo[0][0], &k.maps.myo, x16, oi, bar);
-    tma_2d(&G.wc[0][0], &k.maps.wc, x4, oi, bar);
+    for (int r = 0; r < R; ++r) {
+        const int lr = r0 + r;
+        if (col >= KMAX && col < KMAX + TJ && lr >= KMAX && lr < KMAX + TI)
+            own_c |= 1u << r;
+        if (col > 0 && col < kTW - 1 && lr > 0 && lr < LH - 1) ring_c |= 1u << r;
+    }
+}
+
+// One staged tile: K sub-steps of the region with origin (oi, oj) from
+// stage G, then the interior written back.  f describes the tissue and the
+// launch (its u_out, state and myocyte arrays have row pitch f.pitch; the
+// tracker arrays and stimulus masks row length f.nj).  u1 is the ping-pong
+// partner of the stage's potential.  Thread (col, r0) owns the strip of R
+// rows of column col.  Shared by the single-tissue and the batched kernels.
+template <class M, int ST, int KMAX, int LH, int R, class Stage, class Sm>
+__device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int oi,
+                                         int oj, uint32_t own_c, uint32_t ring_c,
+                                         const Params<float, M::NP> &P)
+{
+    constexpr int LW = kTW;
+    constexpr int NT = LW * (LH / R);
+    constexpr int TI = LH - 2 * KMAX, TJ = LW - 2 * KMAX;
+    constexpr int NS = M::NS;
+    constexpr int NWO = Stencil2D<ST>::NWO;
+    const int tid = threadIdx.x;
+    const int col = tid % LW;
+    const int r0 = (tid / LW) * R;
+    const float dt = f.dt;
+
+    const int xo = oj - floor_to(oj - 1, 4);   // 1..4
+    const int xo8 = oj - floor_to(oj, 16);     // 0..15
+    const int gj = oj + col;
+    const bool col_in = (unsigned)gj < (unsigned)f.nj;
+
+    // per-thread flags and state of the strip
+    typename M::template St<float> st[R];
+    uint32_t myo_bits = 0, inb = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int lr = r0 + r;
+        if (col_in && (unsigned)(oi + lr) < (unsigned)f.ni) inb |= 1u << r;
+        if (G.myo[lr][col + xo8]) myo_bits |= 1u << r;
+        float sv[kMaxTmaState];
+#pragma unroll
+        for (int q = 0; q < NS; ++q) sv[q] = G.s[q][lr][col + xo];
+        st[r] = M::template from_array<float>(sv);
+    }
+    myo_bits &= inb;
+    const uint32_t own = own_c & inb;
+    const uint32_t upd = ring_c & myo_bits;
+    // centre weights of the strip (the stored plane); the sub-steps form
+    // the reference's sum  w_c u + sum_k w_k u_k  as one FMA chain
+    float wcen[R];
+    float4 wreg[R];   // the first four off-centre weights, kept for the tile
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        wcen[r] = G.wc[r0 + r][col + xo];
+        wreg[r] = G.wa[r0 + r][col];
+    }
+
+    // probe cells of this tile
+    uint32_t probe_mine = 0;
+    if (f.n_probe) {
+        for (int i = tid; i < (LH * LW + 31) / 32; i += NT) S.probe_bits[i] = 0;
+        if (tid == 0) S.probe_count = 0;
+        __syncthreads();
+        for (int t = 0; t < f.n_probe; ++t) {
+            const FProbe &pr = f.probe[t];
+            for (int c = tid; c < pr.n_cells; c += NT) {
+                const int64_t p = pr.cells[c];
+                const int gi = (int)(p / f.nj), gjj = (int)(p % f.nj);
+                const int lr = gi - oi, lc = gjj - oj;
+                if (lr >= KMAX && lr < KMAX + TI && lc >= KMAX &&
+                    lc < KMAX + TJ) {
+                    const int e = atomicAdd(&S.probe_count, 1);
+                    if (e < kMaxFusedProbeEntries) {
+                        S.probe_list[e] = ProbeEntry{(int16_t)lr, (int16_t)lc,
+                                                     (int16_t)t, c};
+                        const int bit = lr * LW + lc;
+                        atomicOr(&S.probe_bits[bit >> 5], 1u << (bit & 31));
+                    } else if (f.status) {
+                        atomicOr(f.status, FW_DEV_PROBE_OVERFLOW);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int bit = (r0 + r) * LW + col;
+            if ((S.probe_bits[bit >> 5] >> (bit & 31)) & 1u)
+                probe_mine |= 1u << r;
+        }
+    }
+    uint32_t lat_act = 0, at_done = 0;
+#pragma unroll
+    for (int l = 0; l < kMaxFusedLat; ++l)
+        if (l < f.n_lat) {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if ((own >> r) & 1u) {
+                    const int64_t p = (int64_t)(oi + r0 + r) * f.nj + gj;
+                    if (f.lat[l].activated[p]) lat_act |= 1u << (l * 8 + r);
+                }
+        }
+
+    // ---- sub-steps ----
+    for (int s = 0; s < f.ksteps; ++s) {
+        const int64_t n = f.n0 + s;
+        float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
+        float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;
+
+        if ((f.stim_on >> s) & 1u) {
+            for (int i = 0; i < f.n_stims; ++i) {
+                const FStim &F = f.stims[i];
+                if (!((F.on >> s) & 1u)) continue;
+                if (gj < F.lo1 || gj >= F.hi1) continue;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if (!((myo_bits >> r) & 1u)) continue;
+                    const int lr = r0 + r, gi = oi + lr;
+                    if (gi < F.lo0 || gi >= F.hi0) continue;
+                    if (F.mask && !F.mask[(int64_t)gi * f.nj + gj]) continue;
+                    float x = cur[lr + 1][col + xo];
+                    if (F.kind == FW_STIM_VOLTAGE) {
+                        x = F.value;
+                    } else {
+                        x = x + F.value;
+                        if (F.has_umax && x > F.u_max) x = F.u_max;
+                    }
+                    cur[lr + 1][col + xo] = x;
+                }
+            }
+            __syncthreads();
+        }
+
+        float wl[R + 2], wc[R + 2], wr[R + 2];
+#pragma unroll
+        for (int i = 0; i < R + 2; ++i) {
+            wl[i] = cur[r0 + i][col + xo - 1];
+            wc[i] = cur[r0 + i][col + xo];
+            wr[i] = cur[r0 + i][col + xo + 1];
+        }
+
+        if (own) {
+#pragma unroll
+            for (int a = 0; a < kMaxFusedAt; ++a) {
+                if (a >= f.n_at || !((f.at[a].on >> s) & 1u)) continue;
+                // the strip's maximum first: most sub-steps cross nowhere
+                // (fmaxf skips NaN rows, which never cross)
+                float mx = wc[1];
+#pragma unroll
+                for (int r = 1; r < R; ++r) mx = fmaxf(mx, wc[r + 1]);
+                if (!(mx > f.at[a].thr)) continue;
+                const uint32_t hit =
+                    rows_gt<R>(wc, f.at[a].thr) & own & ~(at_done >> (a * 8));
+                if (hit) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        if (!((hit >> r) & 1u)) continue;
+                        // first crossing: unsigned minimum, "never" = -1
+                        // (activation_time_2d_tracker.py:61-63)
+                        const int64_t p = (int64_t)(oi + r0 + r) * f.nj + gj;
+                        atomicMin(reinterpret_cast<unsigned *>(f.at[a].act) + p,
+                                  (unsigned)n);
+                    }
+                    at_done |= hit << (a * 8);
+                }
+            }
+#pragma unroll
+            for (int l = 0; l < kMaxFusedLat; ++l) {
+                if (l >= f.n_lat || !((f.lat[l].on >> s) & 1u)) continue;
+                // (local_activation_time_2d_tracker.py:71-89)
+                const uint32_t was = (lat_act >> (l * 8)) & 0xffu;
+                const uint32_t rise = rows_ge<R>(wc, f.lat[l].thr) & own & ~was;
+                const uint32_t fall = rows_lt<R>(wc, f.lat[l].thr) & own & was;
+                lat_act ^= (rise | fall) << (l * 8);
+                if (rise) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+                        if ((rise >> r) & 1u)
+                            lat_record(f.lat[l],
+                                       (int64_t)(oi + r0 + r) * f.nj + gj, f.n, n,
+                                       f.status);
+                }
+            }
+        }
+
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float b1 = wc[r + 1];
+            const int lr = r0 + r;
+            const float4 wa = wreg[r];
+            float4 wb = wa;
+            if constexpr (NWO == 8) wb = G.wb[lr][col];
+            const float un = stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r],
+                                             wr[r], wl[r + 1], wr[r + 1],
+                                             wl[r + 2], wc[r + 2], wr[r + 2]);
+            const float uu = M::template update<float>(b1, un, st[r], P, dt);
+            nxt[lr + 1][col + xo] = ((upd >> r) & 1u) ? uu : b1;
+        }
+        // probes: u after the stimuli, the state after the update
+        if (probe_mine && ((f.probe_on >> s) & 1u)) {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if ((probe_mine >> r) & 1u)
+                    write_probes<M>(f, S.probe_list, S.probe_count, r0 + r, col,
+                                    s, wc[r + 1], st[r],
+                                    ((myo_bits >> r) & 1u) != 0,
+                                    (int64_t)(oi + r0 + r) * f.pitch + gj);
+        }
+        __syncthreads();
+    }
+
+    // ---- write the interior back ----
+    float(*fin)[kBoxF] = (f.ksteps & 1) ? S.u1 : G.u;
+    bool nonfinite = false;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (!((own >> r) & 1u)) continue;
+        const int lr = r0 + r;
+        if ((myo_bits >> r) & 1u) {
+            const int64_t pp = (int64_t)(oi + lr) * f.pitch + gj;
+            const float uo = fin[lr + 1][col + xo];
+            f.u_out[pp] = uo;
+            nonfinite |= !isfinite(uo);
+            M::template store<float>(f.state, pp, st[r]);
+        }
+#pragma unroll
+        for (int l = 0; l < kMaxFusedLat; ++l)
+            if (l < f.n_lat)
+                f.lat[l].activated[(int64_t)(oi + lr) * f.nj + gj] =
+                    (lat_act >> (l * 8 + r)) & 1u;
+    }
+    if (nonfinite && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
 }
 
 template <class M, int ST, int KMAX, int LH, int R>
@@ -208,7 +469,6 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
     k_fused_tma(const __grid_constant__ TmaK k)
 {
     constexpr int LW = kTW;
-    constexpr int NT = LW * (LH / R);
     constexpr int TI = LH - 2 * KMAX, TJ = LW - 2 * KMAX;
     constexpr int NS = M::NS;
     constexpr int NWO = Stencil2D<ST>::NWO;
@@ -224,18 +484,8 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
     const FusedK &f = k.f;
 
     const int tid = threadIdx.x;
-    const int col = tid % LW;
-    const int r0 = (tid / LW) * R;
-    // rows of the strip in the region's interior / off its ring: the same
-    // for every tile
-    uint32_t own_c = 0, ring_c = 0;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int lr = r0 + r;
-        if (col >= KMAX && col < KMAX + TJ && lr >= KMAX && lr < KMAX + TI)
-            own_c |= 1u << r;
-        if (col > 0 && col < LW - 1 && lr > 0 && lr < LH - 1) ring_c |= 1u << r;
-    }
+    uint32_t own_c, ring_c;
+    strip_masks<KMAX, LH, R>(tid % LW, (tid / LW) * R, own_c, ring_c);
 
     if (tid == 0) {
         mbar_init(&S.bar[0], 1);
@@ -254,7 +504,6 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
     Params<float, M::NP> P;
 #pragma unroll
     for (int i = 0; i < M::NP; ++i) P.v[i] = f.params[i];
-    const float dt = f.dt;
     unsigned parity = 0u;  // bit sg: phase parity expected next on bar[sg]
 
     for (int it = 0; tile < k.tiles; ++it, tile += gridDim.x) {
@@ -279,214 +528,10 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             if (tid == 0) tma_abandon(k, S.bar, sg, ph, parity, arrived, next);
             return;
         }
-
         const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
         bi = ni_;
         bj = nj_;
-        const int xo = oj - floor_to(oj - 1, 4);   // 1..4
-        const int xo8 = oj - floor_to(oj, 16);     // 0..15
-        const int gj = oj + col;
-        const bool col_in = (unsigned)gj < (unsigned)f.nj;
-
-        // per-thread flags and state of the strip
-        typename M::template St<float> st[R];
-        uint32_t myo_bits = 0, inb = 0;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int lr = r0 + r;
-            if (col_in && (unsigned)(oi + lr) < (unsigned)f.ni) inb |= 1u << r;
-            if (G.myo[lr][col + xo8]) myo_bits |= 1u << r;
-            float sv[kMaxTmaState];
-#pragma unroll
-            for (int q = 0; q < NS; ++q) sv[q] = G.s[q][lr][col + xo];
-            st[r] = M::template from_array<float>(sv);
-        }
-        myo_bits &= inb;
-        const uint32_t own = own_c & inb;
-        const uint32_t upd = ring_c & myo_bits;
-        // centre weights of the strip (the stored plane); the sub-steps form
-        // the reference's sum  w_c u + sum_k w_k u_k  as one FMA chain
-        float wcen[R];
-        float4 wreg[R];   // the first four off-centre weights, kept for the tile
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            wcen[r] = G.wc[r0 + r][col + xo];
-            wreg[r] = G.wa[r0 + r][col];
-        }
-
-        // probe cells of this tile
-        uint32_t probe_mine = 0;
-        if (f.n_probe) {
-            for (int i = tid; i < (LH * LW + 31) / 32; i += NT) S.probe_bits[i] = 0;
-            if (tid == 0) S.probe_count = 0;
-            __syncthreads();
-            for (int t = 0; t < f.n_probe; ++t) {
-                const FProbe &pr = f.probe[t];
-                for (int c = tid; c < pr.n_cells; c += NT) {
-                    const int64_t p = pr.cells[c];
-                    const int gi = (int)(p / f.nj), gjj = (int)(p % f.nj);
-                    const int lr = gi - oi, lc = gjj - oj;
-                    if (lr >= KMAX && lr < KMAX + TI && lc >= KMAX &&
-                        lc < KMAX + TJ) {
-                        const int e = atomicAdd(&S.probe_count, 1);
-                        if (e < kMaxFusedProbeEntries) {
-                            S.probe_list[e] = ProbeEntry{(int16_t)lr, (int16_t)lc,
-                                                         (int16_t)t, c};
-                            const int bit = lr * LW + lc;
-                            atomicOr(&S.probe_bits[bit >> 5], 1u << (bit & 31));
-                        } else if (f.status) {
-                            atomicOr(f.status, FW_DEV_PROBE_OVERFLOW);
-                        }
-                    }
-                }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const int bit = (r0 + r) * LW + col;
-                if ((S.probe_bits[bit >> 5] >> (bit & 31)) & 1u)
-                    probe_mine |= 1u << r;
-            }
-        }
-        uint32_t lat_act = 0, at_done = 0;
-#pragma unroll
-        for (int l = 0; l < kMaxFusedLat; ++l)
-            if (l < f.n_lat) {
-#pragma unroll
-                for (int r = 0; r < R; ++r)
-                    if ((own >> r) & 1u) {
-                        const int64_t p = (int64_t)(oi + r0 + r) * f.nj + gj;
-                        if (f.lat[l].activated[p]) lat_act |= 1u << (l * 8 + r);
-                    }
-            }
-
-        // ---- sub-steps ----
-        for (int s = 0; s < f.ksteps; ++s) {
-            const int64_t n = f.n0 + s;
-            float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
-            float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;
-
-            if ((f.stim_on >> s) & 1u) {
-                for (int i = 0; i < f.n_stims; ++i) {
-                    const FStim &F = f.stims[i];
-                    if (!((F.on >> s) & 1u)) continue;
-                    if (gj < F.lo1 || gj >= F.hi1) continue;
-#pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        if (!((myo_bits >> r) & 1u)) continue;
-                        const int lr = r0 + r, gi = oi + lr;
-                        if (gi < F.lo0 || gi >= F.hi0) continue;
-                        if (F.mask && !F.mask[(int64_t)gi * f.nj + gj]) continue;
-                        float x = cur[lr + 1][col + xo];
-                        if (F.kind == FW_STIM_VOLTAGE) {
-                            x = F.value;
-                        } else {
-                            x = x + F.value;
-                            if (F.has_umax && x > F.u_max) x = F.u_max;
-                        }
-                        cur[lr + 1][col + xo] = x;
-                    }
-                }
-                __syncthreads();
-            }
-
-            float wl[R + 2], wc[R + 2], wr[R + 2];
-#pragma unroll
-            for (int i = 0; i < R + 2; ++i) {
-                wl[i] = cur[r0 + i][col + xo - 1];
-                wc[i] = cur[r0 + i][col + xo];
-                wr[i] = cur[r0 + i][col + xo + 1];
-            }
-
-            if (own) {
-#pragma unroll
-                for (int a = 0; a < kMaxFusedAt; ++a) {
-                    if (a >= f.n_at || !((f.at[a].on >> s) & 1u)) continue;
-                    // the strip's maximum first: most sub-steps cross nowhere
-                    // (fmaxf skips NaN rows, which never cross)
-                    float mx = wc[1];
-#pragma unroll
-                    for (int r = 1; r < R; ++r) mx = fmaxf(mx, wc[r + 1]);
-                    if (!(mx > f.at[a].thr)) continue;
-                    const uint32_t hit =
-                        rows_gt<R>(wc, f.at[a].thr) & own & ~(at_done >> (a * 8));
-                    if (hit) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r) {
-                            if (!((hit >> r) & 1u)) continue;
-                            // first crossing: unsigned minimum, "never" = -1
-                            // (activation_time_2d_tracker.py:61-63)
-                            const int64_t p = (int64_t)(oi + r0 + r) * f.nj + gj;
-                            atomicMin(reinterpret_cast<unsigned *>(f.at[a].act) + p,
-                                      (unsigned)n);
-                        }
-                        at_done |= hit << (a * 8);
-                    }
-                }
-#pragma unroll
-                for (int l = 0; l < kMaxFusedLat; ++l) {
-                    if (l >= f.n_lat || !((f.lat[l].on >> s) & 1u)) continue;
-                    // (local_activation_time_2d_tracker.py:71-89)
-                    const uint32_t was = (lat_act >> (l * 8)) & 0xffu;
-                    const uint32_t rise = rows_ge<R>(wc, f.lat[l].thr) & own & ~was;
-                    const uint32_t fall = rows_lt<R>(wc, f.lat[l].thr) & own & was;
-                    lat_act ^= (rise | fall) << (l * 8);
-                    if (rise) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-                            if ((rise >> r) & 1u)
-                                lat_record(f.lat[l],
-                                           (int64_t)(oi + r0 + r) * f.nj + gj, f.n, n,
-                                           f.status);
-                    }
-                }
-            }
-
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const float b1 = wc[r + 1];
-                const int lr = r0 + r;
-                const float4 wa = wreg[r];
-                const float4 wb = NWO == 8 ? G.wb[NWO == 8 ? lr : 0][col] : wa;
-                const float un = stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r],
-                                                 wr[r], wl[r + 1], wr[r + 1],
-                                                 wl[r + 2], wc[r + 2], wr[r + 2]);
-                const float uu = M::template update<float>(b1, un, st[r], P, dt);
-                nxt[lr + 1][col + xo] = ((upd >> r) & 1u) ? uu : b1;
-            }
-            // probes: u after the stimuli, the state after the update
-            if (probe_mine && ((f.probe_on >> s) & 1u)) {
-#pragma unroll
-                for (int r = 0; r < R; ++r)
-                    if ((probe_mine >> r) & 1u)
-                        write_probes<M>(f, S.probe_list, S.probe_count, r0 + r, col,
-                                        s, wc[r + 1], st[r],
-                                        ((myo_bits >> r) & 1u) != 0,
-                                        (int64_t)(oi + r0 + r) * f.nj + gj);
-            }
-            __syncthreads();
-        }
-
-        // ---- write the interior back ----
-        float(*fin)[kBoxF] = (f.ksteps & 1) ? S.u1 : G.u;
-        bool nonfinite = false;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            if (!((own >> r) & 1u)) continue;
-            const int lr = r0 + r;
-            const int64_t p = (int64_t)(oi + lr) * f.nj + gj;
-            if ((myo_bits >> r) & 1u) {
-                const float uo = fin[lr + 1][col + xo];
-                f.u_out[p] = uo;
-                nonfinite |= !isfinite(uo);
-                M::template store<float>(f.state, p, st[r]);
-            }
-#pragma unroll
-            for (int l = 0; l < kMaxFusedLat; ++l)
-                if (l < f.n_lat)
-                    f.lat[l].activated[p] = (lat_act >> (l * 8 + r)) & 1u;
-        }
-        if (nonfinite && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
+        tma_tile<M, ST, KMAX, LH, R>(f, G, S, oi, oj, own_c, ring_c, P);
         __syncthreads();
     }
 }
@@ -843,13 +888,15 @@ inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
+// A 2D map of (ni, nj) nodes whose rows start `pitch` nodes apart (0: nj).
 inline bool encode_2d(CUtensorMap *m, CUtensorMapDataType t, size_t esize,
-                      const void *base, int64_t nj, int64_t ni, int bw, int bh)
+                      const void *base, int64_t nj, int64_t ni, int bw, int bh,
+                      int64_t pitch = 0)
 {
     auto enc = tensor_map_encoder();
     if (!enc) return false;
     cuuint64_t dims[2] = {(cuuint64_t)nj, (cuuint64_t)ni};
-    cuuint64_t strides[1] = {(cuuint64_t)(nj * esize)};
+    cuuint64_t strides[1] = {(cuuint64_t)((pitch ? pitch : nj) * esize)};
     cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
     cuuint32_t es[2] = {1, 1};
     return enc(m, t, 2, const_cast<void *>(base), dims, strides, box, es,
@@ -859,12 +906,13 @@ inline bool encode_2d(CUtensorMap *m, CUtensorMapDataType t, size_t esize,
 }
 
 inline bool encode_weights(CUtensorMap *m, const void *base, int nwo, int64_t nj,
-                           int64_t ni, int bh)
+                           int64_t ni, int bh, int64_t pitch = 0)
 {
     auto enc = tensor_map_encoder();
     if (!enc) return false;
     cuuint64_t dims[3] = {(cuuint64_t)nwo, (cuuint64_t)nj, (cuuint64_t)ni};
-    cuuint64_t strides[2] = {(cuuint64_t)(nwo * 4), (cuuint64_t)(nj * nwo * 4)};
+    cuuint64_t strides[2] = {(cuuint64_t)(nwo * 4),
+                             (cuuint64_t)((pitch ? pitch : nj) * nwo * 4)};
     cuuint32_t box[3] = {4, (cuuint32_t)kTW, (cuuint32_t)bh};
     cuuint32_t es[3] = {1, 1, 1};
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(base), dims,
@@ -971,6 +1019,7 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     f.ni = (int32_t)a->ni;
     f.nj = (int32_t)a->nj;
     f.n = a->ni * a->nj;
+    f.pitch = (int32_t)a->nj;
     f.status = a->status;
     const int tiles_i = (int)((a->ni + TI - 1) / TI);
     f.tiles_j = (int)((a->nj + TJ - 1) / TJ);

@@ -4,14 +4,14 @@
 // Template parameter T is the type of the potential, the gates, the
 // currents and the concentration rates; the ion-concentration state (TP06:
 // Ca_i, Ca_SR, Ca_ss, Na_i, K_i; Courtemanche: Na_i, K_i, Ca_i, Ca_up,
-// Ca_rel) is always stored as float64.  Under FW_F64 every quantity is
-// float64 and the expressions follow the reference's evaluation order, with
-// CUDA's exp/log/sqrt/pow (a few ulp from the C library's).  Under FW_F32
-// everything is computed in float32 from the concentrations rounded to
-// float, and only the accumulation `c += dt * rate` runs in float64 -- the
-// increments are ~1e-6 of the value, below float32's resolution -- which
-// keeps the float64 pipe (a small fraction of GB300's float32 rate) out of
-// the per-node work.
+// Ca_rel; Luo-Rudy 1991: Ca_i) takes 8 bytes per node in both forms.  Under
+// FW_F64 every quantity is float64 and the expressions follow the
+// reference's evaluation order, with CUDA's exp/log/sqrt/pow (a few ulp from
+// the C library's).  Under FW_F32 everything is computed in float32 from the
+// concentrations rounded to float, and the accumulation `c += dt * rate`
+// -- increments ~1e-6 of the value, below float32's resolution -- is
+// compensated (CPair below), so no float64 arithmetic (a small fraction of
+// GB300's float32 rate) is left in the per-node work.
 //
 // Reference quirks kept: TP06 never updates Ca_i (tp06_2d.py:1098 assigns the
 // new value and then the old one); Courtemanche's IKr conductance is fixed
@@ -70,6 +70,66 @@ __device__ __forceinline__ float buffered_step(float c0, float B, float K,
     return 2.f * q / (p + sqrtf(fmaxf(p * p + 4.f * q, 0.f)));
 }
 
+// ---------------------------------------------------------------- accumulators
+// The ion-concentration accumulators.  float64 form: a double.  float32
+// form: a compensated pair of floats, the value hi + lo with |lo| at most
+// half an ulp of hi (about 48 bits of mantissa), kept in the 8 bytes per
+// node a double would take (float2 per node).  An increment d, ~1e-7 of the
+// value and below float32's resolution of it, is added with Knuth's
+// two-sum error-free transformation -- the rounding error of hi + d is
+// recovered exactly and carried in lo -- so the accumulation runs on the
+// float32 pipe (GB300's float64 rate is a small fraction of it).  The
+// rates see the value rounded to float (hi).
+struct CPair {
+    float hi, lo;
+    __device__ __forceinline__ explicit operator float() const { return hi; }
+    __device__ __forceinline__ CPair &operator+=(float d)
+    {
+        const float s = hi + d;
+        const float bp = s - hi;
+        const float e = (hi - (s - bp)) + (d - bp);
+        const float l = lo + e;
+        hi = s + l;
+        lo = l - (hi - s);
+        return *this;
+    }
+};
+
+template <class T>
+struct ConcOf {
+    using type = double;
+};
+template <>
+struct ConcOf<float> {
+    using type = CPair;
+};
+template <class T>
+using Conc = typename ConcOf<T>::type;
+
+__device__ __forceinline__ void conc_load(double &c, const void *a, int64_t p)
+{
+    c = ((const double *)a)[p];
+}
+__device__ __forceinline__ void conc_load(CPair &c, const void *a, int64_t p)
+{
+    const float2 v = ((const float2 *)a)[p];
+    c.hi = v.x;
+    c.lo = v.y;
+}
+__device__ __forceinline__ void conc_store(void *a, int64_t p, double c)
+{
+    ((double *)a)[p] = c;
+}
+__device__ __forceinline__ void conc_store(void *a, int64_t p, const CPair &c)
+{
+    ((float2 *)a)[p] = make_float2(c.hi, c.lo);
+}
+__device__ __forceinline__ double conc_probe(double c) { return c; }
+__device__ __forceinline__ double conc_probe(const CPair &c)
+{
+    return (double)c.hi + (double)c.lo;
+}
+
 // ---------------------------------------------------------------- TP06
 // Parameters in the order of tp06_2d.py's ionic_kernel_2d signature
 // (:1003-1012); state in TP062D.state_vars order minus u (:77-79).
@@ -88,18 +148,18 @@ struct ModelTP06 {
 
     template <class T>
     struct St {
-        double cai, casr, cass, nai, Ki;
+        Conc<T> cai, casr, cass, nai, Ki;
         T m, h, j, xr1, xr2, xs, r, s, d, f, f2, fcass, rr, oo;
     };
     template <class T>
     __device__ static __forceinline__ St<T> load(void *const *S, int64_t p)
     {
         St<T> x;
-        x.cai = ((const double *)S[s_cai])[p];
-        x.casr = ((const double *)S[s_casr])[p];
-        x.cass = ((const double *)S[s_cass])[p];
-        x.nai = ((const double *)S[s_nai])[p];
-        x.Ki = ((const double *)S[s_Ki])[p];
+        conc_load(x.cai, S[s_cai], p);
+        conc_load(x.casr, S[s_casr], p);
+        conc_load(x.cass, S[s_cass], p);
+        conc_load(x.nai, S[s_nai], p);
+        conc_load(x.Ki, S[s_Ki], p);
         x.m = ((const T *)S[s_m])[p];
         x.h = ((const T *)S[s_h])[p];
         x.j = ((const T *)S[s_j])[p];
@@ -121,10 +181,10 @@ struct ModelTP06 {
                                                  const St<T> &x)
     {
         // Ca_i is not written: the reference never changes it
-        ((double *)S[s_casr])[p] = x.casr;
-        ((double *)S[s_cass])[p] = x.cass;
-        ((double *)S[s_nai])[p] = x.nai;
-        ((double *)S[s_Ki])[p] = x.Ki;
+        conc_store(S[s_casr], p, x.casr);
+        conc_store(S[s_cass], p, x.cass);
+        conc_store(S[s_nai], p, x.nai);
+        conc_store(S[s_Ki], p, x.Ki);
         ((T *)S[s_m])[p] = x.m;
         ((T *)S[s_h])[p] = x.h;
         ((T *)S[s_j])[p] = x.j;
@@ -144,11 +204,11 @@ struct ModelTP06 {
     __device__ static __forceinline__ double probe(const St<T> &x, int i)
     {
         switch (i) {
-        case s_cai: return x.cai;
-        case s_casr: return x.casr;
-        case s_cass: return x.cass;
-        case s_nai: return x.nai;
-        case s_Ki: return x.Ki;
+        case s_cai: return conc_probe(x.cai);
+        case s_casr: return conc_probe(x.casr);
+        case s_cass: return conc_probe(x.cass);
+        case s_nai: return conc_probe(x.nai);
+        case s_Ki: return conc_probe(x.Ki);
         case s_m: return x.m;
         case s_h: return x.h;
         case s_j: return x.j;
@@ -356,14 +416,14 @@ struct ModelTP06 {
             x.nai += dNai;
             x.Ki += dKi;
         } else {
-            // float32 rates, float64 accumulation: the new free calcium is
-            // c0 + delta, delta the root near zero of the same quadratic
+            // float32 rates, compensated accumulation: the new free calcium
+            // is c0 + delta, delta the root near zero of the same quadratic
             // shifted to c0 (see buffered_step), so only the addition needs
-            // the float64 state
-            x.casr += (double)buffered_step(casr, P.v[Bufsr], P.v[Kbufsr], dCaSR);
-            x.cass += (double)buffered_step(cass, P.v[Bufss], P.v[Kbufss], dCaSS);
-            x.nai += (double)dNai;
-            x.Ki += (double)dKi;
+            // the accumulator's precision
+            x.casr += buffered_step(casr, P.v[Bufsr], P.v[Kbufsr], dCaSR);
+            x.cass += buffered_step(cass, P.v[Bufss], P.v[Kbufss], dCaSS);
+            x.nai += dNai;
+            x.Ki += dKi;
         }
         return un - dt * (ikr + iks + ik1 + ito + ina + ibna + ical + ibca + inak +
                           inaca + ipca + ipk);
@@ -388,18 +448,18 @@ struct ModelCRN {
 
     template <class T>
     struct St {
-        double nai, ki, cai, caup, carel;
+        Conc<T> nai, ki, cai, caup, carel;
         T m, h, j, d, f, oa, oi, ua, ui, xr, xs, fca, irel, vrel, urel, wrel;
     };
     template <class T>
     __device__ static __forceinline__ St<T> load(void *const *S, int64_t p)
     {
         St<T> x;
-        x.nai = ((const double *)S[s_nai])[p];
-        x.ki = ((const double *)S[s_ki])[p];
-        x.cai = ((const double *)S[s_cai])[p];
-        x.caup = ((const double *)S[s_caup])[p];
-        x.carel = ((const double *)S[s_carel])[p];
+        conc_load(x.nai, S[s_nai], p);
+        conc_load(x.ki, S[s_ki], p);
+        conc_load(x.cai, S[s_cai], p);
+        conc_load(x.caup, S[s_caup], p);
+        conc_load(x.carel, S[s_carel], p);
         x.m = ((const T *)S[s_m])[p];
         x.h = ((const T *)S[s_h])[p];
         x.j = ((const T *)S[s_j])[p];
@@ -422,11 +482,11 @@ struct ModelCRN {
     __device__ static __forceinline__ void store(void *const *S, int64_t p,
                                                  const St<T> &x)
     {
-        ((double *)S[s_nai])[p] = x.nai;
-        ((double *)S[s_ki])[p] = x.ki;
-        ((double *)S[s_cai])[p] = x.cai;
-        ((double *)S[s_caup])[p] = x.caup;
-        ((double *)S[s_carel])[p] = x.carel;
+        conc_store(S[s_nai], p, x.nai);
+        conc_store(S[s_ki], p, x.ki);
+        conc_store(S[s_cai], p, x.cai);
+        conc_store(S[s_caup], p, x.caup);
+        conc_store(S[s_carel], p, x.carel);
         ((T *)S[s_m])[p] = x.m;
         ((T *)S[s_h])[p] = x.h;
         ((T *)S[s_j])[p] = x.j;
@@ -448,11 +508,11 @@ struct ModelCRN {
     __device__ static __forceinline__ double probe(const St<T> &x, int i)
     {
         switch (i) {
-        case s_nai: return x.nai;
-        case s_ki: return x.ki;
-        case s_cai: return x.cai;
-        case s_caup: return x.caup;
-        case s_carel: return x.carel;
+        case s_nai: return conc_probe(x.nai);
+        case s_ki: return conc_probe(x.ki);
+        case s_cai: return conc_probe(x.cai);
+        case s_caup: return conc_probe(x.caup);
+        case s_carel: return conc_probe(x.carel);
         case s_m: return x.m;
         case s_h: return x.h;
         case s_j: return x.j;
@@ -694,7 +754,7 @@ struct ModelLR91 {
     template <class T>
     struct St {
         T m, h, j, d, f, x;
-        double cai;
+        Conc<T> cai;
     };
     template <class T>
     __device__ static __forceinline__ St<T> load(void *const *S, int64_t p)
@@ -706,7 +766,7 @@ struct ModelLR91 {
         x.d = ((const T *)S[s_d])[p];
         x.f = ((const T *)S[s_f])[p];
         x.x = ((const T *)S[s_x])[p];
-        x.cai = ((const double *)S[s_cai])[p];
+        conc_load(x.cai, S[s_cai], p);
         return x;
     }
     template <class T>
@@ -719,7 +779,7 @@ struct ModelLR91 {
         ((T *)S[s_d])[p] = x.d;
         ((T *)S[s_f])[p] = x.f;
         ((T *)S[s_x])[p] = x.x;
-        ((double *)S[s_cai])[p] = x.cai;
+        conc_store(S[s_cai], p, x.cai);
     }
     template <class T>
     __device__ static __forceinline__ double probe(const St<T> &x, int i)
@@ -731,7 +791,7 @@ struct ModelLR91 {
         case s_d: return x.d;
         case s_f: return x.f;
         case s_x: return x.x;
-        default: return x.cai;
+        default: return conc_probe(x.cai);
         }
     }
     // calc_gating_var (luo_rudy91_2d.py): tau = 1 / (a + b),

@@ -169,6 +169,7 @@ struct ProbeK {
     const T *u;
     void *state[FW_MAX_STATE];
     uint32_t f64_mask;
+    uint32_t pair_mask;
     int32_t n;
     ProbeOne pr[FW_MAX_PROBE];
     int32_t *status;
@@ -194,6 +195,10 @@ __global__ void k_probe(ProbeK<T> k)
                 x = (double)k.u[p];
             else if ((k.f64_mask >> (id - 1)) & 1u)
                 x = ((const double *)k.state[id - 1])[p];
+            else if ((k.pair_mask >> (id - 1)) & 1u) {
+                const float2 c = ((const float2 *)k.state[id - 1])[p];
+                x = (double)c.x + (double)c.y;
+            }
             else
                 x = (double)((const T *)k.state[id - 1])[p];
             P.out[(P.sample * P.n_vars + v) * (int64_t)P.n_cells + c] = x;
@@ -485,9 +490,11 @@ int run_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     ProbeK<T> pk;
     pk.status = a->status;
     for (int i = 0; i < FW_MAX_STATE; ++i) pk.state[i] = a->state[i];
-    pk.f64_mask = 0;
-    for (int i = 0; i < M::NS; ++i)
+    pk.f64_mask = pk.pair_mask = 0;
+    for (int i = 0; i < M::NS; ++i) {
         if (fw_state_is_f64(a->model, a->precision, i)) pk.f64_mask |= 1u << i;
+        if (fw_state_is_pair(a->model, a->precision, i)) pk.pair_mask |= 1u << i;
+    }
 
     const int blocks = grid_for(g.n, kThreads, 152 * 8);
     for (int64_t s = 0; s < n_steps; ++s) {

@@ -85,20 +85,41 @@ class _StateVar:
             return self
         dev = obj.__dict__.get("_dev")
         if dev and self.name in dev:
-            return _device_array(obj, self.name, dev[self.name].cpu().numpy())
+            t = dev[self.name]
+            if self.name in obj.__dict__.get("_pairs", ()):
+                h = t.cpu().numpy()
+                host = h[..., 0].astype(np.float64) + h[..., 1]
+            else:
+                host = t.cpu().numpy()
+            return _device_array(obj, self.name, host)
         return obj.__dict__.get("_host", {}).get(self.name, np.ndarray)
 
     def __set__(self, obj, value):
         dev = obj.__dict__.get("_dev")
         if dev and self.name in dev and isinstance(value, np.ndarray):
             t = dev[self.name]
-            if value.shape != tuple(t.shape):
+            pair = self.name in obj.__dict__.get("_pairs", ())
+            shape = tuple(t.shape[:-1]) if pair else tuple(t.shape)
+            if value.shape != shape:
                 raise ValueError(f"{self.name}: shape {value.shape} != "
-                                 f"{tuple(t.shape)}")
-            t.copy_(torch.as_tensor(np.ascontiguousarray(value)).to(t.dtype))
+                                 f"{shape}")
+            if pair:
+                t.copy_(torch.as_tensor(_split_pair(value)))
+            else:
+                t.copy_(torch.as_tensor(np.ascontiguousarray(value))
+                        .to(t.dtype))
             obj.__dict__["_nonmyo_equal"] = None
             return
         obj.__dict__.setdefault("_host", {})[self.name] = value
+
+
+def _split_pair(value):
+    """float64 values as compensated float32 pairs (hi, lo), hi the value
+    rounded to float32 and lo the rest rounded to float32: (..., 2)."""
+    v = np.asarray(value, dtype=np.float64)
+    hi = v.astype(np.float32)
+    lo = (v - hi.astype(np.float64)).astype(np.float32)
+    return np.ascontiguousarray(np.stack([hi, lo], axis=-1))
 
 
 class CardiacModel:
@@ -231,10 +252,19 @@ class CardiacModel:
         self._dev["u"].fill_(init_u)
         if self._reset_u_new:
             self._dev["u_new"].copy_(self._dev["u"])
+        prec = self._precision()
+        self._pairs = {n for i, n in enumerate(self._state_names)
+                       if _ffi.state_is_pair(self._model_id, prec, i)}
         for i, name in enumerate(self._state_names):
-            t = torch.empty(shape, dtype=self._torch_dtype(i), device=dev)
-            t.fill_(float(getattr(
-                self, "init_" + self._init_names.get(name, name))))
+            v = float(getattr(self, "init_" + self._init_names.get(name, name)))
+            if name in self._pairs:
+                hi, lo = _split_pair(v)
+                t = torch.empty(shape + (2,), dtype=torch.float32, device=dev)
+                t[..., 0].fill_(float(hi))
+                t[..., 1].fill_(float(lo))
+            else:
+                t = torch.empty(shape, dtype=self._torch_dtype(i), device=dev)
+                t.fill_(v)
             self._dev[name] = t
 
     def compute_weights(self):
@@ -258,6 +288,7 @@ class CardiacModel:
                              "grid are not supported: the stencil would "
                              "read outside the grid")
         dev = self._device()
+        self._n_myo = int(myo.sum())
         self._mesh_d = torch.as_tensor(np.ascontiguousarray(mesh, np.int8),
                                        device=dev)
         self._myo_d = torch.as_tensor(myo.astype(np.int8), device=dev)
@@ -489,8 +520,12 @@ class CardiacModel:
             return _ffi.FORM_FUSED
         return _ffi.FORM_FUSED if self._fused_ok() else _ffi.FORM_PLAIN
 
-    def _check_status(self):
-        st = int(self._status.item())
+    def _check_status(self, st=None):
+        """Raise (or warn) for the bits set in the device status word; `st`
+        is a copy of it already on the host, else it is read (a device
+        synchronisation)."""
+        if st is None:
+            st = int(self._status.item())
         if st & _ffi.FW_DEV_TIMEOUT:
             raise RuntimeError(f"{type(self).__name__}: a bounded on-chip "
                                "wait of the fused kernel gave up; the state "
@@ -704,8 +739,8 @@ class _HostView:
 
     def __enter__(self):
         d = self.model.__dict__
-        for n in self.names:
-            d[n] = self.model._dev[n].cpu().numpy()
+        snap = {n: np.asarray(getattr(self.model, n)) for n in self.names}
+        d.update(snap)
         return self
 
     def __exit__(self, *exc):

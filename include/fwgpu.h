@@ -81,8 +81,9 @@ enum fw_stencil {
 };
 
 /* Arithmetic policy.  FW_F64: every array float64 (the reference's default
- * npfloat).  FW_F32: u, gates and weights float32; for TP06 / Courtemanche
- * the ion-concentration state variables stay float64 (see fw_state_is_f64). */
+ * npfloat).  FW_F32: u, gates and weights float32; for TP06, Courtemanche
+ * and Luo-Rudy 1991 the ion-concentration state variables are compensated
+ * float32 pairs (see fw_state_is_pair). */
 enum fw_precision { FW_F64 = 0, FW_F32 = 1 };
 
 /* Execution form.  FW_FORM_PLAIN: one launch per time step (plus a stimulus
@@ -271,6 +272,11 @@ typedef struct fw_step_args {
     fw_tip_tracker tip[FW_MAX_TIP];
     int32_t debug_flags; /* 0 in normal use; FW_DEBUG_* bits for tests      */
     int32_t reserved2;
+    int64_t pitch;       /* row pitch in nodes of u[0], u[1], the state
+                            arrays, myo, weights and weights_packed (their
+                            N is ni * pitch); 0 = nj.  Stimulus masks and
+                            tracker arrays always have rows of nj nodes.
+                            fw_batch_plan only: fw_step takes 0 or nj     */
 } fw_step_args;
 
 /* A planned batch of tissues (fw_batch_plan).  Host-side handle; the
@@ -281,6 +287,8 @@ typedef struct fw_batch {
     int32_t n_tiles;     /* fused regions over all tissues                   */
     int32_t ksteps;      /* time steps per launch                            */
     int32_t grid;        /* persistent CTAs per launch                       */
+    int32_t kernel;      /* 1 = cp.async staging, 2 = TMA pipeline           */
+    int32_t reserved;
 } fw_batch;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -305,8 +313,15 @@ FW_API const char *fw_last_error(void);
 FW_API int fw_model_info(int32_t model, int32_t *n_state, int32_t *n_params);
 
 /* 1 when state variable `index` of `model` is stored as float64 under
- * `precision` (always 1 for FW_F64). */
+ * `precision`: every variable under FW_F64, none under FW_F32. */
 FW_API int fw_state_is_f64(int32_t model, int32_t precision, int32_t index);
+
+/* 1 when state variable `index` of `model` is stored as a compensated
+ * float32 pair under `precision`: the ion concentrations of TP06,
+ * Courtemanche and Luo-Rudy 1991 under FW_F32, 8 bytes per node (float
+ * hi, float lo: the value hi + lo, |lo| <= ulp(hi) / 2).  Other variables
+ * are stored in the precision's type. */
+FW_API int fw_state_is_pair(int32_t model, int32_t precision, int32_t index);
 
 /* Stencil weights.  Replaces Stencil.compute_weights (core/stencil/stencil.py:
  * 14) as implemented by IsotropicStencil2D (isotropic_stencil_2d.py:41-69),

@@ -76,7 +76,8 @@ def _same(a, b, where):
         assert np.array_equal(np.asarray(a), np.asarray(b)), where
 
 
-def test_batch_equals_single_fused(gc):
+@pytest.mark.parametrize("kernel", ["tma", "cp.async"])
+def test_batch_equals_single_fused(gc, kernel):
     import finitewave_gb300 as fg
     cs = _batch_cases()
     single = []
@@ -86,11 +87,12 @@ def test_batch_equals_single_fused(gc):
         m.run()
         single.append(_outputs(m, objs))
     built = [gc.build(c, npfloat="float32") for c in cs]
-    batch = fg.TissueBatch([m for m, _ in built])
+    batch = fg.TissueBatch([m for m, _ in built], kernel=kernel)
     launches0 = fg._ffi.load().fw_launch_count()
     batch.run()
     torch.cuda.synchronize()
     assert fg._ffi.load().fw_launch_count() > launches0
+    assert batch._batch.kernel == (2 if kernel == "tma" else 1)
     for i, ((m, objs), ref) in enumerate(zip(built, single)):
         got = _outputs(m, objs)
         assert got["step"] == ref["step"] and got["t"] == ref["t"], i
@@ -109,6 +111,20 @@ def test_batch_rejects_unsupported(gc):
         fg.TissueBatch([m]).run()
 
 
+class _Restimulate:
+    """Command: u = 1 on the first interior columns at time t."""
+
+    def __init__(self, t):
+        self.t, self.passed = t, False
+
+    def update_status(self, model):
+        self.passed = model.t >= self.t
+        return self.passed
+
+    def execute(self, model):
+        model.u[1:-1, 1:4] = 1.0
+
+
 def test_batch_graph_chunks_equal_direct(gc):
     """Fixed chunks replayed from captured CUDA graphs give the same result
     as direct launches (and as one long run)."""
@@ -118,6 +134,12 @@ def test_batch_graph_chunks_equal_direct(gc):
     for chunk, graphs in ((None, False), (150, False), (150, True)):
         built = [gc.build(c, npfloat="float32") for c in cs]
         b = fg.TissueBatch([m for m, _ in built], chunk=chunk, graphs=graphs)
+        # a command on the first tissue rewrites part of its potential in
+        # mid-run: its state must leave the batch's row-padded copies for
+        # the command and return afterwards
+        seq = fg.CommandSequence()
+        seq.add_command(_Restimulate(3.0))
+        built[0][0].command_sequence = seq
         b.run()
         torch.cuda.synchronize()
         if graphs:

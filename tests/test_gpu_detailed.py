@@ -1,6 +1,6 @@
 """GPU parity of the detailed ionic models (TP06, Courtemanche) through the
 public API: float64 against the reference's golden vectors, float32 (with
-float64 ion concentrations) against float64, and one ionic pass against the
+compensated float32 ion-concentration accumulators) against float64, and one ionic pass against the
 oracle.
 
 The device's exp/log/pow differ from the C library's and numpy's by an ulp or
@@ -91,8 +91,11 @@ def test_detailed_f32_close_to_f64(gc, name, dim):
     r = gc.run(case, npfloat="float32")
     m = r["model"]
     for i, v in enumerate(m._state_names):
-        want = torch.float64 if v in CONC[name] else torch.float32
-        assert m._dev[v].dtype == want, v
+        # concentrations: compensated float32 pairs, read back as float64
+        assert m._dev[v].dtype == torch.float32, v
+        assert m._dev[v].dim() == m._dev["u"].dim() + (v in CONC[name]), v
+        if v in CONC[name]:
+            assert getattr(m, v).dtype == np.float64, v
     du = float(np.max(np.abs(r["u"] - g["u"])))
     assert du < F32_U_ATOL, du
     for v in cases.MODEL_VARS[name][1:]:

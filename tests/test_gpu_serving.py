@@ -1,7 +1,9 @@
 """GPU: the request loop (SimulationServer) serves a mixed trace -- TP06,
 Courtemanche, Aliev-Panfilov and Fenton-Karma, 2D and 3D, float32 and
 float64 -- under an HBM budget that forces queueing, and every request's
-tracker outputs equal those of the same model run alone."""
+tracker outputs equal those of the same model run alone; requests on their
+own streams run on the device at the same time (their device spans
+overlap) and still give each request's results alone, bit for bit."""
 import copy
 
 import numpy as np
@@ -80,3 +82,55 @@ def test_rejects_request_over_budget(env):
     server = fg.SimulationServer(hbm_budget=1024, chunk=100)
     done = server.serve([fg.Request(m)], realtime=False)
     assert done == [] and len(server.rejected) == 1
+
+
+def _tp06_sheet(fg, n, t_max, seed):
+    rng = np.random.default_rng(seed)
+    mesh = (1 + (rng.random((n, n)) <= 0.1)).astype(np.int8)
+    mesh[0, :] = mesh[-1, :] = mesh[:, 0] = mesh[:, -1] = 0
+    tissue = fg.CardiacTissue2D((n, n))
+    tissue.mesh = mesh
+    m = fg.TP062D()
+    m.dt, m.dr, m.t_max = 0.01, 0.25, t_max
+    m.npfloat = "float64"
+    m.cardiac_tissue = tissue
+    seq = fg.StimSequence()
+    seq.add_stim(fg.StimCurrentCoord2D(0, 100, 1.0, 0, n, 1, 6))
+    m.stim_sequence = seq
+    at = fg.ActivationTime2DTracker()
+    at.threshold = -20.0
+    trs = fg.TrackerSequence()
+    trs.add_tracker(at)
+    m.tracker_sequence = trs
+    return m, at
+
+
+def test_requests_overlap_on_device(env):
+    """Three float64 TP06 sheets, each too small to fill the GPU, served
+    together on separate streams: their device spans overlap (the sum of
+    the spans exceeds their union) and each request's activation map
+    equals its run alone."""
+    fg, _ = env
+    cfg = [(192, 0.6, 1), (160, 0.6, 2), (176, 0.6, 3)]
+    alone = []
+    for n, t_max, seed in cfg:
+        m, at = _tp06_sheet(fg, n, t_max, seed)
+        m.run()
+        alone.append(at.output.copy())
+    reqs, ats = [], []
+    for i, (n, t_max, seed) in enumerate(cfg):
+        m, at = _tp06_sheet(fg, n, t_max, seed)
+        reqs.append(fg.Request(m, arrival=0.0, name=str(i)))
+        ats.append(at)
+    server = fg.SimulationServer(chunk=15, streams=4, in_flight=2)
+    server.serve(reqs, realtime=False)
+    st = server.stats()
+    assert st["completed"] == 3
+    spans = sorted(server.device_spans(), key=lambda x: x[1])
+    assert len(spans) == 3
+    assert any(spans[i + 1][1] < spans[i][2] for i in range(2)), spans
+    assert st["device_overlap"] > 1.0, st
+    for r, at, act in zip(reqs, ats, alone):
+        assert r.steps == 60
+        assert np.array_equal(at.output, act), r.name
+        assert r.snapshot() is not None

@@ -84,9 +84,10 @@ def test_batch_tile_out_of_range_raises(gc):
     b = _ffi.Batch()
     _ffi.call("fw_batch_plan", ptrs, 1, n_begin, plan.data_ptr(), size.value,
               ctypes.byref(b), stream)
-    # the tile list, (tissue, tile) int32 pairs, ends the plan: point its
-    # first entry at a tissue that does not exist
-    first_tile = size.value - 8 * b.n_tiles
+    # the tile list ends the plan, its entries start with the tissue index
+    # (int32): point the first entry at a tissue that does not exist
+    entry = 16 if b.kernel == 2 else 8
+    first_tile = size.value - entry * b.n_tiles
     plan[first_tile:first_tile + 4] = torch.tensor(
         [b.n_tissues], dtype=torch.int32).view(torch.uint8).to("cuda")
     nb = ctypes.c_int64()

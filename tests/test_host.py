@@ -182,22 +182,39 @@ def test_lat_layer_reconstruction():
 
 
 def test_detailed_model_layout(lib):
-    """TP06 / Courtemanche: state and parameter lists agree with the
-    library's counts, and under float32 exactly the ion concentrations are
-    float64 arrays."""
+    """TP06 / Courtemanche / Luo-Rudy 1991: state and parameter lists agree
+    with the library's counts; under float64 every state array is float64,
+    under float32 exactly the ion concentrations are compensated pairs."""
     import finitewave_gb300 as fg
     from finitewave_gb300 import _ffi
     conc = {fg.TP062D: {"cai", "casr", "cass", "nai", "Ki"},
-            fg.Courtemanche2D: {"nai", "ki", "cai", "caup", "carel"}}
+            fg.Courtemanche2D: {"nai", "ki", "cai", "caup", "carel"},
+            fg.LuoRudy912D: {"cai"}}
     for cls, names in conc.items():
         m = cls()
         ns, npar = _ffi.model_info(m._model_id)
         assert (len(m._state_names), len(m._param_names)) == (ns, npar)
         for i, name in enumerate(m._state_names):
             assert _ffi.state_is_f64(m._model_id, _ffi.F64, i) == 1
-            assert _ffi.state_is_f64(m._model_id, _ffi.F32, i) == \
+            assert _ffi.state_is_f64(m._model_id, _ffi.F32, i) == 0
+            assert _ffi.state_is_pair(m._model_id, _ffi.F64, i) == 0
+            assert _ffi.state_is_pair(m._model_id, _ffi.F32, i) == \
                 (name in names), name
         assert m.state_vars == ["u"] + list(m._state_names)
+
+
+def test_compensated_pair_split():
+    """Host conversion of float64 values to (hi, lo) float32 pairs: hi is
+    the value rounded to float32, hi + lo recovers it to ~2^-48."""
+    from finitewave_gb300.model import _split_pair
+    rng = np.random.default_rng(3)
+    v = np.concatenate([rng.uniform(1e-5, 1e-3, 100),
+                        rng.uniform(5, 150, 100), [0.0, 1.3, 138.3]])
+    p = _split_pair(v)
+    assert p.dtype == np.float32 and p.shape == v.shape + (2,)
+    assert np.array_equal(p[..., 0], v.astype(np.float32))
+    back = p[..., 0].astype(np.float64) + p[..., 1]
+    assert np.all(np.abs(back - v) <= np.abs(v) * 2.0 ** -46)
 
 
 def test_batch_plan_checks(lib):
