@@ -28,7 +28,7 @@ FW_DEBUG_FORCE_TIMEOUT = 1
 
 MODEL_AP, MODEL_MS, MODEL_FK, MODEL_TP06, MODEL_CRN = 1, 2, 3, 4, 5
 MODEL_BK, MODEL_BO, MODEL_LR91 = 6, 7, 8
-ISO5, ANISO9, ISO7, ANISO19, SYM9 = 1, 2, 3, 4, 5
+ISO5, ANISO9, ISO7, ANISO19, SYM9, ANISO19_XY = 1, 2, 3, 4, 5, 6
 F64, F32 = 0, 1
 FORM_PLAIN, FORM_FUSED = 0, 1
 STIM_VOLTAGE, STIM_CURRENT = 0, 1
@@ -43,8 +43,12 @@ MAX_PROBE_VARS = 8
 MAX_ECG = 2
 MAX_TIP = 1
 MAX_ECG_LEADS = 8
+MAX_FUSED_STATE = 4
 
-STENCIL_NW = {ISO5: 5, ANISO9: 9, ISO7: 7, ANISO19: 19, SYM9: 9}
+STENCIL_NW = {ISO5: 5, ANISO9: 9, ISO7: 7, ANISO19: 19, SYM9: 9,
+              ANISO19_XY: 19}
+# weight planes of the 19-point stencil that in-plane fibers leave at zero
+ANISO19_XY_ZERO = (9, 10, 13, 14, 15, 16, 17, 18)
 
 _i32, _i64, _f64, _vp = (ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
                          ctypes.c_void_p)
@@ -110,7 +114,7 @@ class StepArgs(ctypes.Structure):
                 ("ecg", EcgTracker * MAX_ECG),
                 ("tip", TipTracker * MAX_TIP),
                 ("debug_flags", _i32), ("reserved2", _i32),
-                ("pitch", _i64)]
+                ("pitch", _i64), ("state_b", _vp * MAX_FUSED_STATE)]
 
 
 class Batch(ctypes.Structure):

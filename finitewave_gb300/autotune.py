@@ -107,6 +107,9 @@ def tune(model, steps=96):
         c = model._dev[name].clone()
         keep.append(c)
         a.state[i] = c.data_ptr()
+        c = model._dev[name].clone()
+        keep.append(c)
+        a.state_b[i] = c.data_ptr()
     a.form = _ffi.FORM_FUSED
     stream = torch.cuda.current_stream()
     tma_ok = a.weights_packed and model._shape()[1] % 16 == 0

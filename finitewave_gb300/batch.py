@@ -27,9 +27,9 @@ _BATCH_MODELS = (_ffi.MODEL_AP, _ffi.MODEL_MS, _ffi.MODEL_FK)
 
 class _Mirror:
     """Copies of one model's arrays that the TMA form of the batched kernel
-    reads through tensor maps -- the two potential buffers, the state
-    variables, the myocyte flags and the weights (plus their node-major
-    packing) -- with rows padded to a multiple of 16 nodes (the row pitch a
+    reads through tensor maps -- the two potential buffers, the two buffers
+    of each state variable, the myocyte flags and the weights (plus their
+    node-major packing) -- with rows padded to a multiple of 16 nodes (the row pitch a
     tensor map needs).  The padding columns are non-myocytes holding zero
     in both potential buffers.  The batch advances the copies; `sync_in`
     and `sync_out` move the model's state between them and the model's own
@@ -56,6 +56,8 @@ class _Mirror:
                   for _ in range(2)]
         self.state = [torch.zeros((ni, self.pitch), dtype=f32, device=dev)
                       for _ in m._state_names]
+        self.state_b = [torch.zeros((ni, self.pitch), dtype=f32, device=dev)
+                        for _ in m._state_names]
 
     def valid_for(self, m):
         return m is self.model and m.weights is self.weights_src
@@ -64,8 +66,9 @@ class _Mirror:
         m, nj = self.model, self.nj
         self.u[0][:, :nj].copy_(m._dev["u"])
         self.u[1][:, :nj].copy_(m._dev["u_new"])
-        for t, name in zip(self.state, m._state_names):
+        for t, tb, name in zip(self.state, self.state_b, m._state_names):
             t[:, :nj].copy_(m._dev[name])
+            tb[:, :nj].copy_(m._dev[name])
 
     def sync_out(self):
         m, nj = self.model, self.nj
@@ -76,12 +79,14 @@ class _Mirror:
 
     def swap(self):
         self.u.reverse()
+        self.state, self.state_b = self.state_b, self.state
 
     def apply(self, a):
         """Point a tissue's fw_step_args at the copies."""
         a.u[0], a.u[1] = self.u[0].data_ptr(), self.u[1].data_ptr()
-        for i, t in enumerate(self.state):
+        for i, (t, tb) in enumerate(zip(self.state, self.state_b)):
             a.state[i] = t.data_ptr()
+            a.state_b[i] = tb.data_ptr()
         a.myo = self.myo.data_ptr()
         a.weights = self.w.data_ptr()
         a.weights_packed = self.wpack.data_ptr()

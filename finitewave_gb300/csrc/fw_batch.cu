@@ -59,7 +59,7 @@ struct BHead {
     const float *w;
     const int8_t *myo;
     float *u[2];
-    void *state[kMaxState];
+    void *state[2][kMaxState];   // both state buffers (read [in], write [in ^ 1])
     float params[kMaxParams];
     float dt;
     int32_t model, stencil;
@@ -176,7 +176,7 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
         const bool in = col_in && gi >= 0 && gi < T.ni;
         const int64_t p = in ? (int64_t)gi * T.nj + gj : 0;
         const int8_t m = T.myo[p];
-        st[r] = M::template load<float>(T.state, p);
+        st[r] = M::template load<float>(T.state[in_buf], p);
         wcen[r] = T.w[(int64_t)CEN * T.n + p];
         if (in && m) myo_bits |= 1u << r;
         if (in && col_interior && lr >= KMAX && lr < KMAX + TI) own |= 1u << r;
@@ -318,7 +318,7 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
             const float uo = S.u[fb][lr + 1][col + 1];
             u_out[p] = uo;
             if (!isfinite(uo) && T.status) atomicOr(T.status, FW_DEV_NONFINITE);
-            M::template store<float>(T.state, p, st[r]);
+            M::template store<float>(T.state[in_buf ^ 1], p, st[r]);
         }
         if (T.has_lat) T.lat_activated[p] = (lat_act >> r) & 1u;
     }
@@ -466,8 +466,9 @@ int check_tissue(const fw_step_args *a, int i)
     int ns = 0, np = 0;
     fw_model_info(a->model, &ns, &np);
     for (int s = 0; s < ns; ++s)
-        if (!a->state[s]) {
-            set_error("fw_batch: tissue %d: state %d is NULL", i, s);
+        if (!a->state[s] || !a->state_b[s] || a->state[s] == a->state_b[s]) {
+            set_error("fw_batch: tissue %d: state %d or its second buffer "
+                      "(state_b) is NULL or aliased", i, s);
             return FW_ERR_ARG;
         }
     for (int k = 0; k < a->n_at; ++k)
@@ -516,6 +517,7 @@ struct alignas(128) BTissueT {
     BWin at_win[fused::kMaxFusedAt];
     BWin lat_win[fused::kMaxFusedLat];
     float *u[2];
+    void *state[2][FW_MAX_FUSED_STATE];
     int64_t step_base;
 };
 
@@ -566,6 +568,10 @@ __global__ void k_batch_events(BTissueT *__restrict__ tissues, int32_t n,
         F.ksteps = ks;
         F.u_in = T.u[in_buf];
         F.u_out = T.u[in_buf ^ 1];
+        for (int q = 0; q < FW_MAX_FUSED_STATE; ++q) {
+            F.state[q] = T.state[in_buf][q];
+            F.state_out[q] = T.state[in_buf ^ 1][q];
+        }
     }
 }
 
@@ -613,8 +619,8 @@ __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
     tensormap_acquire(&M.w);
     tensormap_acquire(&M.myo);
     tensormap_acquire(&M.u[in_buf]);
-    tensormap_acquire(&M.s[0]);
-    tensormap_acquire(&M.s[1]);
+    tensormap_acquire(&M.s[in_buf][0]);
+    tensormap_acquire(&M.s[in_buf][1]);
     tensormap_acquire(&M.wc);
     // one arrive on the stage's barrier announces the region's bytes and
     // the launch description's, which rides on the same barrier
@@ -760,7 +766,7 @@ bool tma_tissue_ok(const fw_step_args *a)
     int ns = 0, np = 0;
     fw_model_info(a->model, &ns, &np);
     for (int q = 0; q < ns; ++q)
-        if (!aligned16(a->state[q])) return false;
+        if (!aligned16(a->state[q]) || !aligned16(a->state_b[q])) return false;
     return fused::tensor_map_encoder() != nullptr;
 }
 
@@ -784,11 +790,14 @@ int fill_tma_tissue(const fw_step_args *a, int64_t n_begin, BTissueT &T)
               encode_2d(&T.maps.wc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
                         (const float *)a->weights + (int64_t)cen * a->ni * pitch,
                         a->nj, a->ni, kBoxF, LH, pitch);
-    // the map of a second state array exists for every tissue (the kernel
-    // acquires it); models with one state variable map the first twice
-    for (int q = 0; q < 2 && ok; ++q)
-        ok = encode_2d(&T.maps.s[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
-                       a->state[q < ns ? q : 0], a->nj, a->ni, kBoxF, LH, pitch);
+    // maps of two state arrays in both buffers exist for every tissue (the
+    // kernel acquires them); models with one state variable map the first
+    // twice
+    void *const *sbuf[2] = {a->state, a->state_b};
+    for (int b = 0; b < 2; ++b)
+        for (int q = 0; q < 2 && ok; ++q)
+            ok = encode_2d(&T.maps.s[b][q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                           sbuf[b][q < ns ? q : 0], a->nj, a->ni, kBoxF, LH, pitch);
     if (!ok) {
         set_error("fw_batch_plan: tensor map encoding failed");
         return FW_ERR_UNSUPPORTED;
@@ -796,7 +805,9 @@ int fill_tma_tissue(const fw_step_args *a, int64_t n_begin, BTissueT &T)
     FusedK &f = T.f;
     f.w = nullptr;
     f.myo = a->myo;
-    for (int i = 0; i < FW_MAX_STATE; ++i) f.state[i] = a->state[i];
+    for (int b = 0; b < 2; ++b)
+        for (int q = 0; q < FW_MAX_FUSED_STATE; ++q)
+            T.state[b][q] = q < ns ? sbuf[b][q] : nullptr;
     for (int i = 0; i < FW_MAX_PARAMS; ++i) f.params[i] = (float)a->params[i];
     f.dt = (float)a->dt;
     f.ni = (int32_t)a->ni;
@@ -941,7 +952,10 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
             T.u[1] = (float *)a->u[1];
             int ns = 0, np = 0;
             fw_model_info(a->model, &ns, &np);
-            for (int s = 0; s < kMaxState; ++s) T.state[s] = s < ns ? a->state[s] : nullptr;
+            for (int s = 0; s < kMaxState; ++s) {
+                T.state[0][s] = s < ns ? a->state[s] : nullptr;
+                T.state[1][s] = s < ns ? a->state_b[s] : nullptr;
+            }
             for (int p = 0; p < kMaxParams; ++p) T.params[p] = p < np ? (float)a->params[p] : 0.f;
             T.dt = (float)a->dt;
             T.model = a->model;

@@ -92,7 +92,12 @@ struct alignas(16) FusedK {
     const int8_t *myo;
     const float *u_in;
     float *u_out;
-    void *state[FW_MAX_STATE];
+    // the launch reads the state from `state` and writes the tiles' new
+    // state to `state_out` (the other buffer, fw_step_args.state_b): a
+    // region's halo state is then never one a neighbouring tile of the same
+    // launch has already advanced
+    void *state[FW_MAX_FUSED_STATE];
+    void *state_out[FW_MAX_FUSED_STATE];
     // float32 parameters, rounded on the host: in the kernel they are plain
     // constant-bank operands (no float64 conversion on the device)
     float params[FW_MAX_PARAMS];
@@ -533,7 +538,7 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
             const float uo = S.u[fb][lr + 1][col + 1];
             k.u_out[p] = uo;
             if (!isfinite(uo) && k.status) atomicOr(k.status, FW_DEV_NONFINITE);
-            M::template store<float>(k.state, p, st[r]);
+            M::template store<float>(k.state_out, p, st[r]);
         }
 #pragma unroll
         for (int l = 0; l < kMaxFusedLat; ++l)
@@ -650,7 +655,7 @@ int launch_fused(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     memset(&k, 0, sizeof k);
     k.w = (const float *)a->weights;
     k.myo = a->myo;
-    for (int i = 0; i < FW_MAX_STATE; ++i) k.state[i] = a->state[i];
+    void *const *sbuf[2] = {a->state, a->state_b};
     for (int i = 0; i < FW_MAX_PARAMS; ++i) k.params[i] = (float)a->params[i];
     k.dt = (float)a->dt;
     k.ni = (int32_t)a->ni;
@@ -678,6 +683,10 @@ int launch_fused(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         k.ksteps = (int32_t)ks;
         k.u_in = (const float *)a->u[li & 1];
         k.u_out = (float *)a->u[(li + 1) & 1];
+        for (int q = 0; q < FW_MAX_FUSED_STATE; ++q) {
+            k.state[q] = sbuf[li & 1][q];
+            k.state_out[q] = sbuf[(li + 1) & 1][q];
+        }
         int rc = fill_events(a, k, n0, n1, ks, probe_samples);
         if (rc) return rc;
         kern<<<(unsigned)blocks, NT, SMEM, stream>>>(k);

@@ -60,7 +60,7 @@ struct TmaMaps {
     CUtensorMap w;      // packed weights: dims (NWO, nj, ni)
     CUtensorMap myo;    // int8 (nj, ni)
     CUtensorMap u[2];   // f32 (nj, ni), the two potential buffers
-    CUtensorMap s[kMaxTmaState];
+    CUtensorMap s[2][kMaxTmaState];  // the state arrays, both buffers
     CUtensorMap wc;     // the centre weight plane, f32 (nj, ni)
 };
 
@@ -204,7 +204,8 @@ __device__ __forceinline__ void issue_region(const TmaMaps &maps, int in_buf,
     }
     tma_2d(&G.u[0][0], &maps.u[in_buf], x4, oi - 1, bar);
 #pragma unroll
-    for (int q = 0; q < NS; ++q) tma_2d(&G.s[q][0][0], &maps.s[q], x4, oi, bar);
+    for (int q = 0; q < NS; ++q)
+        tma_2d(&G.s[q][0][0], &maps.s[in_buf][q], x4, oi, bar);
     tma_2d(&G.myo[0][0], &maps.myo, x16, oi, bar);
     tma_2d(&G.wc[0][0], &maps.wc, x4, oi, bar);
 }
@@ -453,7 +454,7 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
             const float uo = fin[lr + 1][col + xo];
             f.u_out[pp] = uo;
             nonfinite |= !isfinite(uo);
-            M::template store<float>(f.state, pp, st[r]);
+            M::template store<float>(f.state_out, pp, st[r]);
         }
 #pragma unroll
         for (int l = 0; l < kMaxFusedLat; ++l)
@@ -860,7 +861,7 @@ __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
                 const float uo = fin[lr + 1][cx + (j & 1)];
                 f.u_out[p] = uo;
                 nonfinite |= !isfinite(uo);
-                M::template store<float>(f.state, p, st[j]);
+                M::template store<float>(f.state_out, p, st[j]);
             }
 #pragma unroll
             for (int l = 0; l < kMaxFusedLat; ++l)
@@ -959,7 +960,8 @@ inline bool tma_usable(const fw_step_args *a, int ns)
     bool ok = aligned16(a->weights_packed) && aligned16(a->weights) &&
               aligned16(a->u[0]) && aligned16(a->u[1]) && aligned16(a->myo) &&
               a->nj % 16 == 0 && a->ni < (1 << 30) && a->nj < (1 << 30);
-    for (int q = 0; q < ns && ok; ++q) ok = aligned16(a->state[q]);
+    for (int q = 0; q < ns && ok; ++q)
+        ok = aligned16(a->state[q]) && aligned16(a->state_b[q]);
     return ok && tensor_map_encoder() != nullptr;
 }
 
@@ -998,8 +1000,10 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
               encode_2d(&k.maps.u[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->u[1],
                         a->nj, a->ni, kBoxF, LH + 2);
     for (int q = 0; q < M::NS && ok; ++q)
-        ok = encode_2d(&k.maps.s[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->state[q],
-                       a->nj, a->ni, kBoxF, LH);
+        ok = encode_2d(&k.maps.s[0][q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                       a->state[q], a->nj, a->ni, kBoxF, LH) &&
+             encode_2d(&k.maps.s[1][q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                       a->state_b[q], a->nj, a->ni, kBoxF, LH);
     // the centre plane of the (nw, ni * nj) float32 weights
     const float *wcen_plane = (const float *)a->weights +
                               (int64_t)Stencil2D<ST>::CENTRE * a->ni * a->nj;
@@ -1013,7 +1017,7 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     FusedK &f = k.f;
     f.w = nullptr;
     f.myo = a->myo;
-    for (int i = 0; i < FW_MAX_STATE; ++i) f.state[i] = a->state[i];
+    void *const *sbuf[2] = {a->state, a->state_b};
     for (int i = 0; i < FW_MAX_PARAMS; ++i) f.params[i] = (float)a->params[i];
     f.dt = (float)a->dt;
     f.ni = (int32_t)a->ni;
@@ -1044,6 +1048,10 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         k.in_buf = (int32_t)(li & 1);
         f.u_in = (const float *)a->u[li & 1];
         f.u_out = (float *)a->u[(li + 1) & 1];
+        for (int q = 0; q < FW_MAX_FUSED_STATE; ++q) {
+            f.state[q] = sbuf[li & 1][q];
+            f.state_out[q] = sbuf[(li + 1) & 1][q];
+        }
         int rc = fill_events(a, f, n0, n1, ks, probe_samples);
         if (rc) return rc;
         kern<<<grid, NT, SMEM, stream>>>(k);
@@ -1067,6 +1075,14 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 {
     const int k = a->fused_k ? a->fused_k : 4;
     int v = a->fused_variant;
+    static_assert(M::NS <= FW_MAX_FUSED_STATE, "fused state buffers");
+    for (int q = 0; q < M::NS; ++q)
+        if (!a->state_b[q] || a->state_b[q] == a->state[q]) {
+            set_error("fw_step (fused): state_b[%d] missing or equal to "
+                      "state[%d] (the fused form needs a second buffer per "
+                      "state variable)", q, q);
+            return FW_ERR_ARG;
+        }
     if (v == 0) v = tma_usable(a, M::NS) ? 3 : 1;
     if ((v == 3 || v == 4) && !tma_usable(a, M::NS)) {
         set_error("fw_step (fused): the TMA kernels need packed weights, "

@@ -36,6 +36,7 @@ inline int stencil_nw(int st)
     case FW_STENCIL_ISO7: return 7;
     case FW_STENCIL_ANISO19: return 19;
     case FW_STENCIL_SYM9: return 9;
+    case FW_STENCIL_ANISO19_XY: return 19;
     }
     return 0;
 }
@@ -94,6 +95,16 @@ __device__ __forceinline__ T diffuse_node(const T *__restrict__ u,
         return u[p - si] * w[p] + u[p - sj] * w[n + p] + u[p - 1] * w[2 * n + p] +
                u[p] * w[3 * n + p] + u[p + 1] * w[4 * n + p] +
                u[p + sj] * w[5 * n + p] + u[p + si] * w[6 * n + p];
+    } else if constexpr (ST == FW_STENCIL_ANISO19_XY) {
+        // asymmetric_stencil_3d.py:140-158 without the terms of planes 9,
+        // 10 and 13-18, which are zero for in-plane fibers (adding them
+        // changes no sum), in the same order
+        return u[p - si - sj] * w[p] + u[p - si] * w[n + p] +
+               u[p - si + sj] * w[2 * n + p] + u[p - sj] * w[3 * n + p] +
+               u[p] * w[4 * n + p] + u[p + sj] * w[5 * n + p] +
+               u[p + si - sj] * w[6 * n + p] + u[p + si] * w[7 * n + p] +
+               u[p + si + sj] * w[8 * n + p] + u[p - 1] * w[11 * n + p] +
+               u[p + 1] * w[12 * n + p];
     } else {
         // asymmetric_stencil_3d.py:140-158
         return u[p - si - sj] * w[p] + u[p - si] * w[n + p] +

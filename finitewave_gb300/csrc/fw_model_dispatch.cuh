@@ -42,6 +42,7 @@ int dispatch_stencil(int32_t stencil, int32_t precision, const F &f)
         FW_ST_CASE(FW_STENCIL_ANISO9)
         FW_ST_CASE(FW_STENCIL_ISO7)
         FW_ST_CASE(FW_STENCIL_ANISO19)
+        FW_ST_CASE(FW_STENCIL_ANISO19_XY)
     }
 #undef FW_ST_CASE
     set_error("unknown stencil %d", stencil);

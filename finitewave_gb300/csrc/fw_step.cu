@@ -94,6 +94,7 @@ int ecg(int32_t stencil, int32_t precision, const void *u, const void *w,
         ECG_CASE(FW_STENCIL_ANISO9)
         ECG_CASE(FW_STENCIL_ISO7)
         ECG_CASE(FW_STENCIL_ANISO19)
+        ECG_CASE(FW_STENCIL_ANISO19_XY)
     }
 #undef ECG_CASE
     return FW_ERR_ARG;
@@ -125,6 +126,7 @@ int diffuse(int32_t stencil, int32_t precision, void *u_new, const void *u,
     case FW_STENCIL_ANISO9: LAUNCH(FW_STENCIL_ANISO9); break;
     case FW_STENCIL_ISO7: LAUNCH(FW_STENCIL_ISO7); break;
     case FW_STENCIL_ANISO19: LAUNCH(FW_STENCIL_ANISO19); break;
+    case FW_STENCIL_ANISO19_XY: LAUNCH(FW_STENCIL_ANISO19_XY); break;
     }
 #undef LAUNCH
     FW_CHECK_LAUNCH("k_diffuse");

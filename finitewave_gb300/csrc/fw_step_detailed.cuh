@@ -24,6 +24,8 @@ int plain_detailed(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         return run_plain<M, FW_STENCIL_ISO7, T>(a, n_begin, n_steps, stream);
     case FW_STENCIL_ANISO19:
         return run_plain<M, FW_STENCIL_ANISO19, T>(a, n_begin, n_steps, stream);
+    case FW_STENCIL_ANISO19_XY:
+        return run_plain<M, FW_STENCIL_ANISO19_XY, T>(a, n_begin, n_steps, stream);
     }
     set_error("unknown stencil %d", a->stencil);
     return FW_ERR_ARG;

@@ -404,6 +404,8 @@ int build_weights(int32_t stencil, int32_t precision, const int8_t *mesh,
                   double dr2, int64_t ni, int64_t nj, int64_t nk, void *w_out,
                   cudaStream_t stream)
 {
+    // the in-plane-fiber form of the 3D stencil is built as the full one
+    if (stencil == FW_STENCIL_ANISO19_XY) stencil = FW_STENCIL_ANISO19;
     int nw = stencil_nw(stencil);
     if (!nw) {
         set_error("fw_build_weights: unknown stencil %d", stencil);

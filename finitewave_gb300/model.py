@@ -108,6 +108,11 @@ class _StateVar:
             else:
                 t.copy_(torch.as_tensor(np.ascontiguousarray(value))
                         .to(t.dtype))
+            other = obj.__dict__.get("_stateb", {}).get(self.name)
+            if other is not None:
+                # the fused form's second buffer equals the state at
+                # non-myocytes (and is overwritten at myocytes)
+                other.copy_(t)
             obj.__dict__["_nonmyo_equal"] = None
             return
         obj.__dict__.setdefault("_host", {})[self.name] = value
@@ -266,6 +271,12 @@ class CardiacModel:
                 t = torch.empty(shape, dtype=self._torch_dtype(i), device=dev)
                 t.fill_(v)
             self._dev[name] = t
+        # second state buffers of the fused form (fw_step_args.state_b): a
+        # fused launch reads the state from one and writes the other
+        self._stateb = {}
+        if (prec == _ffi.F32 and len(shape) == 2 and
+                self._model_id in self._FUSED_MODELS):
+            self._stateb = {n: self._dev[n].clone() for n in self._state_names}
 
     def compute_weights(self):
         """Myocyte indices, stencil choice and device weights
@@ -297,6 +308,12 @@ class CardiacModel:
         if self.stencil is None:
             self.stencil = self.select_stencil(tissue)
         self.weights = self.stencil.compute_weights(self, tissue)
+        self._step_stencil = self.stencil.kind
+        if self.stencil.kind == _ffi.ANISO19 and not bool(
+                self.weights[list(_ffi.ANISO19_XY_ZERO)].any()):
+            # fibers with no z component: the eight planes coupling k +- 1
+            # with i +- 1 or j +- 1 are zero, and the step skips them
+            self._step_stencil = _ffi.ANISO19_XY
         self._pack_weights()
 
     def _pack_weights(self):
@@ -567,7 +584,7 @@ class CardiacModel:
         choice, and no stimuli or trackers."""
         a = _ffi.StepArgs()
         a.model = self._model_id
-        a.stencil = self.stencil.kind
+        a.stencil = getattr(self, "_step_stencil", self.stencil.kind)
         a.precision = self._precision()
         shape = self._shape()
         a.ni, a.nj = shape[0], shape[1]
@@ -581,6 +598,9 @@ class CardiacModel:
         a.u[1] = self._dev["u_new"].data_ptr()
         for i, name in enumerate(self._state_names):
             a.state[i] = self._dev[name].data_ptr()
+            t = getattr(self, "_stateb", {}).get(name)
+            if t is not None:
+                a.state_b[i] = t.data_ptr()
         for i, p in enumerate(self._params()):
             a.params[i] = p
         a.dt = float(self.dt)
@@ -718,10 +738,15 @@ class CardiacModel:
 
     def _finish_segment(self, seg):
         """Account for a segment the device has been given: swap u / u_new
-        after an odd step count, advance t and step."""
+        (and, after a fused segment, the two state buffers) after an odd
+        step count, advance t and step."""
         if seg.n_seg % 2 == 1:
             self._dev["u"], self._dev["u_new"] = (self._dev["u_new"],
                                                   self._dev["u"])
+            if seg.args.form == _ffi.FORM_FUSED:
+                sb = self._stateb
+                for n in self._state_names:
+                    self._dev[n], sb[n] = sb[n], self._dev[n]
         self.t = seg.t_end
         self.step = seg.n0 + seg.n_seg
 

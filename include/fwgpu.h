@@ -76,8 +76,15 @@ enum fw_stencil {
     FW_STENCIL_ANISO9 = 2,  /* AsymmetricStencil2D  (i-1,j-1)...(i+1,j+1)                 */
     FW_STENCIL_ISO7 = 3,    /* IsotropicStencil3D   order of isotropic_stencil_3d.py:16-23  */
     FW_STENCIL_ANISO19 = 4, /* AsymmetricStencil3D  order of asymmetric_stencil_3d.py:25-44 */
-    FW_STENCIL_SYM9 = 5     /* SymmetricStencil2D weights (fw_build_weights only): the
+    FW_STENCIL_SYM9 = 5,    /* SymmetricStencil2D weights (fw_build_weights only): the
                                9-point layout of ANISO9, stepped as ANISO9      */
+    FW_STENCIL_ANISO19_XY = 6 /* ANISO19 weights whose planes 9, 10, 13..18 (the
+                               couplings of k +- 1 with i +- 1 or j +- 1) are all
+                               zero, as AsymmetricStencil3D builds them for fibers
+                               with no z component: stepped reading the other 11
+                               planes (the skipped terms are exact zeros, so the
+                               sums are the ANISO19 ones); stored and built as
+                               ANISO19 (19 planes)                              */
 };
 
 /* Arithmetic policy.  FW_F64: every array float64 (the reference's default
@@ -105,6 +112,7 @@ enum fw_stim_kind { FW_STIM_VOLTAGE = 0, FW_STIM_CURRENT = 1 };
 #define FW_MAX_TIP 1
 #define FW_MAX_ECG 2
 #define FW_MAX_ECG_LEADS 8
+#define FW_MAX_FUSED_STATE 4
 
 /* A set of global step indices n with first <= n <= last and
  * n % stride == 0.  Trackers are active on exactly those steps; the host
@@ -277,6 +285,16 @@ typedef struct fw_step_args {
                             N is ni * pitch); 0 = nj.  Stimulus masks and
                             tracker arrays always have rows of nj nodes.
                             fw_batch_plan only: fw_step takes 0 or nj     */
+    void *state_b[FW_MAX_FUSED_STATE]; /* FW_FORM_FUSED and batches: second
+                            buffers of the state variables (same type and
+                            size as state[], equal to them at non-myocytes).
+                            A launch reads every region's state from one
+                            buffer and writes its tiles' new state to the
+                            other, so no region reads state a neighbouring
+                            tile has already advanced.  The buffers change
+                            roles with u[0] / u[1]: on return the current
+                            state is in state[] after an even number of
+                            steps and in state_b[] after an odd one      */
 } fw_step_args;
 
 /* A planned batch of tissues (fw_batch_plan).  Host-side handle; the

@@ -330,3 +330,92 @@ def test_diffusion_and_ionic_callables(fg, gc, oracle):
                   oracle.MODELS["ap"]["params"])
     assert np.array_equal(model.u_new, un)
     assert np.array_equal(model.v, v)
+
+
+@pytest.mark.parametrize("npfloat", ["float64", "float32"])
+@pytest.mark.parametrize("model", ["ap", "tp06"])
+def test_in_plane_fibers_skip_zero_planes(gc, model, npfloat):
+    """Fibers with no z component leave the eight 19-point weight planes
+    that couple k +- 1 with i +- 1 or j +- 1 at zero; the model then steps
+    with the 11-plane form (FW_STENCIL_ANISO19_XY), whose sums equal the
+    full stencil's bit for bit (the skipped terms are exact zeros)."""
+    from finitewave_gb300 import _ffi
+    case, _ = cases.ap3d(True)
+    fib = np.array(case["fibers"], dtype=np.float64)
+    phi = np.linspace(-np.pi / 3, np.pi / 3, fib.shape[2])
+    fib[..., 0] = np.cos(phi)[None, None, :]
+    fib[..., 1] = np.sin(phi)[None, None, :]
+    fib[..., 2] = 0.0
+    case = dict(case, fibers=fib, model=model)
+    if model == "tp06":
+        case["t_max"] = 4
+        case["stims"] = [dict(kind="current", t=0, value=80, duration=1.0,
+                              box=[(0, 12), (0, 11), (1, 3)])]
+        case["trackers"] = [dict(kind="at", threshold=-20.0)]
+    outs = []
+    for force_full in (False, True):
+        m, objs = gc.build(case, npfloat=npfloat)
+        m.initialize()
+        assert m._step_stencil == _ffi.ANISO19_XY
+        m._step_stencil = _ffi.ANISO19 if force_full else _ffi.ANISO19_XY
+        m.run(initialize=False)
+        outs.append((m.u, objs[0].output, getattr(m, m._state_names[-1])))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    assert np.any(outs[0][0] != outs[0][0].flat[0])
+
+
+def _wave_case():
+    """Aliev-Panfilov 770 x 1024 (more fused regions than the GPU runs at
+    once), 9-point stencil with smooth fibers, 20 % fibrosis, S1 and an S2
+    on the lower-left quadrant at t = 3, activation tracker."""
+    import scipy.ndimage as nd
+    ni, nj = 770, 1024
+    rng = np.random.default_rng(77)
+    mesh = (1 + (rng.random((ni, nj)) <= 0.2)).astype(np.int8)
+    mesh[0, :] = mesh[-1, :] = mesh[:, 0] = mesh[:, -1] = 0
+    g = nd.gaussian_filter(rng.standard_normal((ni, nj)), 16)
+    th = (np.pi / 4) * g / np.abs(g).max()
+    fib = np.stack([np.cos(th), np.sin(th)], -1)
+    return dict(model="ap", mesh=mesh, fibers=fib, stencil="aniso9",
+                dt=0.01, dr=0.25, t_max=12.0,
+                stims=[dict(kind="voltage", t=0, value=1.0,
+                            box=[(0, ni), (1, 6)]),
+                       dict(kind="voltage", t=3, value=1.0,
+                            box=[(ni // 2, ni), (0, nj // 2)])],
+                trackers=[dict(kind="at", threshold=0.5)])
+
+
+def test_fused_bits_do_not_depend_on_tile_order(gc):
+    """With many waves of regions per launch, every fused kernel and both
+    batched kernels give the same bits, in one segment or in an odd one
+    followed by the rest: each launch reads its regions' state from one
+    buffer and writes the new state to the other, so no region sees state
+    that a neighbouring region of the same launch has already advanced."""
+    import finitewave_gb300 as fg
+    case = _wave_case()
+
+    def out(m, objs):
+        return m.u, m.v, objs[0].output
+
+    runs = {}
+    for v in (1, 3, 4):
+        m, objs = gc.build(case, npfloat="float32", form="fused", fused_k=4,
+                           fused_variant=v)
+        m.run()
+        runs[f"v{v}"] = out(m, objs)
+    m, objs = gc.build(case, npfloat="float32", form="fused", fused_k=4,
+                       fused_variant=3)
+    m.initialize()
+    # the same 1200 steps as two device segments, an odd one first
+    assert m._run_segment(555) + m._run_segment(645) == 1200
+    runs["v3_split"] = out(m, objs)
+    for kernel in ("tma", "cp.async"):
+        m, objs = gc.build(case, npfloat="float32")
+        fg.TissueBatch([m], kernel=kernel, chunk=301).run()
+        runs["batch_" + kernel] = out(m, objs)
+    ref = runs.pop("v1")
+    assert np.any(ref[2] > 3.0)        # the S2 wave activated nodes
+    for k, r in runs.items():
+        for a, b in zip(r, ref):
+            assert np.array_equal(a, b), k

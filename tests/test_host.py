@@ -229,6 +229,7 @@ def test_batch_plan_checks(lib):
         a.ni, a.nj, a.nk = ni, nj, 1
         a.weights = a.myo = a.u[0] = a.u[1] = 0x1000
         a.state[0] = a.state[1] = 0x1000
+        a.state_b[0] = a.state_b[1] = 0x2000
         a.n_probe = n_probe
         return a
 
@@ -240,6 +241,10 @@ def test_batch_plan_checks(lib):
 
     rc, one = size([tissue(100, 100)])
     assert rc == _ffi.FW_OK and one > 0
+    # the fused batch needs a second buffer per state variable
+    t = tissue(100, 100)
+    t.state_b[0] = 0
+    assert size([t])[0] == _ffi.FW_ERR_ARG
     rc, two = size([tissue(100, 100), tissue(100, 100)])
     assert rc == _ffi.FW_OK and two > one
     rc, big = size([tissue(1000, 1000)])
