@@ -120,7 +120,7 @@ class StepArgs(ctypes.Structure):
 class Batch(ctypes.Structure):
     _fields_ = [("plan", _vp), ("n_tissues", _i32), ("n_tiles", _i32),
                 ("ksteps", _i32), ("grid", _i32), ("kernel", _i32),
-                ("reserved", _i32)]
+                ("reserved", _i32), ("group_end", _i32 * 6)]
 
 
 class FwError(RuntimeError):

@@ -528,13 +528,22 @@ struct BTileT {
     int32_t oi, oj;        // region origin
 };
 
+template <int NS, int NWO>
 struct BatchTmaSmem {
-    fused::TmaSmem<LH, 2, 8> t;
+    fused::TmaSmem<LH, NS, NWO> t;
     fused::FusedK f[2];    // launch description of each stage's tile
-    int tile[2];           // the stage's tile index (>= n_tiles: none)
+    int tile[2];           // the stage's tile index (>= the group's end: none)
     int oi[2], oj[2];      // its region origin
-    int key[2];            // model * 8 + stencil, -1 for a skipped tile
+    int ok[2];             // 0 for a skipped tile
 };
+
+// The batch's (model, stencil) groups, in the order the plan sorts tiles;
+// each group is advanced by its own instantiation of k_batch_tma.
+constexpr int kGroups = 6;
+constexpr int kGroupKey[kGroups] = {
+    FW_MODEL_AP * 8 + FW_STENCIL_ISO5, FW_MODEL_AP * 8 + FW_STENCIL_ANISO9,
+    FW_MODEL_MS * 8 + FW_STENCIL_ISO5, FW_MODEL_MS * 8 + FW_STENCIL_ANISO9,
+    FW_MODEL_FK * 8 + FW_STENCIL_ISO5, FW_MODEL_FK * 8 + FW_STENCIL_ANISO9};
 
 // The per-launch fields of every tissue's launch description: step window
 // masks of the stimuli and trackers, first step, step count and the
@@ -591,20 +600,23 @@ __device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned b
         : "memory");
 }
 
-// Thread 0: stage tile t (list entry bt) into stage sg.
+// Thread 0: stage tile t (list entry bt) into stage sg.  The tensor maps
+// of a tissue are acquired once for a run of tiles of the same tissue.
+template <class M, int ST, class Sm>
 __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
-                                         int32_t n_tiles, int32_t n_tissues,
-                                         int32_t in_buf, BatchTmaSmem &S, int sg,
-                                         int t, BTileT bt)
+                                         int32_t t_end, int32_t n_tissues,
+                                         int32_t in_buf, Sm &S, int sg, int t,
+                                         BTileT bt, int &acquired)
 {
+    constexpr int NWO = fused::Stencil2D<ST>::NWO;
     S.tile[sg] = t;
-    if (t >= n_tiles) return;
+    if (t >= t_end) return;
     uint64_t *bar = &S.t.bar[sg];
     fused::fence_proxy_async();
     if (bt.tissue < 0 || bt.tissue >= n_tissues) {
         // a corrupted plan: flag it and complete the stage's phase without
         // data, so that the tile is skipped
-        S.key[sg] = -1;
+        S.ok[sg] = 0;
         if (tissues[0].f.status) atomicOr(tissues[0].f.status, FW_DEV_BATCH_FAULT);
         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(
                          fused::smem_u32(bar))
@@ -612,59 +624,40 @@ __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
         return;
     }
     const BTissueT &T = tissues[bt.tissue];
-    S.key[sg] = bt.key;
+    S.ok[sg] = 1;
     S.oi[sg] = bt.oi;
     S.oj[sg] = bt.oj;
-    const fused::TmaMaps &M = T.maps;
-    tensormap_acquire(&M.w);
-    tensormap_acquire(&M.myo);
-    tensormap_acquire(&M.u[in_buf]);
-    tensormap_acquire(&M.s[in_buf][0]);
-    tensormap_acquire(&M.s[in_buf][1]);
-    tensormap_acquire(&M.wc);
+    const fused::TmaMaps &Mp = T.maps;
+    if (bt.tissue != acquired) {
+        tensormap_acquire(&Mp.w);
+        tensormap_acquire(&Mp.myo);
+        tensormap_acquire(&Mp.u[in_buf]);
+        tensormap_acquire(&Mp.wc);
+#pragma unroll
+        for (int q = 0; q < M::NS; ++q) tensormap_acquire(&Mp.s[in_buf][q]);
+        acquired = bt.tissue;
+    }
     // one arrive on the stage's barrier announces the region's bytes and
     // the launch description's, which rides on the same barrier
     constexpr unsigned kF = (unsigned)sizeof(fused::FusedK);
-    auto &G = S.t.stage[sg];
-    switch (bt.key) {
-    case FW_MODEL_AP * 8 + FW_STENCIL_ISO5:
-    case FW_MODEL_MS * 8 + FW_STENCIL_ISO5:
-        fused::issue_region<KMAX, 1, 4>(M, in_buf, G, bar, bt.oi, bt.oj, kF);
-        break;
-    case FW_MODEL_AP * 8 + FW_STENCIL_ANISO9:
-    case FW_MODEL_MS * 8 + FW_STENCIL_ANISO9:
-        fused::issue_region<KMAX, 1, 8>(M, in_buf, G, bar, bt.oi, bt.oj, kF);
-        break;
-    case FW_MODEL_FK * 8 + FW_STENCIL_ISO5:
-        fused::issue_region<KMAX, 2, 4>(M, in_buf, G, bar, bt.oi, bt.oj, kF);
-        break;
-    default:  // FK, ANISO9 (the plan admits no other key)
-        fused::issue_region<KMAX, 2, 8>(M, in_buf, G, bar, bt.oi, bt.oj, kF);
-        break;
-    }
+    fused::issue_region<KMAX, M::NS, NWO>(Mp, in_buf, S.t.stage[sg], bar, bt.oi,
+                                          bt.oj, kF);
     bulk_copy(&S.f[sg], &T.f, kF, bar);
 }
 
+// One (model, stencil) group of the batch: tiles [t_begin, t_end) of the
+// list, taken from counters[0] (counters[1] counts the CTAs that are done;
+// the last one zeroes both).
 template <class M, int ST>
-__device__ __forceinline__ void batch_tile(BatchTmaSmem &S, int sg, uint32_t own_c,
-                                           uint32_t ring_c)
-{
-    const fused::FusedK &f = S.f[sg];
-    Params<float, M::NP> P;
-#pragma unroll
-    for (int i = 0; i < M::NP; ++i) P.v[i] = f.params[i];
-    fused::tma_tile<M, ST, KMAX, LH, kTmaR>(f, S.t.stage[sg], S.t, S.oi[sg], S.oj[sg],
-                                           own_c, ring_c, P);
-}
-
 __global__ void __launch_bounds__(kTmaNT, 1)
     k_batch_tma(const BTissueT *__restrict__ tissues, const BTileT *__restrict__ tiles,
-                int32_t n_tiles, int32_t n_tissues, int32_t in_buf, uint32_t *scratch)
+                int32_t t_begin, int32_t t_end, int32_t n_tissues, int32_t in_buf,
+                uint32_t *counters)
 {
+    using Sm = BatchTmaSmem<M::NS, fused::Stencil2D<ST>::NWO>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned mis = fused::smem_u32(smem_raw) & 127u;
-    BatchTmaSmem &S =
-        *reinterpret_cast<BatchTmaSmem *>(smem_raw + (mis ? 128u - mis : 0u));
+    Sm &S = *reinterpret_cast<Sm *>(smem_raw + (mis ? 128u - mis : 0u));
     const int tid = threadIdx.x;
     uint32_t own_c, ring_c;
     fused::strip_masks<KMAX, LH, kTmaR>(tid % fused::kTW, (tid / fused::kTW) * kTmaR,
@@ -672,34 +665,35 @@ __global__ void __launch_bounds__(kTmaNT, 1)
     const BTileT none{-1, -1, 0, 0};
     // thread 0's look-ahead: tile i + 1 (index and entry) and tile i + 2
     // (index) while tile i is computed
-    int t_next = n_tiles, t_after = n_tiles;
+    int t_next = t_end, t_after = t_end, acquired = -1;
     BTileT b_next = none;
     if (tid == 0) {
         fused::mbar_init(&S.t.bar[0], 1);
         fused::mbar_init(&S.t.bar[1], 1);
         fused::mbar_fence_init();
-        const int t0 = (int)atomicAdd(&scratch[0], 1u);
-        if (t0 < n_tiles) {
-            t_next = (int)atomicAdd(&scratch[0], 1u);
-            if (t_next < n_tiles) t_after = (int)atomicAdd(&scratch[0], 1u);
+        const int t0 = t_begin + (int)atomicAdd(&counters[0], 1u);
+        if (t0 < t_end) {
+            t_next = t_begin + (int)atomicAdd(&counters[0], 1u);
+            if (t_next < t_end) t_after = t_begin + (int)atomicAdd(&counters[0], 1u);
         }
-        batch_issue(tissues, n_tiles, n_tissues, in_buf, S, 0, t0,
-                    t0 < n_tiles ? tiles[t0] : none);
-        if (t_next < n_tiles) b_next = tiles[t_next];
+        batch_issue<M, ST>(tissues, t_end, n_tissues, in_buf, S, 0, t0,
+                           t0 < t_end ? tiles[t0] : none, acquired);
+        if (t_next < t_end) b_next = tiles[t_next];
     }
     __syncthreads();
     unsigned parity = 0u;
     for (int it = 0;; ++it) {
         const int sg = it & 1;
-        if (S.tile[sg] >= n_tiles) break;
+        if (S.tile[sg] >= t_end) break;
         if (tid == 0) {
             // the other stage's readers finished at the barrier that closed
             // the previous iteration
-            batch_issue(tissues, n_tiles, n_tissues, in_buf, S, sg ^ 1, t_next,
-                        b_next);
+            batch_issue<M, ST>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1, t_next,
+                               b_next, acquired);
             t_next = t_after;
-            b_next = t_next < n_tiles ? tiles[t_next] : none;
-            t_after = t_next < n_tiles ? (int)atomicAdd(&scratch[0], 1u) : n_tiles;
+            b_next = t_next < t_end ? tiles[t_next] : none;
+            t_after = t_next < t_end ? t_begin + (int)atomicAdd(&counters[0], 1u)
+                                     : t_end;
         }
         const unsigned ph = (parity >> sg) & 1u;
         const bool arrived = fused::mbar_wait(&S.t.bar[sg], ph);
@@ -709,46 +703,70 @@ __global__ void __launch_bounds__(kTmaNT, 1)
                 // flag it, then wait (bounded) for the copies in flight
                 if (tissues[0].f.status) atomicOr(tissues[0].f.status, FW_DEV_TIMEOUT);
                 if (!arrived) fused::mbar_wait(&S.t.bar[sg], ph);
-                if (S.tile[sg ^ 1] < n_tiles)
+                if (S.tile[sg ^ 1] < t_end)
                     fused::mbar_wait(&S.t.bar[sg ^ 1], (parity >> (sg ^ 1)) & 1u);
             }
             break;
         }
-        switch (S.key[sg]) {
-        case FW_MODEL_AP * 8 + FW_STENCIL_ISO5:
-            batch_tile<ModelAP, FW_STENCIL_ISO5>(S, sg, own_c, ring_c);
-            break;
-        case FW_MODEL_AP * 8 + FW_STENCIL_ANISO9:
-            batch_tile<ModelAP, FW_STENCIL_ANISO9>(S, sg, own_c, ring_c);
-            break;
-        case FW_MODEL_MS * 8 + FW_STENCIL_ISO5:
-            batch_tile<ModelMS, FW_STENCIL_ISO5>(S, sg, own_c, ring_c);
-            break;
-        case FW_MODEL_MS * 8 + FW_STENCIL_ANISO9:
-            batch_tile<ModelMS, FW_STENCIL_ANISO9>(S, sg, own_c, ring_c);
-            break;
-        case FW_MODEL_FK * 8 + FW_STENCIL_ISO5:
-            batch_tile<ModelFK, FW_STENCIL_ISO5>(S, sg, own_c, ring_c);
-            break;
-        case FW_MODEL_FK * 8 + FW_STENCIL_ANISO9:
-            batch_tile<ModelFK, FW_STENCIL_ANISO9>(S, sg, own_c, ring_c);
-            break;
-        default:
-            break;  // skipped (flagged when it was taken)
+        if (S.ok[sg]) {
+            const fused::FusedK &f = S.f[sg];
+            Params<float, M::NP> P;
+#pragma unroll
+            for (int i = 0; i < M::NP; ++i) P.v[i] = f.params[i];
+            fused::tma_tile<M, ST, KMAX, LH, kTmaR>(f, S.t.stage[sg], S.t, S.oi[sg],
+                                                   S.oj[sg], own_c, ring_c, P);
         }
         __syncthreads();
     }
     if (tid == 0) {
         __threadfence();
-        if (atomicAdd(&scratch[1], 1u) == gridDim.x - 1) {
-            atomicExch(&scratch[0], 0u);
-            atomicExch(&scratch[1], 0u);
+        if (atomicAdd(&counters[1], 1u) == gridDim.x - 1) {
+            atomicExch(&counters[0], 0u);
+            atomicExch(&counters[1], 0u);
         }
     }
 }
 
-constexpr size_t kTmaSmem = sizeof(BatchTmaSmem) + 128;
-static_assert(kTmaSmem <= 232448, "the batched TMA stages exceed 227 KB");
+template <class M, int ST>
+constexpr size_t tma_smem()
+{
+    return sizeof(BatchTmaSmem<M::NS, fused::Stencil2D<ST>::NWO>) + 128;
+}
+static_assert(tma_smem<ModelFK, FW_STENCIL_ANISO9>() <= 232448,
+              "the batched TMA stages exceed 227 KB");
+
+// Launch group g's kernel (or set its shared-memory attribute when
+// `attr_only`).
+inline int batch_group_launch(int g, bool attr_only, int grid,
+                              const BTissueT *desc, const BTileT *tl, int32_t t_begin,
+                              int32_t t_end, int32_t n_tissues, int32_t in_buf,
+                              uint32_t *counters, cudaStream_t stream)
+{
+#define FW_BATCH_GROUP(GI, M, ST)                                                 \
+    case GI:                                                                      \
+        if (attr_only) {                                                          \
+            FW_CUDA_CHECK(cudaFuncSetAttribute(                                   \
+                k_batch_tma<M, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                (int)tma_smem<M, ST>()));                                         \
+            return FW_OK;                                                         \
+        }                                                                         \
+        k_batch_tma<M, ST><<<grid, kTmaNT, tma_smem<M, ST>(), stream>>>(          \
+            desc, tl, t_begin, t_end, n_tissues, in_buf, counters);               \
+        FW_CHECK_LAUNCH("k_batch_tma");                                           \
+        return FW_OK;
+    switch (g) {
+        FW_BATCH_GROUP(0, ModelAP, FW_STENCIL_ISO5)
+        FW_BATCH_GROUP(1, ModelAP, FW_STENCIL_ANISO9)
+        FW_BATCH_GROUP(2, ModelMS, FW_STENCIL_ISO5)
+        FW_BATCH_GROUP(3, ModelMS, FW_STENCIL_ANISO9)
+        FW_BATCH_GROUP(4, ModelFK, FW_STENCIL_ISO5)
+        FW_BATCH_GROUP(5, ModelFK, FW_STENCIL_ANISO9)
+    }
+#undef FW_BATCH_GROUP
+    set_error("fw_batch: no group %d", g);
+    return FW_ERR_ARG;
+}
+
 static_assert(sizeof(fused::FusedK) % 16 == 0 && offsetof(BTissueT, f) % 16 == 0,
               "the launch description moves as one bulk copy");
 
@@ -1036,10 +1054,13 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     FW_CUDA_CHECK(cudaGetDevice(&dev));
     FW_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (kernel == 2) {
-        FW_CUDA_CHECK(cudaFuncSetAttribute(
-            k_batch_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaSmem));
-        FW_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_batch_tma, kTmaNT, kTmaSmem));
+        // one persistent CTA per SM (the stages fill its shared memory)
+        for (int g = 0; g < kGroups; ++g) {
+            int rc2 = batch_group_launch(g, true, 0, nullptr, nullptr, 0, 0, 0, 0,
+                                         nullptr, stream);
+            if (rc2) return rc2;
+        }
+        per_sm = 1;
     } else {
         FW_CUDA_CHECK(cudaFuncSetAttribute(
             k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
@@ -1055,6 +1076,14 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     out->ksteps = KMAX;
     out->grid = (int32_t)grid;
     out->kernel = kernel;
+    // cumulative tile counts of the (model, stencil) groups in list order
+    for (int g = 0; g < kGroups; ++g) {
+        int32_t end = 0;
+        for (int i = 0; i < n; ++i)
+            if (tissues[i]->model * 8 + tissues[i]->stencil <= kGroupKey[g])
+                end += (int32_t)tissue_tiles(tissues[i]);
+        out->group_end[g] = end;
+    }
     out->reserved = 0;
     return FW_OK;
 }
@@ -1080,13 +1109,16 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     FW_CUDA_CHECK(cudaStreamIsCapturing(stream, &cap));
     if (cap == cudaStreamCaptureStatusNone) {
-        if (tma)
-            FW_CUDA_CHECK(cudaFuncSetAttribute(k_batch_tma,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kTmaSmem));
-        else
+        if (tma) {
+            for (int g = 0; g < kGroups; ++g) {
+                int rc = batch_group_launch(g, true, 0, nullptr, nullptr, 0, 0, 0, 0,
+                                            nullptr, stream);
+                if (rc) return rc;
+            }
+        } else {
             FW_CUDA_CHECK(cudaFuncSetAttribute(
                 k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
+        }
     }
     const size_t desc_bytes = tma ? sizeof(BTissueT) : sizeof(BTissue);
     const BTissue *desc = reinterpret_cast<const BTissue *>(b->plan);
@@ -1110,9 +1142,20 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
             k_batch_events<<<(unsigned)((b->n_tissues + 3) / 4), eb, 0, stream>>>(
                 desc_t, b->n_tissues, offset + done, (int32_t)ks, in_buf);
             FW_CHECK_LAUNCH("k_batch_events");
-            k_batch_tma<<<b->grid, kTmaNT, kTmaSmem, stream>>>(
-                desc_t, tl_t, b->n_tiles, b->n_tissues, in_buf, scratch);
-            FW_CHECK_LAUNCH("k_batch_tma");
+            // one kernel per (model, stencil) group, each on its own pair
+            // of counters
+            int32_t begin = 0;
+            for (int g = 0; g < kGroups; ++g) {
+                const int32_t end = b->group_end[g];
+                if (end > begin) {
+                    const int grid = end - begin < b->grid ? end - begin : b->grid;
+                    int rc = batch_group_launch(g, false, grid, desc_t, tl_t, begin,
+                                                end, b->n_tissues, in_buf,
+                                                scratch + 2 + 2 * g, stream);
+                    if (rc) return rc;
+                }
+                begin = end;
+            }
         } else {
             k_batch<<<b->grid, NT, kSmem, stream>>>(desc, tl, b->n_tiles,
                                                    b->n_tissues, offset + done,

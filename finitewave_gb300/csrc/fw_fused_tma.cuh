@@ -334,13 +334,31 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
                 }
         }
 
+    // the launch's per-sub-step controls, read once per tile (the batched
+    // kernel keeps its launch description in shared memory)
+    const int ksteps = f.ksteps;
+    const int64_t n0 = f.n0;
+    const uint32_t stim_on = f.stim_on, probe_on = f.probe_on;
+    uint32_t at_on[kMaxFusedAt], lat_on[kMaxFusedLat];
+    float at_thr[kMaxFusedAt], lat_thr[kMaxFusedLat];
+#pragma unroll
+    for (int a = 0; a < kMaxFusedAt; ++a) {
+        at_on[a] = a < f.n_at ? f.at[a].on : 0u;
+        at_thr[a] = f.at[a].thr;
+    }
+#pragma unroll
+    for (int l = 0; l < kMaxFusedLat; ++l) {
+        lat_on[l] = l < f.n_lat ? f.lat[l].on : 0u;
+        lat_thr[l] = f.lat[l].thr;
+    }
+
     // ---- sub-steps ----
-    for (int s = 0; s < f.ksteps; ++s) {
-        const int64_t n = f.n0 + s;
+    for (int s = 0; s < ksteps; ++s) {
+        const int64_t n = n0 + s;
         float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
         float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;
 
-        if ((f.stim_on >> s) & 1u) {
+        if ((stim_on >> s) & 1u) {
             for (int i = 0; i < f.n_stims; ++i) {
                 const FStim &F = f.stims[i];
                 if (!((F.on >> s) & 1u)) continue;
@@ -375,15 +393,15 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
         if (own) {
 #pragma unroll
             for (int a = 0; a < kMaxFusedAt; ++a) {
-                if (a >= f.n_at || !((f.at[a].on >> s) & 1u)) continue;
+                if (!((at_on[a] >> s) & 1u)) continue;
                 // the strip's maximum first: most sub-steps cross nowhere
                 // (fmaxf skips NaN rows, which never cross)
                 float mx = wc[1];
 #pragma unroll
                 for (int r = 1; r < R; ++r) mx = fmaxf(mx, wc[r + 1]);
-                if (!(mx > f.at[a].thr)) continue;
+                if (!(mx > at_thr[a])) continue;
                 const uint32_t hit =
-                    rows_gt<R>(wc, f.at[a].thr) & own & ~(at_done >> (a * 8));
+                    rows_gt<R>(wc, at_thr[a]) & own & ~(at_done >> (a * 8));
                 if (hit) {
 #pragma unroll
                     for (int r = 0; r < R; ++r) {
@@ -399,11 +417,11 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
             }
 #pragma unroll
             for (int l = 0; l < kMaxFusedLat; ++l) {
-                if (l >= f.n_lat || !((f.lat[l].on >> s) & 1u)) continue;
+                if (!((lat_on[l] >> s) & 1u)) continue;
                 // (local_activation_time_2d_tracker.py:71-89)
                 const uint32_t was = (lat_act >> (l * 8)) & 0xffu;
-                const uint32_t rise = rows_ge<R>(wc, f.lat[l].thr) & own & ~was;
-                const uint32_t fall = rows_lt<R>(wc, f.lat[l].thr) & own & was;
+                const uint32_t rise = rows_ge<R>(wc, lat_thr[l]) & own & ~was;
+                const uint32_t fall = rows_lt<R>(wc, lat_thr[l]) & own & was;
                 lat_act ^= (rise | fall) << (l * 8);
                 if (rise) {
 #pragma unroll
@@ -430,7 +448,7 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
             nxt[lr + 1][col + xo] = ((upd >> r) & 1u) ? uu : b1;
         }
         // probes: u after the stimuli, the state after the update
-        if (probe_mine && ((f.probe_on >> s) & 1u)) {
+        if (probe_mine && ((probe_on >> s) & 1u)) {
 #pragma unroll
             for (int r = 0; r < R; ++r)
                 if ((probe_mine >> r) & 1u)
@@ -443,7 +461,7 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
     }
 
     // ---- write the interior back ----
-    float(*fin)[kBoxF] = (f.ksteps & 1) ? S.u1 : G.u;
+    float(*fin)[kBoxF] = (ksteps & 1) ? S.u1 : G.u;
     bool nonfinite = false;
 #pragma unroll
     for (int r = 0; r < R; ++r) {

@@ -307,6 +307,10 @@ typedef struct fw_batch {
     int32_t grid;        /* persistent CTAs per launch                       */
     int32_t kernel;      /* 1 = cp.async staging, 2 = TMA pipeline           */
     int32_t reserved;
+    int32_t group_end[6]; /* kernel 2: end of each (model, stencil) group in
+                             the tile list -- AP/ISO5, AP/ANISO9, MS/ISO5,
+                             MS/ANISO9, FK/ISO5, FK/ANISO9 -- each advanced by
+                             its own kernel launch                          */
 } fw_batch;
 
 /* Library version (major*10000 + minor*100 + patch). */
