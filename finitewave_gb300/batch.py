@@ -28,11 +28,12 @@ _BATCH_MODELS = (_ffi.MODEL_AP, _ffi.MODEL_MS, _ffi.MODEL_FK)
 class _Mirror:
     """Copies of one model's arrays that the TMA form of the batched kernel
     reads through tensor maps -- the two potential buffers, the two buffers
-    of each state variable, the myocyte flags and the weights (plus their
-    node-major packing) -- with rows padded to a multiple of 16 nodes (the row pitch a
-    tensor map needs).  The padding columns are non-myocytes holding zero
-    in both potential buffers.  The batch advances the copies; `sync_in`
-    and `sync_out` move the model's state between them and the model's own
+    of each state variable, the myocyte flags, the weights (plus their
+    node-major packing) and the local activation tracker's flags -- with
+    rows padded to a multiple of 16 nodes (the row pitch a tensor map
+    needs).  The padding columns are non-myocytes holding zero in both
+    potential buffers.  The batch advances the copies; `sync_in` and
+    `sync_out` move the model's state between them and the model's own
     arrays, and `swap` follows the model's u / u_new exchange."""
 
     def __init__(self, m):
@@ -58,24 +59,50 @@ class _Mirror:
                       for _ in m._state_names]
         self.state_b = [torch.zeros((ni, self.pitch), dtype=f32, device=dev)
                         for _ in m._state_names]
+        # device address of a tracker's flags -> (flags, padded copy)
+        self.act = {}
 
     def valid_for(self, m):
         return m is self.model and m.weights is self.weights_src
 
+    def _lat_flags(self):
+        seq = self.model.tracker_sequence
+        if not seq:
+            return []
+        return [tr._activated for tr in seq.sequence
+                if isinstance(tr, LocalActivationTime2DTracker)
+                and tracker.is_native(tr)
+                and getattr(tr, "_activated", None) is not None]
+
     def sync_in(self):
         m, nj = self.model, self.nj
+        ni = self.u[0].shape[0]
         self.u[0][:, :nj].copy_(m._dev["u"])
         self.u[1][:, :nj].copy_(m._dev["u_new"])
         for t, tb, name in zip(self.state, self.state_b, m._state_names):
             t[:, :nj].copy_(m._dev[name])
             tb[:, :nj].copy_(m._dev[name])
+        act = {}
+        for f in self._lat_flags():
+            old = self.act.get(f.data_ptr())
+            if old is not None and old[0] is f:
+                pad = old[1]
+            else:
+                pad = torch.zeros((ni, self.pitch), dtype=torch.uint8,
+                                  device=f.device)
+            pad[:, :nj].copy_(f.view(ni, nj))
+            act[f.data_ptr()] = (f, pad)
+        self.act = act
 
     def sync_out(self):
         m, nj = self.model, self.nj
+        ni = self.u[0].shape[0]
         m._dev["u"].copy_(self.u[0][:, :nj])
         m._dev["u_new"].copy_(self.u[1][:, :nj])
         for t, name in zip(self.state, m._state_names):
             m._dev[name].copy_(t[:, :nj])
+        for f, pad in self.act.values():
+            f.view(ni, nj).copy_(pad[:, :nj])
 
     def swap(self):
         self.u.reverse()
@@ -90,6 +117,12 @@ class _Mirror:
         a.myo = self.myo.data_ptr()
         a.weights = self.w.data_ptr()
         a.weights_packed = self.wpack.data_ptr()
+        for k in range(a.n_lat):
+            pad = self.act.get(a.lat[k].activated)
+            if pad is None:
+                raise RuntimeError("TissueBatch: a local activation tracker "
+                                   "was not set up before the run")
+            a.lat[k].activated = pad[1].data_ptr()
         a.pitch = self.pitch
         a.fused_variant = 0
 

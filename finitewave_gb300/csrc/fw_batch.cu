@@ -524,9 +524,12 @@ struct alignas(128) BTissueT {
 // One entry of the TMA form's tile list.
 struct BTileT {
     int32_t tissue;
-    int32_t key;           // model * 8 + stencil
+    int32_t key;           // model * 8 + stencil, | kTileLat
     int32_t oi, oj;        // region origin
 };
+// BTileT.key: the tissue has a local activation tracker, whose flags are
+// staged with the region
+constexpr int32_t kTileLat = 1 << 8;
 
 template <int NS, int NWO>
 struct BatchTmaSmem {
@@ -628,6 +631,7 @@ __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
     S.oi[sg] = bt.oi;
     S.oj[sg] = bt.oj;
     const fused::TmaMaps &Mp = T.maps;
+    const bool lat = (bt.key & kTileLat) != 0;
     if (bt.tissue != acquired) {
         tensormap_acquire(&Mp.w);
         tensormap_acquire(&Mp.myo);
@@ -635,13 +639,14 @@ __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
         tensormap_acquire(&Mp.wc);
 #pragma unroll
         for (int q = 0; q < M::NS; ++q) tensormap_acquire(&Mp.s[in_buf][q]);
+        if (lat) tensormap_acquire(&Mp.act);
         acquired = bt.tissue;
     }
     // one arrive on the stage's barrier announces the region's bytes and
     // the launch description's, which rides on the same barrier
     constexpr unsigned kF = (unsigned)sizeof(fused::FusedK);
     fused::issue_region<KMAX, M::NS, NWO>(Mp, in_buf, S.t.stage[sg], bar, bt.oi,
-                                          bt.oj, kF);
+                                          bt.oj, kF, lat);
     bulk_copy(&S.f[sg], &T.f, kF, bar);
 }
 
@@ -659,6 +664,10 @@ __global__ void __launch_bounds__(kTmaNT, 1)
     const unsigned mis = fused::smem_u32(smem_raw) & 127u;
     Sm &S = *reinterpret_cast<Sm *>(smem_raw + (mis ? 128u - mis : 0u));
     const int tid = threadIdx.x;
+    // the next group's kernel, launched with programmatic serialisation,
+    // may place its CTAs on the SMs this grid's CTAs leave (its tissues are
+    // not this group's, so nothing it reads is written here)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     uint32_t own_c, ring_c;
     fused::strip_masks<KMAX, LH, kTmaR>(tid % fused::kTW, (tid / fused::kTW) * kTmaR,
                                         own_c, ring_c);
@@ -719,6 +728,10 @@ __global__ void __launch_bounds__(kTmaNT, 1)
         __syncthreads();
     }
     if (tid == 0) {
+        // this grid completes only after the group's kernel launched before
+        // it (a no-op without programmatic serialisation), so the stream's
+        // next ordinary launch finds every group of the launch finished
+        asm volatile("griddepcontrol.wait;" ::: "memory");
         __threadfence();
         if (atomicAdd(&counters[1], 1u) == gridDim.x - 1) {
             atomicExch(&counters[0], 0u);
@@ -736,12 +749,23 @@ static_assert(tma_smem<ModelFK, FW_STENCIL_ANISO9>() <= 232448,
               "the batched TMA stages exceed 227 KB");
 
 // Launch group g's kernel (or set its shared-memory attribute when
-// `attr_only`).
-inline int batch_group_launch(int g, bool attr_only, int grid,
+// `attr_only`).  `overlap`: launched with programmatic stream serialisation,
+// so that its CTAs start as the previous group's CTAs finish instead of
+// after the whole previous grid (the groups' tissues are disjoint).
+inline int batch_group_launch(int g, bool attr_only, bool overlap, int grid,
                               const BTissueT *desc, const BTileT *tl, int32_t t_begin,
                               int32_t t_end, int32_t n_tissues, int32_t in_buf,
                               uint32_t *counters, cudaStream_t stream)
 {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = overlap ? 1 : 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kTmaNT);
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
 #define FW_BATCH_GROUP(GI, M, ST)                                                 \
     case GI:                                                                      \
         if (attr_only) {                                                          \
@@ -750,8 +774,10 @@ inline int batch_group_launch(int g, bool attr_only, int grid,
                 (int)tma_smem<M, ST>()));                                         \
             return FW_OK;                                                         \
         }                                                                         \
-        k_batch_tma<M, ST><<<grid, kTmaNT, tma_smem<M, ST>(), stream>>>(          \
-            desc, tl, t_begin, t_end, n_tissues, in_buf, counters);               \
+        cfg.dynamicSmemBytes = tma_smem<M, ST>();                                 \
+        FW_CUDA_CHECK(cudaLaunchKernelEx(&cfg, k_batch_tma<M, ST>, desc, tl,      \
+                                         t_begin, t_end, n_tissues, in_buf,       \
+                                         counters));                              \
         FW_CHECK_LAUNCH("k_batch_tma");                                           \
         return FW_OK;
     switch (g) {
@@ -773,7 +799,8 @@ static_assert(sizeof(fused::FusedK) % 16 == 0 && offsetof(BTissueT, f) % 16 == 0
 inline bool aligned16(const void *p) { return p && ((uintptr_t)p & 15) == 0; }
 
 // The TMA form can take this tissue: rows (the pitch) a multiple of 16
-// nodes, every TMA-read array 16-byte aligned, packed weights.
+// nodes, every TMA-read array (the local activation flags included)
+// 16-byte aligned, packed weights.
 bool tma_tissue_ok(const fw_step_args *a)
 {
     const int64_t pitch = a->pitch ? a->pitch : a->nj;
@@ -785,6 +812,8 @@ bool tma_tissue_ok(const fw_step_args *a)
     fw_model_info(a->model, &ns, &np);
     for (int q = 0; q < ns; ++q)
         if (!aligned16(a->state[q]) || !aligned16(a->state_b[q])) return false;
+    for (int l = 0; l < a->n_lat; ++l)
+        if (!aligned16(a->lat[l].activated)) return false;
     return fused::tensor_map_encoder() != nullptr;
 }
 
@@ -816,6 +845,10 @@ int fill_tma_tissue(const fw_step_args *a, int64_t n_begin, BTissueT &T)
         for (int q = 0; q < 2 && ok; ++q)
             ok = encode_2d(&T.maps.s[b][q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
                            sbuf[b][q < ns ? q : 0], a->nj, a->ni, kBoxF, LH, pitch);
+    // the local activation flags (rows of `pitch` nodes, like the state)
+    if (ok && a->n_lat > 0)
+        ok = encode_2d(&T.maps.act, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1,
+                       a->lat[0].activated, a->nj, a->ni, kBoxB, LH, pitch);
     if (!ok) {
         set_error("fw_batch_plan: tensor map encoding failed");
         return FW_ERR_UNSUPPORTED;
@@ -1037,7 +1070,9 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
             BTileT *tl = reinterpret_cast<BTileT *>(tiles_host);
             const int32_t tj = (int32_t)((a->nj + TJ - 1) / TJ);
             for (int32_t k = 0; k < nt; ++k)
-                tl[t_count + k] = BTileT{i, a->model * 8 + a->stencil,
+                tl[t_count + k] = BTileT{i,
+                                         a->model * 8 + a->stencil +
+                                             (a->n_lat ? kTileLat : 0),
                                          (k / tj) * TI - KMAX, (k % tj) * TJ - KMAX};
         } else {
             BTile *tl = reinterpret_cast<BTile *>(tiles_host);
@@ -1056,7 +1091,7 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     if (kernel == 2) {
         // one persistent CTA per SM (the stages fill its shared memory)
         for (int g = 0; g < kGroups; ++g) {
-            int rc2 = batch_group_launch(g, true, 0, nullptr, nullptr, 0, 0, 0, 0,
+            int rc2 = batch_group_launch(g, true, false, 0, nullptr, nullptr, 0, 0, 0, 0,
                                          nullptr, stream);
             if (rc2) return rc2;
         }
@@ -1111,7 +1146,7 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
     if (cap == cudaStreamCaptureStatusNone) {
         if (tma) {
             for (int g = 0; g < kGroups; ++g) {
-                int rc = batch_group_launch(g, true, 0, nullptr, nullptr, 0, 0, 0, 0,
+                int rc = batch_group_launch(g, true, false, 0, nullptr, nullptr, 0, 0, 0, 0,
                                             nullptr, stream);
                 if (rc) return rc;
             }
@@ -1144,15 +1179,19 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
             FW_CHECK_LAUNCH("k_batch_events");
             // one kernel per (model, stencil) group, each on its own pair
             // of counters
+            // of a launch: the first after k_batch_events in stream order,
+            // the others overlapping the one before
             int32_t begin = 0;
+            bool first = true;
             for (int g = 0; g < kGroups; ++g) {
                 const int32_t end = b->group_end[g];
                 if (end > begin) {
                     const int grid = end - begin < b->grid ? end - begin : b->grid;
-                    int rc = batch_group_launch(g, false, grid, desc_t, tl_t, begin,
-                                                end, b->n_tissues, in_buf,
+                    int rc = batch_group_launch(g, false, !first, grid, desc_t, tl_t,
+                                                begin, end, b->n_tissues, in_buf,
                                                 scratch + 2 + 2 * g, stream);
                     if (rc) return rc;
+                    first = false;
                 }
                 begin = end;
             }

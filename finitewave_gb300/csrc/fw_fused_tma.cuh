@@ -44,6 +44,7 @@ struct TmaStage {
     alignas(128) float s[NS][LH][kBoxF];               // rows oi .. oi + LH - 1
     alignas(128) int8_t myo[LH][kBoxB];
     alignas(128) float wc[LH][kBoxF];                  // centre weights, rows oi ..
+    alignas(128) uint8_t act[LH][kBoxB];               // local activation flags
 };
 
 template <int LH, int NS, int NWO>
@@ -62,7 +63,9 @@ struct TmaMaps {
     CUtensorMap u[2];   // f32 (nj, ni), the two potential buffers
     CUtensorMap s[2][kMaxTmaState];  // the state arrays, both buffers
     CUtensorMap wc;     // the centre weight plane, f32 (nj, ni)
+    CUtensorMap act;    // the local activation tracker's flags, u8 (nj, ni)
 };
+static_assert(kMaxFusedLat == 1, "one tensor map of local activation flags");
 
 struct TmaK {
     TmaMaps maps;
@@ -182,19 +185,23 @@ __device__ __forceinline__ int floor_to(int x, int m)
 // laid out for more (the batched kernel's stages hold the largest model).
 // PAIRS: the weight map is the column-pair view of encode_weights_pairs, and
 // the weights land as [row][column parity][column pair] (k_fused_tma2).
+// `lat`: also the local activation tracker's flags (maps.act).
 // The barrier has an arrival count of one: this is the stage's only
 // arrive, and it announces the region's bytes plus `extra` bytes of other
 // copies the caller issues on the same barrier.
 template <int KMAX, int NS, int NWO, bool PAIRS = false, class Stage>
 __device__ __forceinline__ void issue_region(const TmaMaps &maps, int in_buf,
                                              Stage &G, uint64_t *bar, int oi,
-                                             int oj, unsigned extra = 0)
+                                             int oj, unsigned extra = 0,
+                                             bool lat = false)
 {
     const int x4 = floor_to(oj - 1, 4), x16 = floor_to(oj, 16);
     const unsigned bytes = (unsigned)(sizeof(G.wa) * (NWO == 8 ? 2 : 1) +
                                       sizeof(G.u) + NS * sizeof(G.s[0]) +
-                                      sizeof(G.myo) + sizeof(G.wc));
+                                      sizeof(G.myo) + sizeof(G.wc)) +
+                           (lat ? (unsigned)sizeof(G.act) : 0u);
     mbar_expect_tx(bar, bytes + extra);
+    if (lat) tma_2d(&G.act[0][0], &maps.act, x16, oi, bar);
     if constexpr (PAIRS) {
         tma_4d(&G.wa[0][0], &maps.w, 0, oj / 2, 0, oi, bar);
         if constexpr (NWO == 8) tma_4d(&G.wb[0][0], &maps.w, 4, oj / 2, 0, oi, bar);
@@ -215,8 +222,9 @@ __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> 
                                            uint64_t *bar, int bi, int bj)
 {
     constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
+    // the column-pair kernel reads the flags from global memory
     issue_region<KMAX, NS, NWO, PAIRS>(k.maps, k.in_buf, G, bar, bi * TI - KMAX,
-                                       bj * TJ - KMAX);
+                                       bj * TJ - KMAX, 0u, !PAIRS && k.f.n_lat > 0);
 }
 
 // Rows r < R of the strip of thread (col, r0) inside the region's interior
@@ -322,17 +330,14 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
                 probe_mine |= 1u << r;
         }
     }
+    // the local activation flags of the strip, staged with the region
     uint32_t lat_act = 0, at_done = 0;
+    if (f.n_lat) {
 #pragma unroll
-    for (int l = 0; l < kMaxFusedLat; ++l)
-        if (l < f.n_lat) {
-#pragma unroll
-            for (int r = 0; r < R; ++r)
-                if ((own >> r) & 1u) {
-                    const int64_t p = (int64_t)(oi + r0 + r) * f.nj + gj;
-                    if (f.lat[l].activated[p]) lat_act |= 1u << (l * 8 + r);
-                }
-        }
+        for (int r = 0; r < R; ++r)
+            if (((own >> r) & 1u) && G.act[r0 + r][col + xo8]) lat_act |= 1u << r;
+    }
+    const uint32_t lat_act0 = lat_act;
 
     // the launch's per-sub-step controls, read once per tile (the batched
     // kernel keeps its launch description in shared memory)
@@ -474,11 +479,9 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
             nonfinite |= !isfinite(uo);
             M::template store<float>(f.state_out, pp, st[r]);
         }
-#pragma unroll
-        for (int l = 0; l < kMaxFusedLat; ++l)
-            if (l < f.n_lat)
-                f.lat[l].activated[(int64_t)(oi + lr) * f.nj + gj] =
-                    (lat_act >> (l * 8 + r)) & 1u;
+        // the flags that changed in this launch (rows of f.pitch nodes)
+        if (((lat_act ^ lat_act0) >> r) & 1u)
+            f.lat[0].activated[(int64_t)(oi + lr) * f.pitch + gj] = (lat_act >> r) & 1u;
     }
     if (nonfinite && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
 }
@@ -971,8 +974,9 @@ inline bool aligned16(const void *p) { return p && ((uintptr_t)p & 15) == 0; }
 
 // True when the TMA form can run this configuration: every array it reads
 // through a tensor map (packed weights, the weights' centre plane, both
-// potential buffers, the myocyte flags and the model's `ns` state arrays)
-// starts on a 16-byte boundary, and rows are a multiple of 16 nodes.
+// potential buffers, the myocyte flags, the model's `ns` state arrays and
+// the local activation tracker's flags) starts on a 16-byte boundary, and
+// rows are a multiple of 16 nodes.
 inline bool tma_usable(const fw_step_args *a, int ns)
 {
     bool ok = aligned16(a->weights_packed) && aligned16(a->weights) &&
@@ -980,6 +984,7 @@ inline bool tma_usable(const fw_step_args *a, int ns)
               a->nj % 16 == 0 && a->ni < (1 << 30) && a->nj < (1 << 30);
     for (int q = 0; q < ns && ok; ++q)
         ok = aligned16(a->state[q]) && aligned16(a->state_b[q]);
+    for (int l = 0; l < a->n_lat && ok; ++l) ok = aligned16(a->lat[l].activated);
     return ok && tensor_map_encoder() != nullptr;
 }
 
@@ -1028,6 +1033,9 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     if (ok)
         ok = encode_2d(&k.maps.wc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, wcen_plane,
                        a->nj, a->ni, kBoxF, LH);
+    if (ok && a->n_lat > 0)
+        ok = encode_2d(&k.maps.act, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1,
+                       a->lat[0].activated, a->nj, a->ni, kBoxB, LH);
     if (!ok) {
         set_error("fw_step (fused TMA): tensor map encoding failed");
         return FW_ERR_UNSUPPORTED;

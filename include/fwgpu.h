@@ -281,10 +281,12 @@ typedef struct fw_step_args {
     int32_t debug_flags; /* 0 in normal use; FW_DEBUG_* bits for tests      */
     int32_t reserved2;
     int64_t pitch;       /* row pitch in nodes of u[0], u[1], the state
-                            arrays, myo, weights and weights_packed (their
-                            N is ni * pitch); 0 = nj.  Stimulus masks and
-                            tracker arrays always have rows of nj nodes.
-                            fw_batch_plan only: fw_step takes 0 or nj     */
+                            arrays, myo, weights, weights_packed and the
+                            local activation trackers' `activated` flags
+                            (their N is ni * pitch); 0 = nj.  Stimulus
+                            masks and the other tracker arrays always have
+                            rows of nj nodes.  fw_batch_plan only: fw_step
+                            takes 0 or nj                                 */
     void *state_b[FW_MAX_FUSED_STATE]; /* FW_FORM_FUSED and batches: second
                             buffers of the state variables (same type and
                             size as state[], equal to them at non-myocytes).

@@ -26,6 +26,10 @@ def gc():
 
 
 def _no_probes(case, keep_at=1):
+    """The case's trackers the batch takes (one activation-time tracker),
+    plus a local activation tracker at u = 0.5 where it has none, so that
+    every tissue also stages and writes back activation flags (with rows
+    padded to the pitch in the TMA form)."""
     c = copy.copy(case)
     out, n_at = [], 0
     for t in case.get("trackers", []):
@@ -36,6 +40,8 @@ def _no_probes(case, keep_at=1):
         elif t["kind"] != "lat":
             continue
         out.append(t)
+    if not any(t["kind"] == "lat" for t in out):
+        out.append(dict(kind="lat", threshold=0.5))
     c["trackers"] = out
     return c
 

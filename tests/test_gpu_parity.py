@@ -224,7 +224,8 @@ def _fused_case(name, aniso, nj):
                 trackers=[dict(kind="at", threshold=0.5),
                           dict(kind="probe", cells=[[3, 3], [75, 70],
                                                     [149, 139], [56, 56]],
-                               vars=cases.MODEL_VARS[name], step=3)])
+                               vars=cases.MODEL_VARS[name], step=3),
+                          dict(kind="lat", threshold=0.5)])
 
 
 @pytest.mark.parametrize("name", ["ap", "ms", "fk"])
@@ -260,7 +261,8 @@ def test_fused_variants_bitwise_equal(gc, name, aniso, k, variant):
     4 x 1 strips or 2 x 2 blocks) forms each node's diffusion sum as the same
     FMA chain over the stored weights and runs the same ionic update, so
     fields, state, activation times and probe traces agree bitwise with the
-    TMA strip kernel (variant 3)."""
+    TMA strip kernel (variant 3).  Local activation flags: read from global
+    memory by variants 1, 2 and 4, staged with the region by variant 3."""
     case = _fused_case(name, aniso, 144)
     r3 = gc.run(case, npfloat="float32", form="fused", fused_k=k,
                 fused_variant=3)
@@ -271,6 +273,9 @@ def test_fused_variants_bitwise_equal(gc, name, aniso, k, variant):
         assert np.array_equal(rv[v], r3[v]), v
         assert np.array_equal(rv["trackers"][1][v], r3["trackers"][1][v]), v
     assert np.array_equal(rv["trackers"][0], r3["trackers"][0])
+    lat3, latv = r3["trackers"][2], rv["trackers"][2]
+    assert lat3.shape == latv.shape and lat3.shape[0] >= 1
+    assert np.array_equal(latv, lat3, equal_nan=True)
 
 
 def test_fused_trackers_cable(gc):
