@@ -501,13 +501,14 @@ int64_t tissue_tiles(const fw_step_args *a)
 // description (a FusedK kept in the plan, whose per-launch fields
 // k_batch_events fills before each launch) and the TMA copies of its region
 // through the tissue's own tensor maps (also in the plan), all completing
-// on the stage's mbarrier.  Thread 0 takes tile indices from the counter two
-// tiles ahead and reads their list entries one tile ahead, so none of its
-// loads is waited for on the way.  Tissues need rows of a multiple of 16
+// on the stage's mbarrier.  Thread 0 claims runs of consecutive tiles from
+// the counter one run ahead and reads each list entry one tile ahead, so
+// none of its loads is waited for on the way.  Tissues need rows of a multiple of 16
 // nodes, which the caller provides as a row pitch (fw_step_args.pitch) on
 // copies of the TMA-read arrays.
 
 constexpr int kTmaR = 4;                           // rows per thread
+constexpr int kRun = 4;                            // tiles per counter claim
 constexpr int kTmaNT = fused::kTW * (LH / kTmaR);  // 512 threads
 
 struct alignas(128) BTissueT {
@@ -651,8 +652,8 @@ __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
 }
 
 // One (model, stencil) group of the batch: tiles [t_begin, t_end) of the
-// list, taken from counters[0] (counters[1] counts the CTAs that are done;
-// the last one zeroes both).
+// list, claimed kRun at a time from counters[0] (counters[1] counts the
+// CTAs that are done; the last one zeroes both).
 template <class M, int ST>
 __global__ void __launch_bounds__(kTmaNT, 1)
     k_batch_tma(const BTissueT *__restrict__ tissues, const BTileT *__restrict__ tiles,
@@ -672,19 +673,34 @@ __global__ void __launch_bounds__(kTmaNT, 1)
     fused::strip_masks<KMAX, LH, kTmaR>(tid % fused::kTW, (tid / fused::kTW) * kTmaR,
                                         own_c, ring_c);
     const BTileT none{-1, -1, 0, 0};
-    // thread 0's look-ahead: tile i + 1 (index and entry) and tile i + 2
-    // (index) while tile i is computed
-    int t_next = t_end, t_after = t_end, acquired = -1;
+    // thread 0's tiles: runs of kRun consecutive list entries (mostly of
+    // one tissue, whose tensor maps are then acquired once per run), each
+    // run's start taken from counters[0] one run ahead; the list entry of
+    // tile i + 1 is read while tile i is computed
+    int run_cur = t_end, run_end = t_end, run_next = t_end, acquired = -1;
+    auto take_run = [&]() -> int {
+        const int64_t s =
+            (int64_t)t_begin + (int64_t)atomicAdd(&counters[0], 1u) * kRun;
+        return s < t_end ? (int)s : t_end;
+    };
+    auto next_tile = [&]() -> int {
+        if (run_cur >= run_end) {
+            if (run_next >= t_end) return t_end;
+            run_cur = run_next;
+            run_end = run_next + kRun < t_end ? run_next + kRun : t_end;
+            run_next = take_run();
+        }
+        return run_cur++;
+    };
+    int t_next = t_end;
     BTileT b_next = none;
     if (tid == 0) {
         fused::mbar_init(&S.t.bar[0], 1);
         fused::mbar_init(&S.t.bar[1], 1);
         fused::mbar_fence_init();
-        const int t0 = t_begin + (int)atomicAdd(&counters[0], 1u);
-        if (t0 < t_end) {
-            t_next = t_begin + (int)atomicAdd(&counters[0], 1u);
-            if (t_next < t_end) t_after = t_begin + (int)atomicAdd(&counters[0], 1u);
-        }
+        run_next = take_run();
+        const int t0 = next_tile();
+        t_next = next_tile();
         batch_issue<M, ST>(tissues, t_end, n_tissues, in_buf, S, 0, t0,
                            t0 < t_end ? tiles[t0] : none, acquired);
         if (t_next < t_end) b_next = tiles[t_next];
@@ -699,10 +715,8 @@ __global__ void __launch_bounds__(kTmaNT, 1)
             // the previous iteration
             batch_issue<M, ST>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1, t_next,
                                b_next, acquired);
-            t_next = t_after;
+            t_next = next_tile();
             b_next = t_next < t_end ? tiles[t_next] : none;
-            t_after = t_next < t_end ? t_begin + (int)atomicAdd(&counters[0], 1u)
-                                     : t_end;
         }
         const unsigned ph = (parity >> sg) & 1u;
         const bool arrived = fused::mbar_wait(&S.t.bar[sg], ph);
