@@ -115,6 +115,9 @@ struct alignas(16) FusedK {
     FLat lat[kMaxFusedLat];
     FProbe probe[FW_MAX_PROBE];
     int32_t *status;
+    // weights formed on chip (fused_variant 5): D_al, D_ac, the scalar
+    // conductivity and D_model * dt / dr**2, rounded to float32
+    float fly_dal, fly_dac, fly_cond, fly_scale;
 };
 
 struct ProbeEntry {

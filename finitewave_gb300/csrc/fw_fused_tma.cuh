@@ -35,6 +35,9 @@ constexpr int kTW = 64;    // region width (nodes)
 constexpr int kBoxF = 72;  // f32 box width: columns oj - 1 .. oj + 64 from a 4-aligned start
 constexpr int kBoxB = 80;  // int8 box width: columns oj .. oj + 63 from a 16-aligned start
 constexpr int kMaxTmaState = 2;
+// f32 box width of the float32 fiber pairs (weights formed on chip): the
+// region's 64 columns, two floats each, from a 16-byte aligned start
+constexpr int kBoxFib = 132;
 
 template <int LH, int NS, int NWO>
 struct TmaStage {
@@ -64,6 +67,7 @@ struct TmaMaps {
     CUtensorMap s[2][kMaxTmaState];  // the state arrays, both buffers
     CUtensorMap wc;     // the centre weight plane, f32 (nj, ni)
     CUtensorMap act;    // the local activation tracker's flags, u8 (nj, ni)
+    CUtensorMap fib;    // float32 fiber pairs, f32 (2 nj, ni) (weights on chip)
 };
 static_assert(kMaxFusedLat == 1, "one tensor map of local activation flags");
 
@@ -189,13 +193,32 @@ __device__ __forceinline__ int floor_to(int x, int m)
 // The barrier has an arrival count of one: this is the stage's only
 // arrive, and it announces the region's bytes plus `extra` bytes of other
 // copies the caller issues on the same barrier.
-template <int KMAX, int NS, int NWO, bool PAIRS = false, class Stage>
+// FLY: instead of the weights, the region's float32 fiber pairs (into the
+// stage's wb area, from which the tile forms its weights on chip).
+template <int KMAX, int NS, int NWO, bool PAIRS = false, bool FLY = false, class Stage>
 __device__ __forceinline__ void issue_region(const TmaMaps &maps, int in_buf,
                                              Stage &G, uint64_t *bar, int oi,
                                              int oj, unsigned extra = 0,
                                              bool lat = false)
 {
     const int x4 = floor_to(oj - 1, 4), x16 = floor_to(oj, 16);
+    if constexpr (FLY) {
+        constexpr int kRows = (int)(sizeof(G.myo) / sizeof(G.myo[0]));
+        constexpr unsigned kFib = (unsigned)(kRows * kBoxFib * sizeof(float));
+        static_assert(NWO == 8 && sizeof(G.wb) >= kFib, "fiber box in the wb area");
+        const unsigned bytes = (unsigned)(sizeof(G.u) + NS * sizeof(G.s[0]) +
+                                          sizeof(G.myo)) +
+                               kFib + (lat ? (unsigned)sizeof(G.act) : 0u);
+        mbar_expect_tx(bar, bytes + extra);
+        if (lat) tma_2d(&G.act[0][0], &maps.act, x16, oi, bar);
+        tma_2d(&G.wb[0][0], &maps.fib, floor_to(2 * oj, 4), oi, bar);
+        tma_2d(&G.u[0][0], &maps.u[in_buf], x4, oi - 1, bar);
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+            tma_2d(&G.s[q][0][0], &maps.s[in_buf][q], x4, oi, bar);
+        tma_2d(&G.myo[0][0], &maps.myo, x16, oi, bar);
+        return;
+    }
     const unsigned bytes = (unsigned)(sizeof(G.wa) * (NWO == 8 ? 2 : 1) +
                                       sizeof(G.u) + NS * sizeof(G.s[0]) +
                                       sizeof(G.myo) + sizeof(G.wc)) +
@@ -217,14 +240,111 @@ __device__ __forceinline__ void issue_region(const TmaMaps &maps, int in_buf,
     tma_2d(&G.wc[0][0], &maps.wc, x4, oi, bar);
 }
 
-template <int KMAX, int LH, int NS, int NWO, bool PAIRS = false>
+template <int KMAX, int LH, int NS, int NWO, bool PAIRS = false, bool FLY = false>
 __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> &G,
                                            uint64_t *bar, int bi, int bj)
 {
     constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
     // the column-pair kernel reads the flags from global memory
-    issue_region<KMAX, NS, NWO, PAIRS>(k.maps, k.in_buf, G, bar, bi * TI - KMAX,
-                                       bj * TJ - KMAX, 0u, !PAIRS && k.f.n_lat > 0);
+    issue_region<KMAX, NS, NWO, PAIRS, FLY>(k.maps, k.in_buf, G, bar,
+                                            bi * TI - KMAX, bj * TJ - KMAX, 0u,
+                                            !PAIRS && k.f.n_lat > 0);
+}
+
+// minor_component (asymmetric_stencil_2d.py:204-259) in float32.
+__device__ __forceinline__ void minor_f32(float d, int m0, int m1, int m2, int m3,
+                                          int m4, int m5, float r[6])
+{
+    const int mh = m2 + m3 + m4 + m5, ml = m0 + m1 + m2 + m3;
+    if (m2 == 0 || m3 == 0 || mh < 3 || ml < 3) {
+        r[0] = r[1] = r[2] = r[3] = r[4] = r[5] = 0.f;
+        return;
+    }
+    const float dh = (float)mh, dl = (float)ml;
+    r[0] = (-d) * (float)m0 / dl;
+    r[1] = (-d) * (float)m1 / dl;
+    r[2] = d * ((float)m2 / dh - (float)m2 / dl);
+    r[3] = d * ((float)m3 / dh - (float)m3 / dl);
+    r[4] = d * (float)m4 / dh;
+    r[5] = d * (float)m5 / dh;
+}
+
+// The region's AsymmetricStencil2D weights formed on chip (fused_variant 5)
+// from the staged float32 fiber pairs (in the stage's wb area) and myocyte
+// flags: the reference's four face fluxes, each a major and a six-point
+// minor component, accumulated in its order (asymmetric_stencil_2d.py:
+// 291-433), the half-step diffusion components 0.5 (D c + D' c) over a node
+// and its +1 neighbour (:104-136), then scaled by D_model dt / dr**2 with 1
+// added to the centre (:46-84) -- all in float32, so within float32
+// rounding of the stored weights (built in float64).  Weights are formed
+// for the myocytes off the region's outer ring (no other node's weights are
+// read) and written where the TMA form stages them: w0..w3 into wa, w5..w8
+// into wb once every thread has read its fibers, the centre into wc.
+template <int LH, int R, class Stage>
+__device__ __forceinline__ void fly_weights(const FusedK &f, Stage &G, int r0,
+                                            int col, int oj, int xo, int xo8)
+{
+    const float *fb = reinterpret_cast<const float *>(&G.wb[0][0]);
+    const int xf = 2 * oj - floor_to(2 * oj, 4);
+    const float dal = f.fly_dal, dac = f.fly_dac, cnd = f.fly_cond;
+    const float sc = f.fly_scale;
+    auto M = [&](int lr, int c) -> int { return G.myo[lr][c + xo8] != 0; };
+    // D_ac (a0 == a1) + (D_al - D_ac) f_a0 f_a1 at region node (lr, c)
+    auto D = [&](int lr, int c, int a0, int a1) -> float {
+        const float *fp = fb + lr * kBoxFib + 2 * c + xf;
+        return (a0 == a1 ? dac : 0.f) + (dal - dac) * fp[a0] * fp[a1];
+    };
+    auto H = [&](int lr, int c, int ax, int comp) -> float {
+        return 0.5f * (D(lr, c, ax, comp) * cnd +
+                       D(lr + (ax == 0), c + (ax == 1), ax, comp) * cnd);
+    };
+    float4 wb_out[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int lr = r0 + r, c = col;
+        float o[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (lr >= 1 && lr <= LH - 2 && c >= 1 && c <= kTW - 2 && M(lr, c)) {
+            float m[6], q;
+            // q (i-1/2, j)
+            q = H(lr - 1, c, 0, 0) * (float)M(lr - 1, c);
+            o[1] += q; o[4] -= q;
+            minor_f32(H(lr - 1, c, 0, 1), M(lr - 1, c - 1), M(lr, c - 1), M(lr - 1, c),
+                      M(lr, c), M(lr - 1, c + 1), M(lr, c + 1), m);
+            o[0] -= m[0]; o[3] -= m[1]; o[1] -= m[2];
+            o[4] -= m[3]; o[2] -= m[4]; o[5] -= m[5];
+            // q (i, j-1/2)
+            q = H(lr, c - 1, 1, 1) * (float)M(lr, c - 1);
+            o[3] += q; o[4] -= q;
+            minor_f32(H(lr, c - 1, 1, 0), M(lr - 1, c - 1), M(lr - 1, c), M(lr, c - 1),
+                      M(lr, c), M(lr + 1, c - 1), M(lr + 1, c), m);
+            o[0] -= m[0]; o[1] -= m[1]; o[3] -= m[2];
+            o[4] -= m[3]; o[6] -= m[4]; o[7] -= m[5];
+            // q (i, j+1/2)
+            q = H(lr, c, 1, 1) * (float)M(lr, c + 1);
+            o[5] += q; o[4] -= q;
+            minor_f32(H(lr, c, 1, 0), M(lr - 1, c + 1), M(lr - 1, c), M(lr, c + 1),
+                      M(lr, c), M(lr + 1, c + 1), M(lr + 1, c), m);
+            o[2] += m[0]; o[1] += m[1]; o[5] += m[2];
+            o[4] += m[3]; o[8] += m[4]; o[7] += m[5];
+            // q (i+1/2, j)
+            q = H(lr, c, 0, 0) * (float)M(lr + 1, c);
+            o[7] += q; o[4] -= q;
+            minor_f32(H(lr, c, 0, 1), M(lr + 1, c - 1), M(lr, c - 1), M(lr + 1, c),
+                      M(lr, c), M(lr + 1, c + 1), M(lr, c + 1), m);
+            o[6] += m[0]; o[3] += m[1]; o[7] += m[2];
+            o[4] += m[3]; o[8] += m[4]; o[5] += m[5];
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) o[k] *= sc;
+        o[4] += 1.f;
+        G.wa[lr][col] = make_float4(o[0], o[1], o[2], o[3]);
+        G.wc[lr][col + xo] = o[4];
+        wb_out[r] = make_float4(o[5], o[6], o[7], o[8]);
+    }
+    __syncthreads();  // the fibers in the wb area have been read
+#pragma unroll
+    for (int r = 0; r < R; ++r) G.wb[r0 + r][col] = wb_out[r];
+    __syncthreads();
 }
 
 // Rows r < R of the strip of thread (col, r0) inside the region's interior
@@ -250,7 +370,8 @@ __device__ __forceinline__ void strip_masks(int col, int r0, uint32_t &own_c,
 // tracker arrays and stimulus masks row length f.nj).  u1 is the ping-pong
 // partner of the stage's potential.  Thread (col, r0) owns the strip of R
 // rows of column col.  Shared by the single-tissue and the batched kernels.
-template <class M, int ST, int KMAX, int LH, int R, class Stage, class Sm>
+template <class M, int ST, int KMAX, int LH, int R, bool FLY = false, class Stage,
+          class Sm>
 __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int oi,
                                          int oj, uint32_t own_c, uint32_t ring_c,
                                          const Params<float, M::NP> &P)
@@ -269,6 +390,7 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
     const int xo8 = oj - floor_to(oj, 16);     // 0..15
     const int gj = oj + col;
     const bool col_in = (unsigned)gj < (unsigned)f.nj;
+    if constexpr (FLY) fly_weights<LH, R>(f, G, r0, col, oj, xo, xo8);
 
     // per-thread flags and state of the strip
     typename M::template St<float> st[R];
@@ -486,7 +608,7 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
     if (nonfinite && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
 }
 
-template <class M, int ST, int KMAX, int LH, int R>
+template <class M, int ST, int KMAX, int LH, int R, bool FLY = false>
 __global__ void __launch_bounds__(kTW *(LH / R), 1)
     k_fused_tma(const __grid_constant__ TmaK k)
 {
@@ -521,7 +643,8 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
     const int tj = f.tiles_j;
     const int di = (int)gridDim.x / tj, dj = (int)gridDim.x % tj;
     int bi = tile / tj, bj = tile % tj;
-    if (tid == 0 && tile < k.tiles) issue_tile<KMAX>(k, S.stage[0], &S.bar[0], bi, bj);
+    if (tid == 0 && tile < k.tiles)
+        issue_tile<KMAX, LH, NS, NWO, false, FLY>(k, S.stage[0], &S.bar[0], bi, bj);
 
     Params<float, M::NP> P;
 #pragma unroll
@@ -541,7 +664,8 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
         const int next = tile + gridDim.x;
         if (tid == 0 && next < k.tiles) {
             fence_proxy_async();
-            issue_tile<KMAX>(k, S.stage[sg ^ 1], &S.bar[sg ^ 1], ni_, nj_);
+            issue_tile<KMAX, LH, NS, NWO, false, FLY>(k, S.stage[sg ^ 1],
+                                                      &S.bar[sg ^ 1], ni_, nj_);
         }
         const unsigned ph = (parity >> sg) & 1u;
         const bool arrived = mbar_wait(&S.bar[sg], ph);
@@ -553,7 +677,7 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
         const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
         bi = ni_;
         bj = nj_;
-        tma_tile<M, ST, KMAX, LH, R>(f, G, S, oi, oj, own_c, ring_c, P);
+        tma_tile<M, ST, KMAX, LH, R, FLY>(f, G, S, oi, oj, own_c, ring_c, P);
         __syncthreads();
     }
 }
@@ -988,8 +1112,22 @@ inline bool tma_usable(const fw_step_args *a, int ns)
     return ok && tensor_map_encoder() != nullptr;
 }
 
+// The same for the weights formed on chip (fused_variant 5): the float32
+// fiber pairs take the place of the weights.
+inline bool tma_fly_usable(const fw_step_args *a, int ns)
+{
+    bool ok = aligned16(a->fibers_f32) && aligned16(a->u[0]) &&
+              aligned16(a->u[1]) && aligned16(a->myo) && a->nj % 16 == 0 &&
+              a->ni < (1 << 30) && a->nj < (1 << 29);
+    for (int q = 0; q < ns && ok; ++q)
+        ok = aligned16(a->state[q]) && aligned16(a->state_b[q]);
+    for (int l = 0; l < a->n_lat && ok; ++l) ok = aligned16(a->lat[l].activated);
+    return ok && tensor_map_encoder() != nullptr;
+}
+
 // PAIRS: the column-pair kernel k_fused_tma2 (R is then 2, fixed by it).
-template <class M, int ST, int KMAX, int LH, int R, bool PAIRS = false>
+// FLY: the weights formed on chip from the float32 fibers (fused_variant 5).
+template <class M, int ST, int KMAX, int LH, int R, bool PAIRS = false, bool FLY = false>
 int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                      cudaStream_t stream)
 {
@@ -997,11 +1135,12 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     constexpr int NT = PAIRS ? (kTW / 2) * (LH / 2) : kTW * (LH / R);
     constexpr int NWO = Stencil2D<ST>::NWO;
     constexpr size_t SMEM = sizeof(TmaSmem<LH, M::NS, NWO>) + 1024;
+    static_assert(!(PAIRS && FLY), "weights on chip: strip kernel only");
     void (*kern)(const TmaK);
     if constexpr (PAIRS)
         kern = k_fused_tma2<M, ST, KMAX, LH>;
     else
-        kern = k_fused_tma<M, ST, KMAX, LH, R>;
+        kern = k_fused_tma<M, ST, KMAX, LH, R, FLY>;
     FW_CUDA_CHECK(cudaFuncSetAttribute(
         kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM));
     if (a->n_lat > kMaxFusedLat) {
@@ -1012,10 +1151,12 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     TmaK k;  // kernel argument, copied at each launch
     memset(&k, 0, sizeof k);
     k.force_timeout = (a->debug_flags & FW_DEBUG_FORCE_TIMEOUT) ? 1 : 0;
-    bool ok = (PAIRS ? encode_weights_pairs(&k.maps.w, a->weights_packed, NWO, a->nj,
-                                            a->ni, LH)
-                     : encode_weights(&k.maps.w, a->weights_packed, NWO, a->nj, a->ni,
-                                      LH)) &&
+    bool ok = (FLY ? encode_2d(&k.maps.fib, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                               a->fibers_f32, 2 * a->nj, a->ni, kBoxFib, LH)
+                   : PAIRS ? encode_weights_pairs(&k.maps.w, a->weights_packed, NWO,
+                                                  a->nj, a->ni, LH)
+                           : encode_weights(&k.maps.w, a->weights_packed, NWO, a->nj,
+                                            a->ni, LH)) &&
               encode_2d(&k.maps.myo, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a->myo,
                         a->nj, a->ni, kBoxB, LH) &&
               encode_2d(&k.maps.u[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->u[0],
@@ -1028,11 +1169,12 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
              encode_2d(&k.maps.s[1][q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
                        a->state_b[q], a->nj, a->ni, kBoxF, LH);
     // the centre plane of the (nw, ni * nj) float32 weights
-    const float *wcen_plane = (const float *)a->weights +
-                              (int64_t)Stencil2D<ST>::CENTRE * a->ni * a->nj;
-    if (ok)
+    if (ok && !FLY) {
+        const float *wcen_plane = (const float *)a->weights +
+                                  (int64_t)Stencil2D<ST>::CENTRE * a->ni * a->nj;
         ok = encode_2d(&k.maps.wc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, wcen_plane,
                        a->nj, a->ni, kBoxF, LH);
+    }
     if (ok && a->n_lat > 0)
         ok = encode_2d(&k.maps.act, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1,
                        a->lat[0].activated, a->nj, a->ni, kBoxB, LH);
@@ -1051,6 +1193,10 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     f.n = a->ni * a->nj;
     f.pitch = (int32_t)a->nj;
     f.status = a->status;
+    f.fly_dal = (float)a->fly_D_al;
+    f.fly_dac = (float)a->fly_D_ac;
+    f.fly_cond = (float)a->fly_cond;
+    f.fly_scale = (float)a->fly_scale;
     const int tiles_i = (int)((a->ni + TI - 1) / TI);
     f.tiles_j = (int)((a->nj + TJ - 1) / TJ);
     k.tiles = tiles_i * f.tiles_j;
@@ -1093,8 +1239,10 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 //   2: cp.async staging, 64 x 64 regions, 512 threads, one CTA per SM;
 //   3: TMA pipeline: persistent CTAs, 64 x 32 regions, 512 threads with
 //      4-node strips, two stages in shared memory;
-//   4: the TMA pipeline with 2 x 2 node blocks per thread (even K only).
-// KMAX (fused_k) in {2, 4, 8} time steps per launch.
+//   4: the TMA pipeline with 2 x 2 node blocks per thread (even K only);
+//   5: variant 3 with the AsymmetricStencil2D weights formed on chip from
+//      float32 fibers (fw_step_args.fibers_f32) instead of read from HBM.
+// KMAX (fused_k) in {2, 4, 8} time steps per launch (3 also for 3 and 5).
 template <class M, int ST>
 int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                    cudaStream_t stream)
@@ -1110,6 +1258,27 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
             return FW_ERR_ARG;
         }
     if (v == 0) v = tma_usable(a, M::NS) ? 3 : 1;
+    if (v == 5) {
+        if constexpr (ST == FW_STENCIL_ANISO9) {
+            if (!tma_fly_usable(a, M::NS)) {
+                set_error("fw_step (fused variant 5): needs fibers_f32 and "
+                          "16-byte aligned potential, state and myocyte "
+                          "arrays with nj %% 16 == 0");
+                return FW_ERR_UNSUPPORTED;
+            }
+#define FW_FLY_CASE(KK)                                                        \
+    return launch_fused_tma<M, ST, KK, 32, 4, false, true>(a, n_begin, n_steps, stream)
+            if (k == 2) FW_FLY_CASE(2);
+            if (k == 3) FW_FLY_CASE(3);
+            if (k == 4) FW_FLY_CASE(4);
+            if (k == 8) FW_FLY_CASE(8);
+#undef FW_FLY_CASE
+        } else {
+            set_error("fw_step (fused variant 5): the weights are formed on "
+                      "chip for AsymmetricStencil2D only");
+            return FW_ERR_UNSUPPORTED;
+        }
+    }
     if ((v == 3 || v == 4) && !tma_usable(a, M::NS)) {
         set_error("fw_step (fused): the TMA kernels need packed weights, "
                   "16-byte aligned weights, potential, state and myocyte "
@@ -1144,7 +1313,8 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 #undef FW_TMA_CASE
 #undef FW_TMA2_CASE
     set_error("fw_step (fused): no kernel for fused_k=%d fused_variant=%d "
-              "(k in 2, 3, 4, 8; variant in 0..4, variant 4 with even k)", k, a->fused_variant);
+              "(k in 2, 3, 4, 8; variant in 0..5, variant 4 with even k, "
+              "variant 5 for AsymmetricStencil2D)", k, a->fused_variant);
     return FW_ERR_UNSUPPORTED;
 }
 

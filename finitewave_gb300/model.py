@@ -608,6 +608,8 @@ class CardiacModel:
         a.fused_k = int(self.fused_k)
         a.fused_variant = int(self.fused_variant)
         a.debug_flags = int(getattr(self, "_debug_flags", 0))
+        if a.fused_variant == 5 and a.form == _ffi.FORM_FUSED:
+            self._fly_args(a)
         if (a.form == _ffi.FORM_FUSED and not a.fused_k and
                 not a.fused_variant and self.autotune):
             from . import autotune
@@ -615,6 +617,29 @@ class CardiacModel:
         self._fused_choice = (a.fused_variant, a.fused_k) \
             if a.form == _ffi.FORM_FUSED else None
         return a
+
+    def _fly_args(self, a):
+        """fused_variant 5 forms the AsymmetricStencil2D weights on chip:
+        the tissue's fibers as float32 pairs (made once) and the stencil's
+        constants."""
+        fly = getattr(self, "_fly", None)
+        tissue = self.cardiac_tissue
+        if fly is None or fly[0] is not tissue.fibers:
+            if (self.stencil.kind != _ffi.ANISO9 or tissue.fibers is None or
+                    np.ndim(tissue.conductivity) != 0):
+                raise ValueError("fused_variant 5 needs an AsymmetricStencil2D "
+                                 "tissue with fibers and a scalar "
+                                 "conductivity")
+            fib = torch.as_tensor(np.ascontiguousarray(
+                np.asarray(tissue.fibers, dtype=np.float32)),
+                device=self._device())
+            fly = (tissue.fibers, fib)
+            self._fly = fly
+        a.fibers_f32 = fly[1].data_ptr()
+        a.fly_D_al = float(self.stencil.D_al)
+        a.fly_D_ac = float(self.stencil.D_ac)
+        a.fly_cond = float(tissue.conductivity)
+        a.fly_scale = float(self.D_model) * float(self.dt) / float(self.dr) ** 2
 
     def _prepare_segment(self, limit, skip_stims=False):
         """The fw_step_args of the next segment of at most `limit` steps

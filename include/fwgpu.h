@@ -266,8 +266,11 @@ typedef struct fw_step_args {
                               64x64 regions; 3 = TMA pipeline (persistent
                               CTAs, double-buffered 64x32 regions, 4 x 1
                               nodes per thread); 4 = the TMA pipeline with
-                              2 x 2 nodes per thread (even fused_k).  All
-                              variants give bitwise the same results        */
+                              2 x 2 nodes per thread (even fused_k).
+                              Variants 1-4 give bitwise the same results;
+                              5 = variant 3 with the AsymmetricStencil2D
+                              weights formed on chip from fibers_f32
+                              (within float32 rounding of the others)      */
     const void *weights_packed; /* FW_FORM_FUSED: off-centre float32 weights
                                    node-major, (N, 4) for ISO5 or (N, 8)
                                    for ANISO9, from fw_pack_weights; NULL
@@ -297,6 +300,17 @@ typedef struct fw_step_args {
                             roles with u[0] / u[1]: on return the current
                             state is in state[] after an even number of
                             steps and in state_b[] after an odd one      */
+    const float *fibers_f32; /* fused_variant 5 only: the fibers of a 2D
+                            AsymmetricStencil2D tissue as float32 (N, 2),
+                            rows of nj nodes, 16-byte aligned.  The kernel
+                            forms each region's nine weights on chip from
+                            them and the myocyte flags (float32 flux sums)
+                            instead of reading weights_packed and the
+                            centre plane; NULL otherwise                  */
+    double fly_D_al, fly_D_ac; /* fused_variant 5: the stencil's D_al, D_ac */
+    double fly_cond;         /* fused_variant 5: the tissue's scalar
+                                conductivity                              */
+    double fly_scale;        /* fused_variant 5: D_model * dt / dr**2      */
 } fw_step_args;
 
 /* A planned batch of tissues (fw_batch_plan).  Host-side handle; the

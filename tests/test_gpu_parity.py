@@ -278,6 +278,32 @@ def test_fused_variants_bitwise_equal(gc, name, aniso, k, variant):
     assert np.array_equal(latv, lat3, equal_nan=True)
 
 
+@pytest.mark.parametrize("name", ["ap", "ms", "fk"])
+@pytest.mark.parametrize("k", [2, 3, 4, 8])
+def test_fused_weights_on_chip(gc, name, k):
+    """Variant 5 forms each region's AsymmetricStencil2D weights on chip in
+    float32 from the fibers and myocyte flags (the stored weights are built
+    in float64 and rounded): against the plain FP32 form with the fused
+    tolerance -- activation steps within one step on >= 99.9 % of the
+    nodes, fields and probe traces within 2e-3 -- and against variant 3 (the
+    same kernel reading the stored weights) within the same bounds."""
+    case = _fused_case(name, True, 144)
+    ref = gc.run(case, npfloat="float32", form="plain")
+    r3 = gc.run(case, npfloat="float32", form="fused", fused_k=k,
+                fused_variant=3)
+    r5 = gc.run(case, npfloat="float32", form="fused", fused_k=k,
+                fused_variant=5)
+    assert int(r5["model"]._status.item()) == 0
+    assert r5["step"] == ref["step"] == 777
+    for other in (ref, r3):
+        assert _at_agree(r5["trackers"][0], other["trackers"][0], 0.01) >= 0.999
+        for v in cases.MODEL_VARS[name]:
+            np.testing.assert_allclose(r5[v], other[v], rtol=0, atol=2e-3)
+            np.testing.assert_allclose(r5["trackers"][1][v],
+                                       other["trackers"][1][v],
+                                       rtol=0, atol=2e-3)
+
+
 def test_fused_trackers_cable(gc):
     """LAT layers and the windowed AT tracker in the fused form (which takes
     up to two activation trackers and one LAT tracker; more fall back to the
