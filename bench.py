@@ -328,6 +328,13 @@ def run_tp06_slab(args, fg, torch, reps):
         m = tp06_slab(fg, prec, shape)
         m.initialize()
         myo = int(m._myo_d.sum().item())
+        if prec == "float32":
+            st_name = {fg._ffi.ANISO19_XY: "ANISO19_XY",
+                       fg._ffi.ANISO19: "ANISO19"}.get(m._step_stencil, "?")
+            rows = getattr(m, "_wrows", None)
+            w_form = (f"{rows.shape[0]} shared weight rows + a 4-byte row "
+                      "index per node" if rows is not None
+                      else "weight planes")
         for _ in range(2):
             m._run_segment(chunk, sync=False)
         reps.barrier()
@@ -351,11 +358,12 @@ def run_tp06_slab(args, fg, torch, reps):
             "dtype": "f32 (ion concentrations as compensated f32 pairs)",
             "fp64_plain": {"value": out["float64"]["value"], "unit": UNIT},
             "speedup_fp32_over_fp64": v32 / out["float64"]["value"],
-            "roofline": {"bound": "fp32+sfu (compute); HBM fraction shown",
+            "weights": w_form,
+            "roofline": {"bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "alg_bytes_per_myocyte_step": B_ALG_TP06,
-                         "kernel": "k_step<ModelTP06, ANISO19, float>"}}
+                         "kernel": f"k_step<ModelTP06, {st_name}, float>"}}
 
 
 # serving trace: Poisson arrivals of TP06 / Courtemanche requests

@@ -116,7 +116,8 @@ class StepArgs(ctypes.Structure):
                 ("debug_flags", _i32), ("reserved2", _i32),
                 ("pitch", _i64), ("state_b", _vp * MAX_FUSED_STATE),
                 ("fibers_f32", _vp), ("fly_D_al", _f64), ("fly_D_ac", _f64),
-                ("fly_cond", _f64), ("fly_scale", _f64)]
+                ("fly_cond", _f64), ("fly_scale", _f64),
+                ("weight_rows", _vp), ("weight_row_index", _vp)]
 
 
 class Batch(ctypes.Structure):

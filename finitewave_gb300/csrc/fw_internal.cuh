@@ -120,6 +120,40 @@ __device__ __forceinline__ T diffuse_node(const T *__restrict__ u,
     }
 }
 
+// The in-plane 3D sum of diffuse_node<FW_STENCIL_ANISO19_XY> with the
+// node's weights taken from a row of 12 values (planes 0-8, 11, 12 and a
+// pad) of a table of distinct rows: the same products in the same order.
+template <class T>
+__device__ __forceinline__ T diffuse_row_xy(const T *__restrict__ u,
+                                            const T *__restrict__ row, int64_t p,
+                                            int64_t si, int64_t sj)
+{
+    T w[12];
+    if constexpr (sizeof(T) == 4) {
+        const float4 *r = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float4 v = __ldg(r + q);
+            w[4 * q] = v.x;
+            w[4 * q + 1] = v.y;
+            w[4 * q + 2] = v.z;
+            w[4 * q + 3] = v.w;
+        }
+    } else {
+        const double2 *r = reinterpret_cast<const double2 *>(row);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const double2 v = __ldg(r + q);
+            w[2 * q] = v.x;
+            w[2 * q + 1] = v.y;
+        }
+    }
+    return u[p - si - sj] * w[0] + u[p - si] * w[1] + u[p - si + sj] * w[2] +
+           u[p - sj] * w[3] + u[p] * w[4] + u[p + sj] * w[5] +
+           u[p + si - sj] * w[6] + u[p + si] * w[7] + u[p + si + sj] * w[8] +
+           u[p - 1] * w[9] + u[p + 1] * w[10];
+}
+
 // Launch helpers ------------------------------------------------------------
 
 inline int grid_for(int64_t n, int threads, int max_blocks = 152 * 16)

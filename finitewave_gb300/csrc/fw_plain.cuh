@@ -84,6 +84,10 @@ template <class T>
 struct StepK {
     const int8_t *myo;
     const T *w;
+    // FW_STENCIL_ANISO19_XY: the weights as distinct rows of 12 values
+    // (planes 0-8, 11, 12, padding) and each node's row, or NULL
+    const T *wrow;
+    const int32_t *widx;
     const T *u;
     T *un;
     void *state[FW_MAX_STATE];
@@ -146,7 +150,16 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<M, T>::value))
         T uc = k.u[p];
         if (k.n_at | k.n_lat) track(k, p, uc);
         if (!k.myo[p]) continue;
-        T un = diffuse_node<ST, T>(k.u, k.w, p, k.n, k.si, k.sj);
+        T un;
+        if constexpr (ST == FW_STENCIL_ANISO19_XY) {
+            if (k.wrow)
+                un = diffuse_row_xy<T>(k.u, k.wrow + (int64_t)k.widx[p] * 12, p,
+                                       k.si, k.sj);
+            else
+                un = diffuse_node<ST, T>(k.u, k.w, p, k.n, k.si, k.sj);
+        } else {
+            un = diffuse_node<ST, T>(k.u, k.w, p, k.n, k.si, k.sj);
+        }
         auto st = M::template load<T>(k.state, p);
         un = M::template update<T>(uc, un, st, P, dt);
         M::template store<T>(k.state, p, st);
@@ -479,6 +492,14 @@ int run_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     StepK<T> k;
     k.myo = a->myo;
     k.w = (const T *)a->weights;
+    k.wrow = (const T *)a->weight_rows;
+    k.widx = a->weight_row_index;
+    if (k.wrow && (ST != FW_STENCIL_ANISO19_XY || !k.widx ||
+                   ((uintptr_t)k.wrow & 15) != 0)) {
+        set_error("fw_step: weight_rows needs FW_STENCIL_ANISO19_XY, a row "
+                  "index and 16-byte aligned rows");
+        return FW_ERR_ARG;
+    }
     for (int i = 0; i < FW_MAX_STATE; ++i) k.state[i] = a->state[i];
     for (int i = 0; i < FW_MAX_PARAMS; ++i) k.params[i] = (T)a->params[i];
     k.dt = (T)a->dt;

@@ -315,6 +315,35 @@ class CardiacModel:
             # with i +- 1 or j +- 1 are zero, and the step skips them
             self._step_stencil = _ffi.ANISO19_XY
         self._pack_weights()
+        self._weight_rows()
+
+    def _weight_rows(self, force=False):
+        """FW_STENCIL_ANISO19_XY steps read the eleven weight planes 0-8,
+        11 and 12.  When the grid's nodes share few distinct rows of them
+        (one per fiber layer and myocyte neighbourhood in a slab with
+        layered fibers), keep the distinct rows (padded to 12 values) and
+        each node's row instead: the step then reads a 4-byte row index per
+        node from HBM and the rows from L2, with the same sums.  Kept when
+        the rows take at most a quarter of the planes' bytes and 32 MB
+        (`force`: whenever the form applies, for tests)."""
+        self._wrows = self._widx = None
+        self._wrows_src = self.weights
+        if getattr(self, "_step_stencil", None) != _ffi.ANISO19_XY:
+            return
+        w = self.weights
+        n = w[0].numel()
+        planes = w[[0, 1, 2, 3, 4, 5, 6, 7, 8, 11, 12]].reshape(11, n)
+        ibits = torch.int32 if w.dtype == torch.float32 else torch.int64
+        bits = planes.t().contiguous().view(ibits)
+        uniq, inv = torch.unique(bits, dim=0, return_inverse=True)
+        row_bytes = uniq.shape[0] * 12 * w.element_size()
+        if not force and (row_bytes * 4 > n * 11 * w.element_size() or
+                          row_bytes > 32 << 20):
+            return   # little sharing: the planes themselves
+        rows = torch.zeros((uniq.shape[0], 12), dtype=w.dtype, device=w.device)
+        rows[:, :11] = uniq.view(w.dtype)
+        self._wrows = rows
+        self._widx = inv.to(torch.int32).contiguous()
 
     def _pack_weights(self):
         """Node-major copy of the off-centre weights for the TMA form of the
@@ -592,6 +621,12 @@ class CardiacModel:
         a.mesh = self._mesh_d.data_ptr()
         a.myo = self._myo_d.data_ptr()
         a.weights = self.weights.data_ptr()
+        if getattr(self, "_wrows", None) is not None:
+            if self.weights is not self._wrows_src:
+                self._weight_rows()   # the weights were replaced
+            if self._wrows is not None and a.stencil == _ffi.ANISO19_XY:
+                a.weight_rows = self._wrows.data_ptr()
+                a.weight_row_index = self._widx.data_ptr()
         wpack = getattr(self, "_wpack", None)
         a.weights_packed = wpack.data_ptr() if wpack is not None else None
         a.u[0] = self._dev["u"].data_ptr()

@@ -311,6 +311,14 @@ typedef struct fw_step_args {
     double fly_cond;         /* fused_variant 5: the tissue's scalar
                                 conductivity                              */
     double fly_scale;        /* fused_variant 5: D_model * dt / dr**2      */
+    const void *weight_rows; /* FW_STENCIL_ANISO19_XY, plain form: the
+                            distinct rows of the eleven weight planes it
+                            reads (0-8, 11, 12), in the precision's type,
+                            padded to 12 values per row (16-byte aligned),
+                            with weight_row_index giving each node's row;
+                            the step reads these instead of `weights`
+                            (same values, same sums).  NULL otherwise      */
+    const int32_t *weight_row_index; /* (N) row of each node, or NULL    */
 } fw_step_args;
 
 /* A planned batch of tissues (fw_batch_plan).  Host-side handle; the

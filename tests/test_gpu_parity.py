@@ -369,7 +369,9 @@ def test_in_plane_fibers_skip_zero_planes(gc, model, npfloat):
     """Fibers with no z component leave the eight 19-point weight planes
     that couple k +- 1 with i +- 1 or j +- 1 at zero; the model then steps
     with the 11-plane form (FW_STENCIL_ANISO19_XY), whose sums equal the
-    full stencil's bit for bit (the skipped terms are exact zeros)."""
+    full stencil's bit for bit (the skipped terms are exact zeros) -- read
+    from the weight planes or from the table of distinct weight rows with a
+    row index per node (weight_rows), which hold the same values."""
     from finitewave_gb300 import _ffi
     case, _ = cases.ap3d(True)
     fib = np.array(case["fibers"], dtype=np.float64)
@@ -384,15 +386,26 @@ def test_in_plane_fibers_skip_zero_planes(gc, model, npfloat):
                               box=[(0, 12), (0, 11), (1, 3)])]
         case["trackers"] = [dict(kind="at", threshold=-20.0)]
     outs = []
-    for force_full in (False, True):
+    for form in ("rows", "planes", "full"):
         m, objs = gc.build(case, npfloat=npfloat)
         m.initialize()
         assert m._step_stencil == _ffi.ANISO19_XY
-        m._step_stencil = _ffi.ANISO19 if force_full else _ffi.ANISO19_XY
+        if form == "rows":
+            m._weight_rows(force=True)
+            assert m._wrows is not None
+            assert m._wrows.shape[0] < m._widx.numel()
+            # every node's row holds its eleven weights
+            w = m.weights.reshape(m.weights.shape[0], -1)
+            planes = w[[0, 1, 2, 3, 4, 5, 6, 7, 8, 11, 12]].t()
+            assert torch.equal(m._wrows[m._widx.long(), :11], planes)
+        else:
+            m._wrows = None
+        m._step_stencil = _ffi.ANISO19 if form == "full" else _ffi.ANISO19_XY
         m.run(initialize=False)
         outs.append((m.u, objs[0].output, getattr(m, m._state_names[-1])))
-    for a, b in zip(outs[0], outs[1]):
-        assert np.array_equal(a, b)
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
     assert np.any(outs[0][0] != outs[0][0].flat[0])
 
 
