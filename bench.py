@@ -247,8 +247,9 @@ def run_batched(args, fg, torch, reps):
             "myocytes": sum(myo), "time_steps_per_bench_step": chunk,
             "bench_steps": k_b, "launches": int(launches),
             "ms_per_step": 1e3 * el / k_b,
-            "kernel": {"name": ("k_batch_tma" if batch_kernel == 2
-                                else "k_batch"),
+            "kernel": {"name": {1: "k_batch", 2: "k_batch_tma",
+                                3: "k_batch_tma (column pairs, f32x2)"}
+                               [batch_kernel],
                        "value": kernel_value,
                        "ms_per_time_step": kms / chunk,
                        "launches_per_bench_step": int(kl)},
@@ -1130,7 +1131,7 @@ def main():
                     help="skip the batched many-tissue measurement")
     ap.add_argument("--batched-tissues", type=int, default=N_TISSUES)
     ap.add_argument("--batch-kernel", default="tma",
-                    choices=["tma", "cp.async"])
+                    choices=["tma", "pairs", "cp.async"])
     ap.add_argument("--no-tp06", action="store_true",
                     help="skip the TP06 slab measurement")
     ap.add_argument("--no-accuracy", action="store_true",

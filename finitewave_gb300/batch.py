@@ -139,12 +139,14 @@ class TissueBatch:
     the TMA pipeline over row-padded copies of the tissues' arrays (made
     once per model and kept by the batch, about 90 bytes per node), state
     copied in at the start of run() and out at its end and around host-side
-    commands and state savers; "cp.async" runs the kernel that stages with
-    4-byte asynchronous copies straight from the models' arrays."""
+    commands and state savers; "pairs" runs the same pipeline with 2 x 2
+    nodes per thread advanced in two-wide float32 instructions (the same
+    bits as "tma"); "cp.async" runs the kernel that stages with 4-byte
+    asynchronous copies straight from the models' arrays."""
 
     def __init__(self, models=(), chunk=None, graphs=True, kernel="tma"):
-        if kernel not in ("tma", "cp.async"):
-            raise ValueError("kernel must be 'tma' or 'cp.async'")
+        if kernel not in ("tma", "pairs", "cp.async"):
+            raise ValueError("kernel must be 'tma', 'pairs' or 'cp.async'")
         self.models = list(models)
         self.chunk = chunk
         self.graphs = graphs
@@ -256,7 +258,7 @@ class TissueBatch:
         remaining = [int(np.ceil((m.t_max - m.t) / m.dt)) for m in ms]
         active = [i for i in range(len(ms)) if remaining[i] > 0]
         stream = torch.cuda.current_stream(dev).cuda_stream
-        tma = self.kernel == "tma"
+        tma = self.kernel in ("tma", "pairs")
         mirrors = [self._mirror(m) for m in ms] if tma else None
         if tma:
             for mir in mirrors:
@@ -270,6 +272,8 @@ class TissueBatch:
             for i, seg in zip(active, segs):
                 if tma:
                     mirrors[i].apply(seg.args)
+                    if self.kernel == "pairs":
+                        seg.args.fused_variant = 6
                 else:
                     seg.args.fused_variant = 1
             k = len(segs)

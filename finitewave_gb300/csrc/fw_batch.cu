@@ -302,7 +302,7 @@ __device__ __forceinline__ void run_tile(const BStim *stims, int tile,
             const float un = fused::stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r],
                                                     wr[r], wl[r + 1], wr[r + 1],
                                                     wl[r + 2], wc[r + 2], wr[r + 2]);
-            const float uu = M::template update<float>(b1, un, st[r], P, dt);
+            const float uu = fused::fused_update<M>(b1, un, st[r], P, dt);
             nxt[lr + 1][col + 1] = ((upd >> r) & 1u) ? uu : b1;
         }
         __syncthreads();
@@ -536,6 +536,7 @@ template <int NS, int NWO>
 struct BatchTmaSmem {
     fused::TmaSmem<LH, NS, NWO> t;
     fused::FusedK f[2];    // launch description of each stage's tile
+    int ftissue[2];        // the tissue whose description f[] holds (-1: none)
     int tile[2];           // the stage's tile index (>= the group's end: none)
     int oi[2], oj[2];      // its region origin
     int ok[2];             // 0 for a skipped tile
@@ -606,7 +607,8 @@ __device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned b
 
 // Thread 0: stage tile t (list entry bt) into stage sg.  The tensor maps
 // of a tissue are acquired once for a run of tiles of the same tissue.
-template <class M, int ST, class Sm>
+// PAIR: the column-pair kernel, whose weight map is the column-pair view.
+template <class M, int ST, bool PAIR, class Sm>
 __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
                                          int32_t t_end, int32_t n_tissues,
                                          int32_t in_buf, Sm &S, int sg, int t,
@@ -644,17 +646,26 @@ __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
         acquired = bt.tissue;
     }
     // one arrive on the stage's barrier announces the region's bytes and
-    // the launch description's, which rides on the same barrier
+    // the launch description's, which rides on the same barrier; a stage
+    // whose last tile was of the same tissue holds it already (tiles come
+    // in runs of one tissue, and a description does not change within a
+    // launch)
     constexpr unsigned kF = (unsigned)sizeof(fused::FusedK);
-    fused::issue_region<KMAX, M::NS, NWO>(Mp, in_buf, S.t.stage[sg], bar, bt.oi,
-                                          bt.oj, kF, lat);
-    bulk_copy(&S.f[sg], &T.f, kF, bar);
+    const bool fresh = S.ftissue[sg] != bt.tissue;
+    fused::issue_region<KMAX, M::NS, NWO, PAIR>(Mp, in_buf, S.t.stage[sg], bar,
+                                                bt.oi, bt.oj, fresh ? kF : 0u, lat);
+    if (fresh) {
+        bulk_copy(&S.f[sg], &T.f, kF, bar);
+        S.ftissue[sg] = bt.tissue;
+    }
 }
 
 // One (model, stencil) group of the batch: tiles [t_begin, t_end) of the
 // list, claimed kRun at a time from counters[0] (counters[1] counts the
-// CTAs that are done; the last one zeroes both).
-template <class M, int ST>
+// CTAs that are done; the last one zeroes both).  PAIR (kernel 3): the tile
+// code of the column-pair kernels in two-wide float32 instructions
+// (tma_tile2), 2 x 2 nodes per thread, the same bits as the strip tiles.
+template <class M, int ST, bool PAIR>
 __global__ void __launch_bounds__(kTmaNT, 1)
     k_batch_tma(const BTissueT *__restrict__ tissues, const BTileT *__restrict__ tiles,
                 int32_t t_begin, int32_t t_end, int32_t n_tissues, int32_t in_buf,
@@ -670,8 +681,12 @@ __global__ void __launch_bounds__(kTmaNT, 1)
     // not this group's, so nothing it reads is written here)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     uint32_t own_c, ring_c;
-    fused::strip_masks<KMAX, LH, kTmaR>(tid % fused::kTW, (tid / fused::kTW) * kTmaR,
-                                        own_c, ring_c);
+    if constexpr (PAIR)
+        fused::pair_masks<KMAX, LH>(2 * (tid % (fused::kTW / 2)),
+                                    (tid / (fused::kTW / 2)) * 2, own_c, ring_c);
+    else
+        fused::strip_masks<KMAX, LH, kTmaR>(tid % fused::kTW,
+                                            (tid / fused::kTW) * kTmaR, own_c, ring_c);
     const BTileT none{-1, -1, 0, 0};
     // thread 0's tiles: runs of kRun consecutive list entries (mostly of
     // one tissue, whose tensor maps are then acquired once per run), each
@@ -698,10 +713,11 @@ __global__ void __launch_bounds__(kTmaNT, 1)
         fused::mbar_init(&S.t.bar[0], 1);
         fused::mbar_init(&S.t.bar[1], 1);
         fused::mbar_fence_init();
+        S.ftissue[0] = S.ftissue[1] = -1;
         run_next = take_run();
         const int t0 = next_tile();
         t_next = next_tile();
-        batch_issue<M, ST>(tissues, t_end, n_tissues, in_buf, S, 0, t0,
+        batch_issue<M, ST, PAIR>(tissues, t_end, n_tissues, in_buf, S, 0, t0,
                            t0 < t_end ? tiles[t0] : none, acquired);
         if (t_next < t_end) b_next = tiles[t_next];
     }
@@ -713,7 +729,8 @@ __global__ void __launch_bounds__(kTmaNT, 1)
         if (tid == 0) {
             // the other stage's readers finished at the barrier that closed
             // the previous iteration
-            batch_issue<M, ST>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1, t_next,
+            batch_issue<M, ST, PAIR>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1,
+                                     t_next,
                                b_next, acquired);
             t_next = next_tile();
             b_next = t_next < t_end ? tiles[t_next] : none;
@@ -736,8 +753,13 @@ __global__ void __launch_bounds__(kTmaNT, 1)
             Params<float, M::NP> P;
 #pragma unroll
             for (int i = 0; i < M::NP; ++i) P.v[i] = f.params[i];
-            fused::tma_tile<M, ST, KMAX, LH, kTmaR>(f, S.t.stage[sg], S.t, S.oi[sg],
-                                                   S.oj[sg], own_c, ring_c, P);
+            if constexpr (PAIR)
+                fused::tma_tile2<M, ST, KMAX, LH, true>(f, S.t.stage[sg], S.t, S.oi[sg],
+                                                        S.oj[sg], own_c, ring_c, P);
+            else
+                fused::tma_tile<M, ST, KMAX, LH, kTmaR>(f, S.t.stage[sg], S.t,
+                                                       S.oi[sg], S.oj[sg], own_c,
+                                                       ring_c, P);
         }
         __syncthreads();
     }
@@ -762,11 +784,32 @@ constexpr size_t tma_smem()
 static_assert(tma_smem<ModelFK, FW_STENCIL_ANISO9>() <= 232448,
               "the batched TMA stages exceed 227 KB");
 
+using BatchTmaKernel = void (*)(const BTissueT *, const BTileT *, int32_t, int32_t,
+                                int32_t, int32_t, uint32_t *);
+
+inline int batch_group_launch_k(BatchTmaKernel kern, size_t smem, bool attr_only,
+                                cudaLaunchConfig_t &cfg, const BTissueT *desc,
+                                const BTileT *tl, int32_t t_begin, int32_t t_end,
+                                int32_t n_tissues, int32_t in_buf, uint32_t *counters)
+{
+    if (attr_only) {
+        FW_CUDA_CHECK(cudaFuncSetAttribute(
+            kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return FW_OK;
+    }
+    cfg.dynamicSmemBytes = smem;
+    FW_CUDA_CHECK(cudaLaunchKernelEx(&cfg, kern, desc, tl, t_begin, t_end, n_tissues,
+                                     in_buf, counters));
+    FW_CHECK_LAUNCH("k_batch_tma");
+    return FW_OK;
+}
+
 // Launch group g's kernel (or set its shared-memory attribute when
-// `attr_only`).  `overlap`: launched with programmatic stream serialisation,
-// so that its CTAs start as the previous group's CTAs finish instead of
-// after the whole previous grid (the groups' tissues are disjoint).
-inline int batch_group_launch(int g, bool attr_only, bool overlap, int grid,
+// `attr_only`); `pair`: the column-pair form (kernel 3).  `overlap`:
+// launched with programmatic stream serialisation, so that its CTAs start
+// as the previous group's CTAs finish instead of after the whole previous
+// grid (the groups' tissues are disjoint).
+inline int batch_group_launch(int g, bool pair, bool attr_only, bool overlap, int grid,
                               const BTissueT *desc, const BTileT *tl, int32_t t_begin,
                               int32_t t_end, int32_t n_tissues, int32_t in_buf,
                               uint32_t *counters, cudaStream_t stream)
@@ -782,18 +825,14 @@ inline int batch_group_launch(int g, bool attr_only, bool overlap, int grid,
     cfg.numAttrs = 1;
 #define FW_BATCH_GROUP(GI, M, ST)                                                 \
     case GI:                                                                      \
-        if (attr_only) {                                                          \
-            FW_CUDA_CHECK(cudaFuncSetAttribute(                                   \
-                k_batch_tma<M, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                (int)tma_smem<M, ST>()));                                         \
-            return FW_OK;                                                         \
-        }                                                                         \
-        cfg.dynamicSmemBytes = tma_smem<M, ST>();                                 \
-        FW_CUDA_CHECK(cudaLaunchKernelEx(&cfg, k_batch_tma<M, ST>, desc, tl,      \
-                                         t_begin, t_end, n_tissues, in_buf,       \
-                                         counters));                              \
-        FW_CHECK_LAUNCH("k_batch_tma");                                           \
-        return FW_OK;
+        if (pair)                                                                 \
+            return batch_group_launch_k(k_batch_tma<M, ST, true>,                 \
+                                        tma_smem<M, ST>(), attr_only, cfg, desc,  \
+                                        tl, t_begin, t_end, n_tissues, in_buf,    \
+                                        counters);                                \
+        return batch_group_launch_k(k_batch_tma<M, ST, false>, tma_smem<M, ST>(), \
+                                    attr_only, cfg, desc, tl, t_begin, t_end,     \
+                                    n_tissues, in_buf, counters);
     switch (g) {
         FW_BATCH_GROUP(0, ModelAP, FW_STENCIL_ISO5)
         FW_BATCH_GROUP(1, ModelAP, FW_STENCIL_ANISO9)
@@ -832,7 +871,7 @@ bool tma_tissue_ok(const fw_step_args *a)
 }
 
 // Fill one tissue's descriptor of the TMA form.
-int fill_tma_tissue(const fw_step_args *a, int64_t n_begin, BTissueT &T)
+int fill_tma_tissue(const fw_step_args *a, int64_t n_begin, BTissueT &T, bool pair)
 {
     using namespace fused;
     const int64_t pitch = a->pitch ? a->pitch : a->nj;
@@ -840,8 +879,10 @@ int fill_tma_tissue(const fw_step_args *a, int64_t n_begin, BTissueT &T)
     const int cen = a->stencil == FW_STENCIL_ISO5 ? 2 : 4;
     int ns = 0, np = 0;
     fw_model_info(a->model, &ns, &np);
-    bool ok = encode_weights(&T.maps.w, a->weights_packed, nwo, a->nj, a->ni, LH,
-                             pitch) &&
+    bool ok = (pair ? encode_weights_pairs(&T.maps.w, a->weights_packed, nwo, a->nj,
+                                           a->ni, LH, pitch)
+                    : encode_weights(&T.maps.w, a->weights_packed, nwo, a->nj, a->ni,
+                                     LH, pitch)) &&
               encode_2d(&T.maps.myo, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a->myo, a->nj,
                         a->ni, kBoxB, LH, pitch) &&
               encode_2d(&T.maps.u[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->u[0],
@@ -917,15 +958,17 @@ int fill_tma_tissue(const fw_step_args *a, int64_t n_begin, BTissueT &T)
 }
 
 // Kernel of a batch: 2 (TMA) when every tissue can take it, unless every
-// tissue asks for cp.async staging (fused_variant 1 or 2); else 1.  A row
-// pitch other than nj needs the TMA kernel.
+// tissue asks for cp.async staging (fused_variant 1 or 2), or 3 (TMA,
+// column pairs in two-wide instructions) when every tissue asks for
+// fused_variant 6; else 1.  A row pitch other than nj needs a TMA kernel.
 int choose_kernel(const fw_step_args *const *tissues, int32_t n, int *kernel)
 {
-    bool tma = true, cp = true, pitched = false;
+    bool tma = true, cp = true, pair = true, pitched = false;
     for (int i = 0; i < n; ++i) {
         const fw_step_args *a = tissues[i];
         tma &= tma_tissue_ok(a);
         cp &= a->fused_variant == 1 || a->fused_variant == 2;
+        pair &= a->fused_variant == 6;
         pitched |= a->pitch != 0 && a->pitch != a->nj;
     }
     if (pitched && (!tma || cp)) {
@@ -934,7 +977,7 @@ int choose_kernel(const fw_step_args *const *tissues, int32_t n, int *kernel)
                   "packed weights)");
         return FW_ERR_UNSUPPORTED;
     }
-    *kernel = tma && !cp ? 2 : 1;
+    *kernel = tma && !cp ? (pair ? 3 : 2) : 1;
     return FW_OK;
 }
 
@@ -963,8 +1006,8 @@ int batch_plan_size(const fw_step_args *const *tissues, int32_t n,
         int rc = choose_kernel(tissues, n, &kernel);
         if (rc) return rc;
     }
-    const size_t desc = kernel == 2 ? sizeof(BTissueT) : sizeof(BTissue);
-    const size_t tile = kernel == 2 ? sizeof(BTileT) : sizeof(BTile);
+    const size_t desc = kernel >= 2 ? sizeof(BTissueT) : sizeof(BTissue);
+    const size_t tile = kernel >= 2 ? sizeof(BTileT) : sizeof(BTile);
     *bytes = (int64_t)(align_up(desc * n, 256) + tile * (size_t)n_tiles);
     return FW_OK;
 }
@@ -989,21 +1032,21 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     int kernel = 1;
     rc = choose_kernel(tissues, n, &kernel);
     if (rc) return rc;
-    if (((uintptr_t)plan & (kernel == 2 ? 127 : 15)) != 0) {
+    if (((uintptr_t)plan & (kernel >= 2 ? 127 : 15)) != 0) {
         set_error("fw_batch_plan: plan must be %d-byte aligned",
-                  kernel == 2 ? 128 : 16);
+                  kernel >= 2 ? 128 : 16);
         return FW_ERR_ARG;
     }
     // host staging, 128-byte aligned like the device plan (the descriptors
     // of the TMA form hold 64-byte aligned tensor maps)
     std::vector<unsigned char> raw((size_t)need + 128, 0);
     unsigned char *host = raw.data() + ((128 - ((uintptr_t)raw.data() & 127)) & 127);
-    const size_t desc_bytes = kernel == 2 ? sizeof(BTissueT) : sizeof(BTissue);
+    const size_t desc_bytes = kernel >= 2 ? sizeof(BTissueT) : sizeof(BTissue);
     unsigned char *tiles_host = host + align_up(desc_bytes * n, 256);
-    if (kernel == 2) {
+    if (kernel >= 2) {
         BTissueT *desc = reinterpret_cast<BTissueT *>(host);
         for (int i = 0; i < n; ++i) {
-            rc = fill_tma_tissue(tissues[i], n_begin[i], desc[i]);
+            rc = fill_tma_tissue(tissues[i], n_begin[i], desc[i], kernel == 3);
             if (rc) return rc;
         }
     } else {
@@ -1080,7 +1123,7 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     for (int i : order) {
         const fw_step_args *a = tissues[i];
         const int32_t nt = (int32_t)tissue_tiles(a);
-        if (kernel == 2) {
+        if (kernel >= 2) {
             BTileT *tl = reinterpret_cast<BTileT *>(tiles_host);
             const int32_t tj = (int32_t)((a->nj + TJ - 1) / TJ);
             for (int32_t k = 0; k < nt; ++k)
@@ -1102,11 +1145,11 @@ int batch_plan(const fw_step_args *const *tissues, int32_t n,
     int dev = 0, sms = 0, per_sm = 0;
     FW_CUDA_CHECK(cudaGetDevice(&dev));
     FW_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    if (kernel == 2) {
+    if (kernel >= 2) {
         // one persistent CTA per SM (the stages fill its shared memory)
         for (int g = 0; g < kGroups; ++g) {
-            int rc2 = batch_group_launch(g, true, false, 0, nullptr, nullptr, 0, 0, 0, 0,
-                                         nullptr, stream);
+            int rc2 = batch_group_launch(g, kernel == 3, true, false, 0, nullptr,
+                                         nullptr, 0, 0, 0, 0, nullptr, stream);
             if (rc2) return rc2;
         }
         per_sm = 1;
@@ -1142,7 +1185,7 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
 {
     using namespace batch;
     if (!b || !b->plan || !scratch || b->n_tissues <= 0 || b->grid <= 0 ||
-        (b->kernel != 1 && b->kernel != 2)) {
+        b->kernel < 1 || b->kernel > 3) {
         set_error("fw_batch_run: empty plan or NULL scratch");
         return FW_ERR_ARG;
     }
@@ -1154,14 +1197,14 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
     // the plan set the shared-memory attribute on this device; set it again
     // unless the stream is being captured into a CUDA graph (the launches
     // alone are recorded then)
-    const bool tma = b->kernel == 2;
+    const bool tma = b->kernel >= 2, pair = b->kernel == 3;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     FW_CUDA_CHECK(cudaStreamIsCapturing(stream, &cap));
     if (cap == cudaStreamCaptureStatusNone) {
         if (tma) {
             for (int g = 0; g < kGroups; ++g) {
-                int rc = batch_group_launch(g, true, false, 0, nullptr, nullptr, 0, 0, 0, 0,
-                                            nullptr, stream);
+                int rc = batch_group_launch(g, pair, true, false, 0, nullptr, nullptr, 0,
+                                            0, 0, 0, nullptr, stream);
                 if (rc) return rc;
             }
         } else {
@@ -1201,7 +1244,7 @@ int batch_run(const fw_batch *b, uint32_t *scratch, int64_t offset,
                 const int32_t end = b->group_end[g];
                 if (end > begin) {
                     const int grid = end - begin < b->grid ? end - begin : b->grid;
-                    int rc = batch_group_launch(g, false, !first, grid, desc_t, tl_t,
+                    int rc = batch_group_launch(g, pair, false, !first, grid, desc_t, tl_t,
                                                 begin, end, b->n_tissues, in_buf,
                                                 scratch + 2 + 2 * g, stream);
                     if (rc) return rc;
@@ -1253,7 +1296,7 @@ int batch_run_noalloc(const fw_batch *b, int64_t offset, int64_t n_steps,
 {
     // the argument checks of batch_run, before the one-time set-up
     if (!b || !b->plan || b->n_tissues <= 0 || b->grid <= 0 ||
-        (b->kernel != 1 && b->kernel != 2)) {
+        b->kernel < 1 || b->kernel > 3) {
         set_error("fw_batch_run_noalloc: empty plan");
         return FW_ERR_ARG;
     }

@@ -39,6 +39,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <type_traits>
+
 #include "fw_internal.cuh"
 #include "fw_models.cuh"
 
@@ -172,23 +174,88 @@ __device__ __forceinline__ float stencil_fma(float wcen, float c, const float4 &
                                              float ur, float ml, float mr, float dl,
                                              float dc, float dr)
 {
-    float un = wcen * c;
+    float un = f_mul(wcen, c);
     if constexpr (ST == FW_STENCIL_ISO5) {
-        un = fmaf(wa.x, uc, un);
-        un = fmaf(wa.y, ml, un);
-        un = fmaf(wa.z, mr, un);
-        un = fmaf(wa.w, dc, un);
+        un = f_fma(wa.x, uc, un);
+        un = f_fma(wa.y, ml, un);
+        un = f_fma(wa.z, mr, un);
+        un = f_fma(wa.w, dc, un);
     } else {
-        un = fmaf(wa.x, ul, un);
-        un = fmaf(wa.y, uc, un);
-        un = fmaf(wa.z, ur, un);
-        un = fmaf(wa.w, ml, un);
-        un = fmaf(wb.x, mr, un);
-        un = fmaf(wb.y, dl, un);
-        un = fmaf(wb.z, dc, un);
-        un = fmaf(wb.w, dr, un);
+        un = f_fma(wa.x, ul, un);
+        un = f_fma(wa.y, uc, un);
+        un = f_fma(wa.z, ur, un);
+        un = f_fma(wa.w, ml, un);
+        un = f_fma(wb.x, mr, un);
+        un = f_fma(wb.y, dl, un);
+        un = f_fma(wb.z, dc, un);
+        un = f_fma(wb.w, dr, un);
     }
     return un;
+}
+
+// stencil_fma for two adjacent nodes of a row in two-wide instructions:
+// w[q] = (node 0's, node 1's) off-centre weight q, and each window argument
+// the pair of values the two nodes' chains take at that position.  Each
+// lane is stencil_fma's chain, bit for bit.
+template <int ST>
+__device__ __forceinline__ float2 stencil_fma2(float2 wcen, float2 c, const float2 *w,
+                                               float2 ul, float2 uc, float2 ur,
+                                               float2 ml, float2 mr, float2 dl,
+                                               float2 dc, float2 dr)
+{
+    float2 un = f2_mul(wcen, c);
+    if constexpr (ST == FW_STENCIL_ISO5) {
+        un = f2_fma(w[0], uc, un);
+        un = f2_fma(w[1], ml, un);
+        un = f2_fma(w[2], mr, un);
+        un = f2_fma(w[3], dc, un);
+    } else {
+        un = f2_fma(w[0], ul, un);
+        un = f2_fma(w[1], uc, un);
+        un = f2_fma(w[2], ur, un);
+        un = f2_fma(w[3], ml, un);
+        un = f2_fma(w[4], mr, un);
+        un = f2_fma(w[5], dl, un);
+        un = f2_fma(w[6], dc, un);
+        un = f2_fma(w[7], dr, un);
+    }
+    return un;
+}
+
+// The ionic update of the fused and batched kernels: a model with a
+// two-node form (M::update_pair) uses its explicitly rounded float32
+// update (M::update_fused), which the pair form reproduces per node;
+// otherwise update<float>, once per node.
+template <class M, class = void>
+struct has_pair_form : std::false_type {};
+template <class M>
+struct has_pair_form<M, std::void_t<decltype(&M::update_pair)>> : std::true_type {};
+
+template <class M>
+__device__ __forceinline__ float fused_update(float u, float un,
+                                              typename M::template St<float> &x,
+                                              const Params<float, M::NP> &P, float dt)
+{
+    if constexpr (has_pair_form<M>::value)
+        return M::update_fused(u, un, x, P, dt);
+    else
+        return M::template update<float>(u, un, x, P, dt);
+}
+
+template <class M>
+__device__ __forceinline__ float2 fused_update_pair(float2 u, float2 un,
+                                                   typename M::template St<float> &x0,
+                                                   typename M::template St<float> &x1,
+                                                   const Params<float, M::NP> &P,
+                                                   float dt)
+{
+    if constexpr (has_pair_form<M>::value) {
+        return M::update_pair(u, un, x0, x1, P, dt);
+    } else {
+        const float a = M::template update<float>(u.x, un.x, x0, P, dt);
+        const float b = M::template update<float>(u.y, un.y, x1, P, dt);
+        return make_float2(a, b);
+    }
 }
 
 // Rows r < R of a strip (potential x[r + 1]) that compare with a threshold,
@@ -515,7 +582,7 @@ __global__ void __launch_bounds__(LW *(LH / R), MINB)
             const float un = stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r], wr[r],
                                              wl[r + 1], wr[r + 1], wl[r + 2],
                                              wc[r + 2], wr[r + 2]);
-            const float uu = M::template update<float>(b1, un, st[r], P, dt);
+            const float uu = fused_update<M>(b1, un, st[r], P, dt);
             nxt[lr + 1][col + 1] = ((upd >> r) & 1u) ? uu : b1;
         }
         // probes: u after the stimuli, the state after the update

@@ -245,10 +245,9 @@ __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> 
                                            uint64_t *bar, int bi, int bj)
 {
     constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
-    // the column-pair kernel reads the flags from global memory
     issue_region<KMAX, NS, NWO, PAIRS, FLY>(k.maps, k.in_buf, G, bar,
                                             bi * TI - KMAX, bj * TJ - KMAX, 0u,
-                                            !PAIRS && k.f.n_lat > 0);
+                                            k.f.n_lat > 0);
 }
 
 // minor_component (asymmetric_stencil_2d.py:204-259) in float32.
@@ -571,7 +570,7 @@ __device__ __forceinline__ void tma_tile(const FusedK &f, Stage &G, Sm &S, int o
             const float un = stencil_fma<ST>(wcen[r], b1, wa, wb, wl[r], wc[r],
                                              wr[r], wl[r + 1], wr[r + 1],
                                              wl[r + 2], wc[r + 2], wr[r + 2]);
-            const float uu = M::template update<float>(b1, un, st[r], P, dt);
+            const float uu = fused_update<M>(b1, un, st[r], P, dt);
             nxt[lr + 1][col + xo] = ((upd >> r) & 1u) ? uu : b1;
         }
         // probes: u after the stimuli, the state after the update
@@ -694,14 +693,345 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
 // float4s.  Each node's arithmetic is k_fused_tma's, in the same order.
 // Needs an even region origin (even KMAX), which makes the float2 offsets
 // 8-byte aligned.
+//
+// PACK (fused variant 6): the two columns of a row advance together in
+// Blackwell's two-wide float32 instructions (f2_fma, f2_mul, f2_add: one
+// issue for both lanes, each lane rounded as the scalar instruction).  The
+// block's weights are read from the stage once per tile into registers as
+// (column c0, column c0 + 1) pairs; a sub-step forms a row's two diffusion
+// sums as one chain of pair FMAs over the window pairs left = (c0 - 1, c0),
+// centre = (c0, c0 + 1) and right = (c0 + 1, c0 + 2), and the ionic update
+// in pair form where the model has one (M::update_pair).  The arithmetic
+// instructions per node about halve; every node keeps k_fused_tma's bits.
 
-template <class M, int ST, int KMAX, int LH>
+// Nodes j = 2 r + h (row r0 + r, column c0 + h) of the block of thread
+// (c0, r0) inside the region's interior (own) and off its outer ring (ring).
+template <int KMAX, int LH>
+__device__ __forceinline__ void pair_masks(int c0, int r0, uint32_t &own_c,
+                                           uint32_t &ring_c)
+{
+    constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
+    own_c = ring_c = 0;
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int lr = r0 + r, lc = c0 + h, j = 2 * r + h;
+            if (lc >= KMAX && lc < KMAX + TJ && lr >= KMAX && lr < KMAX + TI)
+                own_c |= 1u << j;
+            if (lc > 0 && lc < kTW - 1 && lr > 0 && lr < LH - 1) ring_c |= 1u << j;
+        }
+}
+
+// One staged tile of the column-pair kernels (k_fused_tma2 and the batched
+// pair kernel): K sub-steps of the region with origin (oi, oj) from stage G,
+// then the interior written back.  As tma_tile: u_out, state and the local
+// activation flags have row pitch f.pitch, the tracker arrays and stimulus
+// masks row length f.nj; u1 is the ping-pong partner of the stage's
+// potential.
+template <class M, int ST, int KMAX, int LH, bool PACK, class Stage, class Sm>
+__device__ __forceinline__ void tma_tile2(const FusedK &f, Stage &G, Sm &S, int oi,
+                                          int oj, uint32_t own_c, uint32_t ring_c,
+                                          const Params<float, M::NP> &P)
+{
+    constexpr int LW = kTW, HW = kTW / 2;   // columns, column pairs
+    constexpr int R = 2;                     // rows per thread
+    constexpr int NT = HW * (LH / R);
+    constexpr int TI = LH - 2 * KMAX, TJ = LW - 2 * KMAX;
+    constexpr int NS = M::NS;
+    constexpr int NWO = Stencil2D<ST>::NWO;
+    const int tid = threadIdx.x;
+    const int cp = tid % HW;        // column pair
+    const int c0 = 2 * cp;          // first of the thread's two columns
+    const int r0 = (tid / HW) * R;
+    const float dt = f.dt;
+
+    const int xo = oj - floor_to(oj - 1, 4);   // 2 or 4 (oj is even)
+    const int xo8 = oj - floor_to(oj, 16);     // 0..14, even
+    const int gj0 = oj + c0;
+    const int cx = c0 + xo;                    // float2-aligned window column
+
+    typename M::template St<float> st[2 * R];
+    uint32_t myo_bits = 0, inb = 0;
+    float wcen[2 * R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int lr = r0 + r, gi = oi + lr;
+        const bool row_in = (unsigned)gi < (unsigned)f.ni;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = 2 * r + h;
+            if (row_in && (unsigned)(gj0 + h) < (unsigned)f.nj) inb |= 1u << j;
+            if (G.myo[lr][c0 + h + xo8]) myo_bits |= 1u << j;
+        }
+        float sv0[kMaxTmaState], sv1[kMaxTmaState];
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            const float2 v2 = *reinterpret_cast<const float2 *>(&G.s[q][lr][cx]);
+            sv0[q] = v2.x;
+            sv1[q] = v2.y;
+        }
+        st[2 * r] = M::template from_array<float>(sv0);
+        st[2 * r + 1] = M::template from_array<float>(sv1);
+        const float2 w2 = *reinterpret_cast<const float2 *>(&G.wc[lr][cx]);
+        wcen[2 * r] = w2.x;
+        wcen[2 * r + 1] = w2.y;
+    }
+    myo_bits &= inb;
+    const uint32_t own = own_c & inb;
+    const uint32_t upd = ring_c & myo_bits;
+
+    // PACK: the block's weights as (column c0, column c0 + 1) pairs, read
+    // once for the tile
+    float2 wp[PACK ? R : 1][PACK ? NWO : 1];
+    float2 wcp[PACK ? R : 1];
+    if constexpr (PACK) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int lr = r0 + r;
+            const float4 a0 = G.wa[lr][cp], a1 = G.wa[lr][HW + cp];
+            wp[r][0] = make_float2(a0.x, a1.x);
+            wp[r][1] = make_float2(a0.y, a1.y);
+            wp[r][2] = make_float2(a0.z, a1.z);
+            wp[r][3] = make_float2(a0.w, a1.w);
+            if constexpr (NWO == 8) {
+                const float4 b0 = G.wb[lr][cp], b1 = G.wb[lr][HW + cp];
+                wp[r][4] = make_float2(b0.x, b1.x);
+                wp[r][5] = make_float2(b0.y, b1.y);
+                wp[r][6] = make_float2(b0.z, b1.z);
+                wp[r][7] = make_float2(b0.w, b1.w);
+            }
+            wcp[r] = make_float2(wcen[2 * r], wcen[2 * r + 1]);
+        }
+    }
+
+    // probe cells of this tile
+    uint32_t probe_mine = 0;
+    if (f.n_probe) {
+        for (int i = tid; i < (LH * LW + 31) / 32; i += NT) S.probe_bits[i] = 0;
+        if (tid == 0) S.probe_count = 0;
+        __syncthreads();
+        for (int t = 0; t < f.n_probe; ++t) {
+            const FProbe &pr = f.probe[t];
+            for (int c = tid; c < pr.n_cells; c += NT) {
+                const int64_t p = pr.cells[c];
+                const int gi = (int)(p / f.nj), gjj = (int)(p % f.nj);
+                const int lr = gi - oi, lc = gjj - oj;
+                if (lr >= KMAX && lr < KMAX + TI && lc >= KMAX && lc < KMAX + TJ) {
+                    const int e = atomicAdd(&S.probe_count, 1);
+                    if (e < kMaxFusedProbeEntries) {
+                        S.probe_list[e] = ProbeEntry{(int16_t)lr, (int16_t)lc,
+                                                     (int16_t)t, c};
+                        const int bit = lr * LW + lc;
+                        atomicOr(&S.probe_bits[bit >> 5], 1u << (bit & 31));
+                    } else if (f.status) {
+                        atomicOr(f.status, FW_DEV_PROBE_OVERFLOW);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 2 * R; ++j) {
+            const int bit = (r0 + j / 2) * LW + c0 + (j & 1);
+            if ((S.probe_bits[bit >> 5] >> (bit & 31)) & 1u) probe_mine |= 1u << j;
+        }
+    }
+    // the local activation flags of the block, staged with the region
+    uint32_t lat_act = 0, at_done = 0;
+    if (f.n_lat) {
+#pragma unroll
+        for (int j = 0; j < 2 * R; ++j)
+            if (((own >> j) & 1u) && G.act[r0 + j / 2][c0 + (j & 1) + xo8])
+                lat_act |= 1u << j;
+    }
+    const uint32_t lat_act0 = lat_act;
+
+    // the launch's per-sub-step controls, read once per tile
+    const int ksteps = f.ksteps;
+    const int64_t n0 = f.n0;
+    const uint32_t stim_on = f.stim_on, probe_on = f.probe_on;
+    uint32_t at_on[kMaxFusedAt], lat_on[kMaxFusedLat];
+    float at_thr[kMaxFusedAt], lat_thr[kMaxFusedLat];
+#pragma unroll
+    for (int aa = 0; aa < kMaxFusedAt; ++aa) {
+        at_on[aa] = aa < f.n_at ? f.at[aa].on : 0u;
+        at_thr[aa] = f.at[aa].thr;
+    }
+#pragma unroll
+    for (int l = 0; l < kMaxFusedLat; ++l) {
+        lat_on[l] = l < f.n_lat ? f.lat[l].on : 0u;
+        lat_thr[l] = f.lat[l].thr;
+    }
+
+    // ---- sub-steps ----
+    for (int s = 0; s < ksteps; ++s) {
+        const int64_t n = n0 + s;
+        float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
+        float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;
+
+        if ((stim_on >> s) & 1u) {
+            for (int i = 0; i < f.n_stims; ++i) {
+                const FStim &F = f.stims[i];
+                if (!((F.on >> s) & 1u)) continue;
+#pragma unroll
+                for (int j = 0; j < 2 * R; ++j) {
+                    if (!((myo_bits >> j) & 1u)) continue;
+                    const int lr = r0 + j / 2, gi = oi + lr, gj = gj0 + (j & 1);
+                    if (gj < F.lo1 || gj >= F.hi1) continue;
+                    if (gi < F.lo0 || gi >= F.hi0) continue;
+                    if (F.mask && !F.mask[(int64_t)gi * f.nj + gj]) continue;
+                    float x = cur[lr + 1][cx + (j & 1)];
+                    if (F.kind == FW_STIM_VOLTAGE) {
+                        x = F.value;
+                    } else {
+                        x = x + F.value;
+                        if (F.has_umax && x > F.u_max) x = F.u_max;
+                    }
+                    cur[lr + 1][cx + (j & 1)] = x;
+                }
+            }
+            __syncthreads();
+        }
+
+        // window rows r0 - 1 .. r0 + R: a = column c0 - 1, (m0, m1) =
+        // columns c0, c0 + 1, b = column c0 + 2
+        float a[R + 2], m0[R + 2], m1[R + 2], b[R + 2];
+#pragma unroll
+        for (int i = 0; i < R + 2; ++i) {
+            a[i] = cur[r0 + i][cx - 1];
+            const float2 mm = *reinterpret_cast<const float2 *>(&cur[r0 + i][cx]);
+            m0[i] = mm.x;
+            m1[i] = mm.y;
+            b[i] = cur[r0 + i][cx + 2];
+        }
+
+        if (own) {
+            const float mx = fmaxf(fmaxf(m0[1], m1[1]), fmaxf(m0[2], m1[2]));
+#pragma unroll
+            for (int aa = 0; aa < kMaxFusedAt; ++aa) {
+                if (!((at_on[aa] >> s) & 1u)) continue;
+                // (fmaxf skips NaN nodes, which never cross)
+                const float thr = at_thr[aa];
+                if (!(mx > thr)) continue;
+                uint32_t hit = (m0[1] > thr ? 1u : 0u) | (m1[1] > thr ? 2u : 0u) |
+                               (m0[2] > thr ? 4u : 0u) | (m1[2] > thr ? 8u : 0u);
+                hit &= own & ~(at_done >> (aa * 8));
+                if (hit) {
+#pragma unroll
+                    for (int j = 0; j < 2 * R; ++j) {
+                        if (!((hit >> j) & 1u)) continue;
+                        // first crossing: unsigned minimum, "never" = -1
+                        // (activation_time_2d_tracker.py:61-63)
+                        const int64_t p =
+                            (int64_t)(oi + r0 + j / 2) * f.nj + gj0 + (j & 1);
+                        atomicMin(reinterpret_cast<unsigned *>(f.at[aa].act) + p,
+                                  (unsigned)n);
+                    }
+                    at_done |= hit << (aa * 8);
+                }
+            }
+#pragma unroll
+            for (int l = 0; l < kMaxFusedLat; ++l) {
+                if (!((lat_on[l] >> s) & 1u)) continue;
+                // (local_activation_time_2d_tracker.py:71-89)
+                const float thr = lat_thr[l];
+                const uint32_t ge = (m0[1] >= thr ? 1u : 0u) | (m1[1] >= thr ? 2u : 0u) |
+                                    (m0[2] >= thr ? 4u : 0u) | (m1[2] >= thr ? 8u : 0u);
+                const uint32_t lt = (m0[1] < thr ? 1u : 0u) | (m1[1] < thr ? 2u : 0u) |
+                                    (m0[2] < thr ? 4u : 0u) | (m1[2] < thr ? 8u : 0u);
+                const uint32_t was = (lat_act >> (l * 8)) & 0xffu;
+                const uint32_t rise = ge & own & ~was;
+                const uint32_t fall = lt & own & was;
+                lat_act ^= (rise | fall) << (l * 8);
+                if (rise) {
+#pragma unroll
+                    for (int j = 0; j < 2 * R; ++j)
+                        if ((rise >> j) & 1u)
+                            lat_record(f.lat[l],
+                                       (int64_t)(oi + r0 + j / 2) * f.nj + gj0 + (j & 1),
+                                       f.n, n, f.status);
+                }
+            }
+        }
+
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int lr = r0 + r;
+            float2 uu;
+            if constexpr (PACK) {
+                const float2 c1 = make_float2(m0[r + 1], m1[r + 1]);
+                const float2 un = stencil_fma2<ST>(
+                    wcp[r], c1, wp[r], make_float2(a[r], m0[r]),
+                    make_float2(m0[r], m1[r]), make_float2(m1[r], b[r]),
+                    make_float2(a[r + 1], m0[r + 1]), make_float2(m1[r + 1], b[r + 1]),
+                    make_float2(a[r + 2], m0[r + 2]), make_float2(m0[r + 2], m1[r + 2]),
+                    make_float2(m1[r + 2], b[r + 2]));
+                uu = fused_update_pair<M>(c1, un, st[2 * r], st[2 * r + 1], P, dt);
+            } else {
+                const float4 wa0 = G.wa[lr][cp], wa1 = G.wa[lr][HW + cp];
+                float4 wb0 = wa0, wb1 = wa1;
+                if constexpr (NWO == 8) {
+                    wb0 = G.wb[lr][cp];
+                    wb1 = G.wb[lr][HW + cp];
+                }
+                const float un0 = stencil_fma<ST>(wcen[2 * r], m0[r + 1], wa0, wb0, a[r],
+                                                  m0[r], m1[r], a[r + 1], m1[r + 1],
+                                                  a[r + 2], m0[r + 2], m1[r + 2]);
+                const float un1 = stencil_fma<ST>(wcen[2 * r + 1], m1[r + 1], wa1, wb1,
+                                                  m0[r], m1[r], b[r], m0[r + 1],
+                                                  b[r + 1], m0[r + 2], m1[r + 2],
+                                                  b[r + 2]);
+                uu.x = fused_update<M>(m0[r + 1], un0, st[2 * r], P, dt);
+                uu.y = fused_update<M>(m1[r + 1], un1, st[2 * r + 1], P, dt);
+            }
+            float2 o;
+            o.x = ((upd >> (2 * r)) & 1u) ? uu.x : m0[r + 1];
+            o.y = ((upd >> (2 * r + 1)) & 1u) ? uu.y : m1[r + 1];
+            *reinterpret_cast<float2 *>(&nxt[lr + 1][cx]) = o;
+        }
+        // probes: u after the stimuli, the state after the update
+        if (probe_mine && ((probe_on >> s) & 1u)) {
+#pragma unroll
+            for (int j = 0; j < 2 * R; ++j)
+                if ((probe_mine >> j) & 1u)
+                    write_probes<M>(f, S.probe_list, S.probe_count, r0 + j / 2,
+                                    c0 + (j & 1), s,
+                                    (j & 1) ? m1[j / 2 + 1] : m0[j / 2 + 1], st[j],
+                                    ((myo_bits >> j) & 1u) != 0,
+                                    (int64_t)(oi + r0 + j / 2) * f.pitch + gj0 +
+                                        (j & 1));
+        }
+        __syncthreads();
+    }
+
+    // ---- write the interior back ----
+    float(*fin)[kBoxF] = (ksteps & 1) ? S.u1 : G.u;
+    bool nonfinite = false;
+#pragma unroll
+    for (int j = 0; j < 2 * R; ++j) {
+        if (!((own >> j) & 1u)) continue;
+        const int lr = r0 + j / 2;
+        const int64_t pp = (int64_t)(oi + lr) * f.pitch + gj0 + (j & 1);
+        if ((myo_bits >> j) & 1u) {
+            const float uo = fin[lr + 1][cx + (j & 1)];
+            f.u_out[pp] = uo;
+            nonfinite |= !isfinite(uo);
+            M::template store<float>(f.state_out, pp, st[j]);
+        }
+        // the flags that changed in this launch (rows of f.pitch nodes)
+        if (((lat_act ^ lat_act0) >> j) & 1u)
+            f.lat[0].activated[pp] = (lat_act >> j) & 1u;
+    }
+    if (nonfinite && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
+}
+
+template <class M, int ST, int KMAX, int LH, bool PACK>
 __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
     k_fused_tma2(const __grid_constant__ TmaK k)
 {
     constexpr int LW = kTW, HW = kTW / 2;   // columns, column pairs
     constexpr int R = 2;                     // rows per thread
-    constexpr int NT = HW * (LH / R);
     constexpr int TI = LH - 2 * KMAX, TJ = LW - 2 * KMAX;
     constexpr int NS = M::NS;
     constexpr int NWO = Stencil2D<ST>::NWO;
@@ -716,21 +1046,8 @@ __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
     const FusedK &f = k.f;
 
     const int tid = threadIdx.x;
-    const int cp = tid % HW;        // column pair
-    const int c0 = 2 * cp;          // first of the thread's two columns
-    const int r0 = (tid / HW) * R;
-    // node j = 2 r + h sits at row r0 + r, column c0 + h; the masks below do
-    // not depend on the tile
-    uint32_t own_c = 0, ring_c = 0;
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int lr = r0 + r, lc = c0 + h, j = 2 * r + h;
-            if (lc >= KMAX && lc < KMAX + TJ && lr >= KMAX && lr < KMAX + TI)
-                own_c |= 1u << j;
-            if (lc > 0 && lc < LW - 1 && lr > 0 && lr < LH - 1) ring_c |= 1u << j;
-        }
+    uint32_t own_c, ring_c;
+    pair_masks<KMAX, LH>(2 * (tid % HW), (tid / HW) * R, own_c, ring_c);
 
     if (tid == 0) {
         mbar_init(&S.bar[0], 1);
@@ -748,7 +1065,6 @@ __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
     Params<float, M::NP> P;
 #pragma unroll
     for (int i = 0; i < M::NP; ++i) P.v[i] = f.params[i];
-    const float dt = f.dt;
     unsigned parity = 0u;
 
     for (int it = 0; tile < k.tiles; ++it, tile += gridDim.x) {
@@ -772,248 +1088,10 @@ __global__ void __launch_bounds__((kTW / 2) * (LH / 2), 1)
             if (tid == 0) tma_abandon(k, S.bar, sg, ph, parity, arrived, next);
             return;
         }
-
         const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
         bi = ni_;
         bj = nj_;
-        const int xo = oj - floor_to(oj - 1, 4);   // 2 or 4 (oj is even)
-        const int xo8 = oj - floor_to(oj, 16);     // 0..14, even
-        const int gj0 = oj + c0;
-        const int cx = c0 + xo;                    // float2-aligned window column
-
-        typename M::template St<float> st[2 * R];
-        uint32_t myo_bits = 0, inb = 0;
-        float wcen[2 * R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int lr = r0 + r, gi = oi + lr;
-            const bool row_in = (unsigned)gi < (unsigned)f.ni;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int j = 2 * r + h;
-                if (row_in && (unsigned)(gj0 + h) < (unsigned)f.nj) inb |= 1u << j;
-                if (G.myo[lr][c0 + h + xo8]) myo_bits |= 1u << j;
-            }
-            float sv0[kMaxTmaState], sv1[kMaxTmaState];
-#pragma unroll
-            for (int q = 0; q < NS; ++q) {
-                const float2 v2 = *reinterpret_cast<const float2 *>(&G.s[q][lr][cx]);
-                sv0[q] = v2.x;
-                sv1[q] = v2.y;
-            }
-            st[2 * r] = M::template from_array<float>(sv0);
-            st[2 * r + 1] = M::template from_array<float>(sv1);
-            const float2 w2 = *reinterpret_cast<const float2 *>(&G.wc[lr][cx]);
-            wcen[2 * r] = w2.x;
-            wcen[2 * r + 1] = w2.y;
-        }
-        myo_bits &= inb;
-        const uint32_t own = own_c & inb;
-        const uint32_t upd = ring_c & myo_bits;
-
-        // probe cells of this tile
-        uint32_t probe_mine = 0;
-        if (f.n_probe) {
-            for (int i = tid; i < (LH * LW + 31) / 32; i += NT) S.probe_bits[i] = 0;
-            if (tid == 0) S.probe_count = 0;
-            __syncthreads();
-            for (int t = 0; t < f.n_probe; ++t) {
-                const FProbe &pr = f.probe[t];
-                for (int c = tid; c < pr.n_cells; c += NT) {
-                    const int64_t p = pr.cells[c];
-                    const int gi = (int)(p / f.nj), gjj = (int)(p % f.nj);
-                    const int lr = gi - oi, lc = gjj - oj;
-                    if (lr >= KMAX && lr < KMAX + TI && lc >= KMAX &&
-                        lc < KMAX + TJ) {
-                        const int e = atomicAdd(&S.probe_count, 1);
-                        if (e < kMaxFusedProbeEntries) {
-                            S.probe_list[e] = ProbeEntry{(int16_t)lr, (int16_t)lc,
-                                                         (int16_t)t, c};
-                            const int bit = lr * LW + lc;
-                            atomicOr(&S.probe_bits[bit >> 5], 1u << (bit & 31));
-                        } else if (f.status) {
-                            atomicOr(f.status, FW_DEV_PROBE_OVERFLOW);
-                        }
-                    }
-                }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int j = 0; j < 2 * R; ++j) {
-                const int bit = (r0 + j / 2) * LW + c0 + (j & 1);
-                if ((S.probe_bits[bit >> 5] >> (bit & 31)) & 1u) probe_mine |= 1u << j;
-            }
-        }
-        uint32_t lat_act = 0, at_done = 0;
-#pragma unroll
-        for (int l = 0; l < kMaxFusedLat; ++l)
-            if (l < f.n_lat) {
-#pragma unroll
-                for (int j = 0; j < 2 * R; ++j)
-                    if ((own >> j) & 1u) {
-                        const int64_t p =
-                            (int64_t)(oi + r0 + j / 2) * f.nj + gj0 + (j & 1);
-                        if (f.lat[l].activated[p]) lat_act |= 1u << (l * 8 + j);
-                    }
-            }
-
-        // ---- sub-steps ----
-        for (int s = 0; s < f.ksteps; ++s) {
-            const int64_t n = f.n0 + s;
-            float(*cur)[kBoxF] = (s & 1) ? S.u1 : G.u;
-            float(*nxt)[kBoxF] = (s & 1) ? G.u : S.u1;
-
-            if ((f.stim_on >> s) & 1u) {
-                for (int i = 0; i < f.n_stims; ++i) {
-                    const FStim &F = f.stims[i];
-                    if (!((F.on >> s) & 1u)) continue;
-#pragma unroll
-                    for (int j = 0; j < 2 * R; ++j) {
-                        if (!((myo_bits >> j) & 1u)) continue;
-                        const int lr = r0 + j / 2, gi = oi + lr, gj = gj0 + (j & 1);
-                        if (gj < F.lo1 || gj >= F.hi1) continue;
-                        if (gi < F.lo0 || gi >= F.hi0) continue;
-                        if (F.mask && !F.mask[(int64_t)gi * f.nj + gj]) continue;
-                        float x = cur[lr + 1][cx + (j & 1)];
-                        if (F.kind == FW_STIM_VOLTAGE) {
-                            x = F.value;
-                        } else {
-                            x = x + F.value;
-                            if (F.has_umax && x > F.u_max) x = F.u_max;
-                        }
-                        cur[lr + 1][cx + (j & 1)] = x;
-                    }
-                }
-                __syncthreads();
-            }
-
-            // window rows r0 - 1 .. r0 + R: a = column c0 - 1, (m0, m1) =
-            // columns c0, c0 + 1, b = column c0 + 2
-            float a[R + 2], m0[R + 2], m1[R + 2], b[R + 2];
-#pragma unroll
-            for (int i = 0; i < R + 2; ++i) {
-                a[i] = cur[r0 + i][cx - 1];
-                const float2 mm = *reinterpret_cast<const float2 *>(&cur[r0 + i][cx]);
-                m0[i] = mm.x;
-                m1[i] = mm.y;
-                b[i] = cur[r0 + i][cx + 2];
-            }
-
-            if (own) {
-                float mx = fmaxf(fmaxf(m0[1], m1[1]), fmaxf(m0[2], m1[2]));
-#pragma unroll
-                for (int aa = 0; aa < kMaxFusedAt; ++aa) {
-                    if (aa >= f.n_at || !((f.at[aa].on >> s) & 1u)) continue;
-                    // (fmaxf skips NaN nodes, which never cross)
-                    if (!(mx > f.at[aa].thr)) continue;
-                    const float thr = f.at[aa].thr;
-                    uint32_t hit = (m0[1] > thr ? 1u : 0u) | (m1[1] > thr ? 2u : 0u) |
-                                   (m0[2] > thr ? 4u : 0u) | (m1[2] > thr ? 8u : 0u);
-                    hit &= own & ~(at_done >> (aa * 8));
-                    if (hit) {
-#pragma unroll
-                        for (int j = 0; j < 2 * R; ++j) {
-                            if (!((hit >> j) & 1u)) continue;
-                            // first crossing: unsigned minimum, "never" = -1
-                            // (activation_time_2d_tracker.py:61-63)
-                            const int64_t p =
-                                (int64_t)(oi + r0 + j / 2) * f.nj + gj0 + (j & 1);
-                            atomicMin(reinterpret_cast<unsigned *>(f.at[aa].act) + p,
-                                      (unsigned)n);
-                        }
-                        at_done |= hit << (aa * 8);
-                    }
-                }
-#pragma unroll
-                for (int l = 0; l < kMaxFusedLat; ++l) {
-                    if (l >= f.n_lat || !((f.lat[l].on >> s) & 1u)) continue;
-                    // (local_activation_time_2d_tracker.py:71-89)
-                    const float thr = f.lat[l].thr;
-                    const uint32_t ge = (m0[1] >= thr ? 1u : 0u) |
-                                        (m1[1] >= thr ? 2u : 0u) |
-                                        (m0[2] >= thr ? 4u : 0u) |
-                                        (m1[2] >= thr ? 8u : 0u);
-                    const uint32_t lt = (m0[1] < thr ? 1u : 0u) |
-                                        (m1[1] < thr ? 2u : 0u) |
-                                        (m0[2] < thr ? 4u : 0u) |
-                                        (m1[2] < thr ? 8u : 0u);
-                    const uint32_t was = (lat_act >> (l * 8)) & 0xffu;
-                    const uint32_t rise = ge & own & ~was;
-                    const uint32_t fall = lt & own & was;
-                    lat_act ^= (rise | fall) << (l * 8);
-                    if (rise) {
-#pragma unroll
-                        for (int j = 0; j < 2 * R; ++j)
-                            if ((rise >> j) & 1u)
-                                lat_record(f.lat[l],
-                                           (int64_t)(oi + r0 + j / 2) * f.nj + gj0 +
-                                               (j & 1),
-                                           f.n, n, f.status);
-                    }
-                }
-            }
-
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const int lr = r0 + r;
-                const float4 wa0 = G.wa[lr][cp], wa1 = G.wa[lr][HW + cp];
-                float4 wb0 = wa0, wb1 = wa1;
-                if constexpr (NWO == 8) {
-                    wb0 = G.wb[lr][cp];
-                    wb1 = G.wb[lr][HW + cp];
-                }
-                const float un0 = stencil_fma<ST>(wcen[2 * r], m0[r + 1], wa0, wb0,
-                                                  a[r], m0[r], m1[r], a[r + 1],
-                                                  m1[r + 1], a[r + 2], m0[r + 2],
-                                                  m1[r + 2]);
-                const float un1 = stencil_fma<ST>(wcen[2 * r + 1], m1[r + 1], wa1, wb1,
-                                                  m0[r], m1[r], b[r], m0[r + 1],
-                                                  b[r + 1], m0[r + 2], m1[r + 2],
-                                                  b[r + 2]);
-                const float uu0 =
-                    M::template update<float>(m0[r + 1], un0, st[2 * r], P, dt);
-                const float uu1 =
-                    M::template update<float>(m1[r + 1], un1, st[2 * r + 1], P, dt);
-                float2 o;
-                o.x = ((upd >> (2 * r)) & 1u) ? uu0 : m0[r + 1];
-                o.y = ((upd >> (2 * r + 1)) & 1u) ? uu1 : m1[r + 1];
-                *reinterpret_cast<float2 *>(&nxt[lr + 1][cx]) = o;
-            }
-            // probes: u after the stimuli, the state after the update
-            if (probe_mine && ((f.probe_on >> s) & 1u)) {
-#pragma unroll
-                for (int j = 0; j < 2 * R; ++j)
-                    if ((probe_mine >> j) & 1u)
-                        write_probes<M>(f, S.probe_list, S.probe_count, r0 + j / 2,
-                                        c0 + (j & 1), s,
-                                        (j & 1) ? m1[j / 2 + 1] : m0[j / 2 + 1], st[j],
-                                        ((myo_bits >> j) & 1u) != 0,
-                                        (int64_t)(oi + r0 + j / 2) * f.nj + gj0 +
-                                            (j & 1));
-            }
-            __syncthreads();
-        }
-
-        // ---- write the interior back ----
-        float(*fin)[kBoxF] = (f.ksteps & 1) ? S.u1 : G.u;
-        bool nonfinite = false;
-#pragma unroll
-        for (int j = 0; j < 2 * R; ++j) {
-            if (!((own >> j) & 1u)) continue;
-            const int lr = r0 + j / 2;
-            const int64_t p = (int64_t)(oi + lr) * f.nj + gj0 + (j & 1);
-            if ((myo_bits >> j) & 1u) {
-                const float uo = fin[lr + 1][cx + (j & 1)];
-                f.u_out[p] = uo;
-                nonfinite |= !isfinite(uo);
-                M::template store<float>(f.state_out, p, st[j]);
-            }
-#pragma unroll
-            for (int l = 0; l < kMaxFusedLat; ++l)
-                if (l < f.n_lat)
-                    f.lat[l].activated[p] = (lat_act >> (l * 8 + j)) & 1u;
-        }
-        if (nonfinite && f.status) atomicOr(f.status, FW_DEV_NONFINITE);
+        tma_tile2<M, ST, KMAX, LH, PACK>(f, G, S, oi, oj, own_c, ring_c, P);
         __syncthreads();
     }
 }
@@ -1069,14 +1147,17 @@ inline bool encode_weights(CUtensorMap *m, const void *base, int nwo, int64_t nj
 
 // The same packed weights viewed as (q, column pair, column parity, row):
 // a box of 32 pairs x 2 parities lands as [row][parity][pair] float4s.
+// With a row pitch (a multiple of 16 nodes, rows padded with zero weights)
+// the view spans the pitch: columns nj .. pitch - 1 read the padding.
 inline bool encode_weights_pairs(CUtensorMap *m, const void *base, int nwo,
-                                 int64_t nj, int64_t ni, int bh)
+                                 int64_t nj, int64_t ni, int bh, int64_t pitch = 0)
 {
     auto enc = tensor_map_encoder();
     if (!enc) return false;
-    cuuint64_t dims[4] = {(cuuint64_t)nwo, (cuuint64_t)(nj / 2), 2, (cuuint64_t)ni};
+    const int64_t w = pitch ? pitch : nj;
+    cuuint64_t dims[4] = {(cuuint64_t)nwo, (cuuint64_t)(w / 2), 2, (cuuint64_t)ni};
     cuuint64_t strides[3] = {(cuuint64_t)(2 * nwo * 4), (cuuint64_t)(nwo * 4),
-                             (cuuint64_t)(nj * nwo * 4)};
+                             (cuuint64_t)(w * nwo * 4)};
     cuuint32_t box[4] = {4, (cuuint32_t)(kTW / 2), 2, (cuuint32_t)bh};
     cuuint32_t es[4] = {1, 1, 1, 1};
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void *>(base), dims,
@@ -1125,9 +1206,11 @@ inline bool tma_fly_usable(const fw_step_args *a, int ns)
     return ok && tensor_map_encoder() != nullptr;
 }
 
-// PAIRS: the column-pair kernel k_fused_tma2 (R is then 2, fixed by it).
+// PAIRS: the column-pair kernel k_fused_tma2 (R is then 2, fixed by it),
+// PACK: its two-wide float32 form (fused_variant 6).
 // FLY: the weights formed on chip from the float32 fibers (fused_variant 5).
-template <class M, int ST, int KMAX, int LH, int R, bool PAIRS = false, bool FLY = false>
+template <class M, int ST, int KMAX, int LH, int R, bool PAIRS = false, bool FLY = false,
+          bool PACK = false>
 int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                      cudaStream_t stream)
 {
@@ -1138,7 +1221,7 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     static_assert(!(PAIRS && FLY), "weights on chip: strip kernel only");
     void (*kern)(const TmaK);
     if constexpr (PAIRS)
-        kern = k_fused_tma2<M, ST, KMAX, LH>;
+        kern = k_fused_tma2<M, ST, KMAX, LH, PACK>;
     else
         kern = k_fused_tma<M, ST, KMAX, LH, R, FLY>;
     FW_CUDA_CHECK(cudaFuncSetAttribute(
@@ -1241,7 +1324,9 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 //      4-node strips, two stages in shared memory;
 //   4: the TMA pipeline with 2 x 2 node blocks per thread (even K only);
 //   5: variant 3 with the AsymmetricStencil2D weights formed on chip from
-//      float32 fibers (fw_step_args.fibers_f32) instead of read from HBM.
+//      float32 fibers (fw_step_args.fibers_f32) instead of read from HBM;
+//   6: variant 4 in two-wide float32 instructions (each node's bits those
+//      of variants 3 and 4; even K only).
 // KMAX (fused_k) in {2, 4, 8} time steps per launch (3 also for 3 and 5).
 template <class M, int ST>
 int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
@@ -1279,7 +1364,7 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
             return FW_ERR_UNSUPPORTED;
         }
     }
-    if ((v == 3 || v == 4) && !tma_usable(a, M::NS)) {
+    if ((v == 3 || v == 4 || v == 6) && !tma_usable(a, M::NS)) {
         set_error("fw_step (fused): the TMA kernels need packed weights, "
                   "16-byte aligned weights, potential, state and myocyte "
                   "arrays and nj %% 16 == 0");
@@ -1291,6 +1376,9 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     return launch_fused_tma<M, ST, KK, 32, 4>(a, n_begin, n_steps, stream)
 #define FW_TMA2_CASE(KK)                                                       \
     return launch_fused_tma<M, ST, KK, 32, 2, true>(a, n_begin, n_steps, stream)
+#define FW_PACK_CASE(KK)                                                       \
+    return launch_fused_tma<M, ST, KK, 32, 2, true, false, true>(a, n_begin,   \
+                                                                n_steps, stream)
     if (v == 1) {
         if (k == 2) FW_CP_CASE(2, 32, 2);
         if (k == 4) FW_CP_CASE(4, 32, 2);
@@ -1308,13 +1396,18 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         if (k == 2) FW_TMA2_CASE(2);
         if (k == 4) FW_TMA2_CASE(4);
         if (k == 8) FW_TMA2_CASE(8);
+    } else if (v == 6) {
+        if (k == 2) FW_PACK_CASE(2);
+        if (k == 4) FW_PACK_CASE(4);
+        if (k == 8) FW_PACK_CASE(8);
     }
 #undef FW_CP_CASE
 #undef FW_TMA_CASE
 #undef FW_TMA2_CASE
+#undef FW_PACK_CASE
     set_error("fw_step (fused): no kernel for fused_k=%d fused_variant=%d "
-              "(k in 2, 3, 4, 8; variant in 0..5, variant 4 with even k, "
-              "variant 5 for AsymmetricStencil2D)", k, a->fused_variant);
+              "(k in 2, 3, 4, 8; variant in 0..6, variants 4 and 6 with even "
+              "k, variant 5 for AsymmetricStencil2D)", k, a->fused_variant);
     return FW_ERR_UNSUPPORTED;
 }
 

@@ -27,6 +27,59 @@ struct Params {
     T v[N];
 };
 
+// float32 operations with a fixed rounding -- to nearest even, subnormal
+// inputs and results flushed to zero -- as inline PTX, so that neither FMA
+// contraction nor the translation unit's flags change them.  The pair forms
+// are Blackwell's two-wide f32x2 instructions (one issue for two lanes);
+// each lane is rounded exactly as the scalar operation, so an update written
+// once with f_* and once with f2_* gives the same bits per node.
+__device__ __forceinline__ float f_add(float a, float b)
+{
+    float d;
+    asm("add.rn.ftz.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+    return d;
+}
+__device__ __forceinline__ float f_mul(float a, float b)
+{
+    float d;
+    asm("mul.rn.ftz.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+    return d;
+}
+__device__ __forceinline__ float f_fma(float a, float b, float c)
+{
+    float d;
+    asm("fma.rn.ftz.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b)
+{
+    float2 d;
+    asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+        " add.rn.ftz.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b)
+{
+    float2 d;
+    asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+        " mul.rn.ftz.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c)
+{
+    float2 d;
+    asm("{\n .reg .b64 ra, rb, rc, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+        " mov.b64 rc, {%6, %7};\n fma.rn.ftz.f32x2 rd, ra, rb, rc;\n mov.b64 {%0, %1}, rd;\n}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+__device__ __forceinline__ float2 f2_dup(float x) { return make_float2(x, x); }
+
 // Precision-matched transcendental calls (float -> the float functions, so
 // that no float64 arithmetic sneaks into the float32 kernels).
 __device__ __forceinline__ float fw_tanh(float x) { return tanhf(x); }
@@ -102,6 +155,44 @@ struct ModelAP {
             x.v = v;
             return un + dt * ((-k) * u * (u - a) * (u - (T)1.) - u * v);
         }
+    }
+    // The float32 update of the fused and batched kernels: update<float>'s
+    // rearrangement with every rounding explicit (-dt (k cub + u v) for
+    // dt (-k cub - u v), the same value), and its two-node form, which
+    // gives each node the same bits.
+    __device__ static __forceinline__ float update_fused(float u, float un,
+                                                         St<float> &x,
+                                                         const Params<float, NP> &P,
+                                                         float dt)
+    {
+        const float a = P.v[0], k = P.v[1], eap = P.v[2], mu_1 = P.v[3],
+                    mu_2 = P.v[4];
+        float v = x.v;
+        const float ua1 = f_add(u, -(a + 1.f));
+        const float q = __fdividef(f_mul(mu_1, v), f_add(mu_2, u));
+        const float g = f_fma(f_mul(k, u), ua1, v);
+        v = f_fma(f_mul(-dt, f_add(eap, q)), g, v);
+        x.v = v;
+        const float cub = f_mul(f_fma(ua1, u, a), u);
+        return f_fma(-dt, f_fma(k, cub, f_mul(u, v)), un);
+    }
+    __device__ static __forceinline__ float2 update_pair(float2 u, float2 un,
+                                                         St<float> &x0, St<float> &x1,
+                                                         const Params<float, NP> &P,
+                                                         float dt)
+    {
+        const float a = P.v[0], k = P.v[1], eap = P.v[2], mu_1 = P.v[3],
+                    mu_2 = P.v[4];
+        float2 v = make_float2(x0.v, x1.v);
+        const float2 ua1 = f2_add(u, f2_dup(-(a + 1.f)));
+        const float2 num = f2_mul(f2_dup(mu_1), v), den = f2_add(f2_dup(mu_2), u);
+        const float2 q = make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+        const float2 g = f2_fma(f2_mul(f2_dup(k), u), ua1, v);
+        v = f2_fma(f2_mul(f2_dup(-dt), f2_add(f2_dup(eap), q)), g, v);
+        x0.v = v.x;
+        x1.v = v.y;
+        const float2 cub = f2_mul(f2_fma(ua1, u, f2_dup(a)), u);
+        return f2_fma(f2_dup(-dt), f2_fma(f2_dup(k), cub, f2_mul(u, v)), un);
     }
 };
 

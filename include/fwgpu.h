@@ -267,10 +267,13 @@ typedef struct fw_step_args {
                               CTAs, double-buffered 64x32 regions, 4 x 1
                               nodes per thread); 4 = the TMA pipeline with
                               2 x 2 nodes per thread (even fused_k).
-                              Variants 1-4 give bitwise the same results;
-                              5 = variant 3 with the AsymmetricStencil2D
-                              weights formed on chip from fibers_f32
-                              (within float32 rounding of the others)      */
+                              6 = variant 4 in two-wide float32
+                              instructions (f32x2, even fused_k).
+                              Variants 1-4 and 6 give bitwise the same
+                              results; 5 = variant 3 with the
+                              AsymmetricStencil2D weights formed on chip
+                              from fibers_f32 (within float32 rounding of
+                              the others)                                  */
     const void *weights_packed; /* FW_FORM_FUSED: off-centre float32 weights
                                    node-major, (N, 4) for ISO5 or (N, 8)
                                    for ANISO9, from fw_pack_weights; NULL
@@ -329,9 +332,12 @@ typedef struct fw_batch {
     int32_t n_tiles;     /* fused regions over all tissues                   */
     int32_t ksteps;      /* time steps per launch                            */
     int32_t grid;        /* persistent CTAs per launch                       */
-    int32_t kernel;      /* 1 = cp.async staging, 2 = TMA pipeline           */
+    int32_t kernel;      /* 1 = cp.async staging, 2 = TMA pipeline, 3 = TMA
+                            pipeline with 2 x 2 nodes per thread in two-wide
+                            float32 instructions (every tissue planned with
+                            fused_variant 6); 2 and 3 give the same bits   */
     int32_t reserved;
-    int32_t group_end[6]; /* kernel 2: end of each (model, stencil) group in
+    int32_t group_end[6]; /* kernels 2, 3: end of each (model, stencil) group in
                              the tile list -- AP/ISO5, AP/ANISO9, MS/ISO5,
                              MS/ANISO9, FK/ISO5, FK/ANISO9 -- each advanced by
                              its own kernel launch                          */

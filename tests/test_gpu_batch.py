@@ -82,7 +82,7 @@ def _same(a, b, where):
         assert np.array_equal(np.asarray(a), np.asarray(b)), where
 
 
-@pytest.mark.parametrize("kernel", ["tma", "cp.async"])
+@pytest.mark.parametrize("kernel", ["tma", "pairs", "cp.async"])
 def test_batch_equals_single_fused(gc, kernel):
     import finitewave_gb300 as fg
     cs = _batch_cases()
@@ -98,7 +98,7 @@ def test_batch_equals_single_fused(gc, kernel):
     batch.run()
     torch.cuda.synchronize()
     assert fg._ffi.load().fw_launch_count() > launches0
-    assert batch._batch.kernel == (2 if kernel == "tma" else 1)
+    assert batch._batch.kernel == {"tma": 2, "pairs": 3, "cp.async": 1}[kernel]
     for i, ((m, objs), ref) in enumerate(zip(built, single)):
         got = _outputs(m, objs)
         assert got["step"] == ref["step"] and got["t"] == ref["t"], i

@@ -231,14 +231,16 @@ def _fused_case(name, aniso, nj):
 @pytest.mark.parametrize("name", ["ap", "ms", "fk"])
 @pytest.mark.parametrize("aniso", [False, True])
 @pytest.mark.parametrize("k", [2, 4, 8])
-@pytest.mark.parametrize("variant,nj", [(1, 140), (2, 140), (3, 144), (4, 144)])
+@pytest.mark.parametrize("variant,nj", [(1, 140), (2, 140), (3, 144), (4, 144),
+                                        (6, 144)])
 def test_fused_matches_plain_f32(gc, name, aniso, k, variant, nj):
     """Fused temporal blocking vs the plain FP32 form on a grid of several
     tiles (150 x nj), S1 plus a cross-field S2, 777 steps (an odd count, not
     a multiple of k): same activation steps within one step, fields within
     a tolerance that covers FMA-vs-no-FMA rounding.  Variants 1 and 2 stage
     with cp.async; variants 3 and 4 are the persistent TMA pipeline (rows of
-    a multiple of 16 nodes) with 4 x 1 and 2 x 2 nodes per thread."""
+    a multiple of 16 nodes) with 4 x 1 and 2 x 2 nodes per thread, variant 6
+    the 2 x 2 kernel in two-wide float32 instructions."""
     case = _fused_case(name, aniso, nj)
     ref = gc.run(case, npfloat="float32", form="plain")
     r = gc.run(case, npfloat="float32", form="fused", fused_k=k,
@@ -255,14 +257,15 @@ def test_fused_matches_plain_f32(gc, name, aniso, k, variant, nj):
 @pytest.mark.parametrize("name", ["ap", "ms", "fk"])
 @pytest.mark.parametrize("aniso", [False, True])
 @pytest.mark.parametrize("k", [2, 4, 8])
-@pytest.mark.parametrize("variant", [1, 2, 4])
+@pytest.mark.parametrize("variant", [1, 2, 4, 6])
 def test_fused_variants_bitwise_equal(gc, name, aniso, k, variant):
     """Every fused kernel (cp.async 64 x 32 and 64 x 64 regions, TMA with
-    4 x 1 strips or 2 x 2 blocks) forms each node's diffusion sum as the same
-    FMA chain over the stored weights and runs the same ionic update, so
-    fields, state, activation times and probe traces agree bitwise with the
-    TMA strip kernel (variant 3).  Local activation flags: read from global
-    memory by variants 1, 2 and 4, staged with the region by variant 3."""
+    4 x 1 strips or 2 x 2 blocks, the 2 x 2 kernel in two-wide float32
+    instructions) forms each node's diffusion sum as the same FMA chain over
+    the stored weights and runs the same ionic update, so fields, state,
+    activation times and probe traces agree bitwise with the TMA strip
+    kernel (variant 3).  Local activation flags: read from global memory by
+    variants 1 and 2, staged with the region by variants 3, 4 and 6."""
     case = _fused_case(name, aniso, 144)
     r3 = gc.run(case, npfloat="float32", form="fused", fused_k=k,
                 fused_variant=3)
@@ -443,7 +446,7 @@ def test_fused_bits_do_not_depend_on_tile_order(gc):
         return m.u, m.v, objs[0].output
 
     runs = {}
-    for v in (1, 3, 4):
+    for v in (1, 3, 4, 6):
         m, objs = gc.build(case, npfloat="float32", form="fused", fused_k=4,
                            fused_variant=v)
         m.run()
@@ -454,7 +457,7 @@ def test_fused_bits_do_not_depend_on_tile_order(gc):
     # the same 1200 steps as two device segments, an odd one first
     assert m._run_segment(555) + m._run_segment(645) == 1200
     runs["v3_split"] = out(m, objs)
-    for kernel in ("tma", "cp.async"):
+    for kernel in ("tma", "pairs", "cp.async"):
         m, objs = gc.build(case, npfloat="float32")
         fg.TissueBatch([m], kernel=kernel, chunk=301).run()
         runs["batch_" + kernel] = out(m, objs)

@@ -368,9 +368,9 @@ def test_autotune_cache_logic(tmp_path, monkeypatch):
     assert autotune.choose(m) == (3, 4) and len(calls) == 2       # re-tuned
     assert json.loads(path.read_text())[autotune.key(m)]["k"] == 4
     autotune._memo.clear()
-    # TMA candidates (variants 3 and 4) come first, cp.async ones after
-    assert {v for v, _ in autotune._TMA} == {3, 4}
-    assert all(k % 2 == 0 for v, k in autotune._TMA if v == 4)
+    # TMA candidates (variants 3, 4 and 6) come first, cp.async ones after
+    assert {v for v, _ in autotune._TMA} == {3, 4, 6}
+    assert all(k % 2 == 0 for v, k in autotune._TMA if v in (4, 6))
 
 
 def _fmaf(a, b, c):
