@@ -105,6 +105,12 @@ def workload_inputs(n=N, seed=SEED, sigma=64.0):
 # batched workload: 256 independent 2D tissues (see batched_specs)
 N_TISSUES = 256
 BCL = {"ap": 60.0, "ms": 1000.0, "fk": 1000.0}
+# each model's restitution range [ERP, BCL]: ERP is the shortest S1-S2
+# coupling interval after 8 S1 beats at the BCL whose S2 still propagates,
+# measured once in float64 by tests/golden/make_restitution.py (written to
+# tests/golden/restitution.json, which a CPU test keeps equal to these)
+RESTITUTION = {"ap": (25.710938, 60.0), "ms": (317.1875, 1000.0),
+               "fk": (165.039062, 1000.0)}
 B_ALG_BATCH = {("ap", "iso5"): 17, ("ap", "aniso9"): 25,
                ("ms", "iso5"): 17, ("ms", "aniso9"): 25,
                ("fk", "iso5"): 25, ("fk", "aniso9"): 33}
@@ -116,8 +122,9 @@ def batched_specs(n_tissues=N_TISSUES, seed=SEED):
     isotropic or 9-point anisotropic (smooth random fibers, sigma = side/64
     nodes), diffuse fibrosis with p uniform in [0, 0.3]; S1-S2 protocol: 8
     S1 beats from the left edge at the model's basic cycle length, then an
-    S2 on the lower-left quadrant after a coupling interval uniform in
-    [0.5, 1] x BCL.  Seeded; all randomness from default_rng(seed)."""
+    S2 on the lower-left quadrant after a coupling interval uniform over the
+    model's measured restitution range (RESTITUTION).  Seeded; all
+    randomness from default_rng(seed)."""
     rng = np.random.default_rng(seed)
     specs = []
     for i in range(n_tissues):
@@ -125,7 +132,8 @@ def batched_specs(n_tissues=N_TISSUES, seed=SEED):
         model = ("ap", "ms", "fk")[int(rng.integers(3))]
         aniso = bool(rng.integers(2))
         p = float(rng.uniform(0.0, 0.3))
-        ci = float(rng.uniform(0.5, 1.0)) * BCL[model]
+        lo, hi = RESTITUTION[model]
+        ci = float(rng.uniform(lo, hi))
         specs.append(dict(side=side, model=model, aniso=aniso, p=p, ci=ci,
                           seed=int(rng.integers(1 << 31))))
     return specs

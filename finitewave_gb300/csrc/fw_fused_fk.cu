@@ -1,6 +1,6 @@
 // fw_fused_fk.cu -- instantiations of the fused FP32 kernel for ModelFK
 // (one translation unit per model so that they compile in parallel).
-#include "fw_fused_tma.cuh"
+#include "fw_fused_march.cuh"
 
 namespace fw {
 

@@ -1316,6 +1316,11 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
     return FW_OK;
 }
 
+// the row-marching wavefront (fw_fused_march.cuh, fused variant 7)
+template <class M, int ST, int KMAX>
+int launch_fused_march(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
+                       cudaStream_t stream);
+
 // Kernel choice (fw_step_args.fused_variant):
 //   0: automatic -- the TMA pipeline when it can run, else 1;
 //   1: cp.async staging, 64 x 32 regions, 256 threads, two CTAs per SM;
@@ -1326,7 +1331,9 @@ int launch_fused_tma(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
 //   5: variant 3 with the AsymmetricStencil2D weights formed on chip from
 //      float32 fibers (fw_step_args.fibers_f32) instead of read from HBM;
 //   6: variant 4 in two-wide float32 instructions (each node's bits those
-//      of variants 3 and 4; even K only).
+//      of variants 3 and 4; even K only);
+//   7: the row-marching wavefront: 64-column strips marched down in 8-row
+//      blocks with the K time levels in flight (K <= 4, no probes).
 // KMAX (fused_k) in {2, 4, 8} time steps per launch (3 also for 3 and 5).
 template <class M, int ST>
 int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
@@ -1364,7 +1371,7 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
             return FW_ERR_UNSUPPORTED;
         }
     }
-    if ((v == 3 || v == 4 || v == 6) && !tma_usable(a, M::NS)) {
+    if ((v == 3 || v == 4 || v == 6 || v == 7) && !tma_usable(a, M::NS)) {
         set_error("fw_step (fused): the TMA kernels need packed weights, "
                   "16-byte aligned weights, potential, state and myocyte "
                   "arrays and nj %% 16 == 0");
@@ -1400,14 +1407,19 @@ int fused_dispatch(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
         if (k == 2) FW_PACK_CASE(2);
         if (k == 4) FW_PACK_CASE(4);
         if (k == 8) FW_PACK_CASE(8);
+    } else if (v == 7) {
+        if (k == 2) return launch_fused_march<M, ST, 2>(a, n_begin, n_steps, stream);
+        if (k == 3) return launch_fused_march<M, ST, 3>(a, n_begin, n_steps, stream);
+        if (k == 4) return launch_fused_march<M, ST, 4>(a, n_begin, n_steps, stream);
     }
 #undef FW_CP_CASE
 #undef FW_TMA_CASE
 #undef FW_TMA2_CASE
 #undef FW_PACK_CASE
     set_error("fw_step (fused): no kernel for fused_k=%d fused_variant=%d "
-              "(k in 2, 3, 4, 8; variant in 0..6, variants 4 and 6 with even "
-              "k, variant 5 for AsymmetricStencil2D)", k, a->fused_variant);
+              "(k in 2, 3, 4, 8; variant in 0..7, variants 4 and 6 with even "
+              "k, variant 5 for AsymmetricStencil2D, variant 7 with k <= 4)",
+              k, a->fused_variant);
     return FW_ERR_UNSUPPORTED;
 }
 

@@ -268,8 +268,11 @@ typedef struct fw_step_args {
                               nodes per thread); 4 = the TMA pipeline with
                               2 x 2 nodes per thread (even fused_k).
                               6 = variant 4 in two-wide float32
-                              instructions (f32x2, even fused_k).
-                              Variants 1-4 and 6 give bitwise the same
+                              instructions (f32x2, even fused_k);
+                              7 = 64-column strips marched down the rows
+                              with the fused_k <= 4 time levels in flight
+                              (no probe trackers).
+                              Variants 1-4, 6 and 7 give bitwise the same
                               results; 5 = variant 3 with the
                               AsymmetricStencil2D weights formed on chip
                               from fibers_f32 (within float32 rounding of

@@ -18,8 +18,9 @@ the 1-node boundary ring; S1 = voltage stimulus u = 1 on columns 1..5
 (``StimVoltageCoord2D``, ``stim_voltage_coord_2d.py:49-67``) at t = b BCL,
 b = 0..7; S2 = the same stimulus at t = 7 BCL + CI.  The S2 propagates when
 the probe node (row 2, column 100) crosses u >= 0.5 (the local activation
-tracker's test, ``local_activation_time_2d_tracker.py:82-83``) after the S2
-and within three of the first beat's travel times to it.  ERP is bisected
+tracker's test, ``local_activation_time_2d_tracker.py:82-83``) a ninth time
+-- once per S1 beat and once for the S2 -- within three of the first beat's
+travel times to it after the S2.  ERP is bisected
 over CI in [0.05, 1] BCL to 1/256 of that interval; the recorded ERP is the
 shortest tested interval that propagated.
 
@@ -48,6 +49,7 @@ THRESHOLD = 0.5
 def _setup(model):
     sys.path.insert(0, ROOT)
     from oracle import oracle as O
+    O.set_threads(1)   # a 348-myocyte strand: one thread per process
     spec = O.MODELS[model]
     mesh = np.zeros(SHAPE, dtype=np.int8)
     mesh[1:-1, 1:-1] = 1
@@ -103,7 +105,7 @@ def measure(model):
     def propagates(ci):
         t_s2 = 7 * bcl + ci
         c = _pace(model, ci, stop_after=t_s2 + 3 * travel)
-        return any(x > t_s2 for x in c)
+        return len(c) >= 9
 
     lo, hi = 0.05 * bcl, bcl
     assert propagates(hi), f"{model}: an S2 one BCL after the last S1 fails"
@@ -124,8 +126,8 @@ def main():
         res = dict(zip(models, pool.map(measure, models)))
     out = {"protocol": "8 S1 at BCL + S2 at CI on columns 1..5 of a 3 x 116 "
                        "strand (dt 0.01, dr 0.25, iso5, float64 oracle); "
-                       "propagation: probe (2, 100) crosses u >= 0.5 after "
-                       "the S2; ERP bisected over [0.05, 1] BCL",
+                       "propagation: probe (2, 100) crosses u >= 0.5 a "
+                       "ninth time; ERP bisected over [0.05, 1] BCL",
            "models": {m: {k: round(v, 6) if isinstance(v, float) else v
                           for k, v in r.items()} for m, r in res.items()}}
     with open(os.path.join(HERE, "restitution.json"), "w") as f:

@@ -282,6 +282,44 @@ def test_fused_variants_bitwise_equal(gc, name, aniso, k, variant):
 
 
 @pytest.mark.parametrize("name", ["ap", "ms", "fk"])
+@pytest.mark.parametrize("aniso", [False, True])
+@pytest.mark.parametrize("k", [2, 3, 4])
+def test_fused_march_bitwise_equal(gc, name, aniso, k):
+    """Variant 7 marches 64-column strips down the rows with the K time
+    levels in flight (no halo rows, state and tracker flags handed from
+    level to level in registers, the levels' rows in shared-memory rings):
+    every node's arithmetic is the tile kernels', so fields, state,
+    activation times and local activation times are bitwise those of the
+    TMA strip kernel (variant 3).  The case without its probe tracker
+    (variant 7 takes none)."""
+    case = _fused_case(name, aniso, 144)
+    case["trackers"] = [t for t in case["trackers"] if t["kind"] != "probe"]
+    r3 = gc.run(case, npfloat="float32", form="fused", fused_k=k,
+                fused_variant=3)
+    r7 = gc.run(case, npfloat="float32", form="fused", fused_k=k,
+                fused_variant=7)
+    assert int(r7["model"]._status.item()) == 0
+    assert r7["step"] == r3["step"] == 777
+    for v in cases.MODEL_VARS[name]:
+        assert np.array_equal(r7[v], r3[v]), v
+    assert np.array_equal(r7["trackers"][0], r3["trackers"][0])
+    lat3, lat7 = r3["trackers"][1], r7["trackers"][1]
+    assert lat3.shape == lat7.shape and lat3.shape[0] >= 1
+    assert np.array_equal(lat7, lat3, equal_nan=True)
+
+
+def test_fused_march_rejects_probes(gc):
+    """Variant 7 takes no probe trackers: asking for it with one raises
+    (the automatic choice never picks it then)."""
+    import finitewave_gb300 as fg
+    case = _fused_case("ap", True, 144)
+    m, _ = gc.build(case, npfloat="float32", form="fused", fused_k=4,
+                    fused_variant=7)
+    with pytest.raises(fg._ffi.FwError, match="probe"):
+        m.run()
+
+
+@pytest.mark.parametrize("name", ["ap", "ms", "fk"])
 @pytest.mark.parametrize("k", [2, 3, 4, 8])
 def test_fused_weights_on_chip(gc, name, k):
     """Variant 5 forms each region's AsymmetricStencil2D weights on chip in
@@ -446,7 +484,7 @@ def test_fused_bits_do_not_depend_on_tile_order(gc):
         return m.u, m.v, objs[0].output
 
     runs = {}
-    for v in (1, 3, 4, 6):
+    for v in (1, 3, 4, 6, 7):
         m, objs = gc.build(case, npfloat="float32", form="fused", fused_k=4,
                            fused_variant=v)
         m.run()

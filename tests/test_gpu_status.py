@@ -46,7 +46,7 @@ def _case():
                 trackers=[dict(kind="at", threshold=0.5)])
 
 
-@pytest.mark.parametrize("variant", [3, 4, 6])
+@pytest.mark.parametrize("variant", [3, 4, 6, 7])
 def test_forced_timeout_raises(gc, variant):
     from finitewave_gb300 import _ffi
     case = _case()

@@ -368,9 +368,9 @@ def test_autotune_cache_logic(tmp_path, monkeypatch):
     assert autotune.choose(m) == (3, 4) and len(calls) == 2       # re-tuned
     assert json.loads(path.read_text())[autotune.key(m)]["k"] == 4
     autotune._memo.clear()
-    # TMA candidates (variants 3, 4 and 6) come first, cp.async ones after
-    assert {v for v, _ in autotune._TMA} == {3, 4, 6}
-    assert all(k % 2 == 0 for v, k in autotune._TMA if v in (4, 6))
+    # TMA candidates (variants 3 and 4) come first, cp.async ones after
+    assert {v for v, _ in autotune._TMA} == {3, 4}
+    assert all(k % 2 == 0 for v, k in autotune._TMA if v == 4)
 
 
 def _fmaf(a, b, c):
@@ -596,3 +596,25 @@ def test_plugin_classification_and_host_steps():
     m.step, m.t = 35, 0.35
     assert m._steps_before_host(200, [], [tr]) == 0
     assert m._steps_before_host(200, [], [EveryStep()]) == 0
+
+
+def test_batched_restitution_ranges_match_measurement():
+    """The batched configuration draws each tissue's S1-S2 coupling interval
+    from its model's restitution range; the ranges in bench.py are the ones
+    tests/golden/make_restitution.py measured with the float64 oracle."""
+    import importlib.util
+    import json
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location(
+        "bench_for_test", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    with open(os.path.join(root, "tests", "golden", "restitution.json")) as f:
+        meas = json.load(f)["models"]
+    for m, (lo, hi) in bench.RESTITUTION.items():
+        assert hi == meas[m]["bcl"] == bench.BCL[m]
+        assert lo == meas[m]["erp"] and 0 < lo < hi
+    specs = bench.batched_specs(64)
+    for s in specs:
+        lo, hi = bench.RESTITUTION[s["model"]]
+        assert lo <= s["ci"] <= hi
