@@ -25,7 +25,6 @@ FW_DEV_TIP_OVERFLOW = 16
 FW_DEV_NONFINITE = 32
 
 FW_DEBUG_FORCE_TIMEOUT = 1
-FW_DEBUG_NO_PREFETCH = 2
 
 MODEL_AP, MODEL_MS, MODEL_FK, MODEL_TP06, MODEL_CRN = 1, 2, 3, 4, 5
 MODEL_BK, MODEL_BO, MODEL_LR91 = 6, 7, 8

@@ -16,8 +16,6 @@
 //   the caller's buffers then swap roles.
 #pragma once
 
-#include <type_traits>
-
 #include "fw_internal.cuh"
 #include "fw_models.cuh"
 
@@ -168,116 +166,6 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<M, T>::value))
         k.un[p] = un;
         if (!isfinite(un) && k.status) atomicOr(k.status, FW_DEV_NONFINITE);
     }
-}
-
-// ---- k_step_pipe: the float32 step of the detailed models ------------------------
-//
-// The detailed models (TP06, Courtemanche, Luo-Rudy 1991) read ~20 state
-// arrays per node and step; k_step's loads of one node's state sit between
-// it and its update, and at the occupancy their register needs allow the
-// warps wait on them (long-scoreboard stalls).  Here each thread prefetches
-// the state of its next myocyte into shared memory with cp.async (4- or
-// 8-byte copies, the concentration pairs as 8 bytes) while it updates the
-// current one, two stages per thread; the arithmetic and the operation
-// order are k_step's, so the results are the same bits.  A thread reads back
-// only its own copies (cp.async.wait_group), so no barrier is needed.
-
-// Byte layout of one stage: variable v holds kThreads elements of 8 bytes
-// (an ion-concentration pair) or 4 bytes, one per thread.
-template <class M>
-struct PipeLayout {
-    static constexpr int esize(int v) { return M::is_conc(v) ? 8 : 4; }
-    static constexpr int offset(int v)
-    {
-        int o = 0;
-        for (int i = 0; i < v; ++i) o += esize(i) * kThreads;
-        return o;
-    }
-    static constexpr int stage_bytes() { return offset(M::NS); }
-};
-
-template <class M, class = void>
-struct HasConcLayout : std::false_type {};
-template <class M>
-struct HasConcLayout<M, std::void_t<decltype(M::is_conc(0))>> : std::true_type {};
-
-__device__ __forceinline__ void cp_async_bytes(void *smem, const void *gmem, int bytes)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    if (bytes == 8)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem)
-                     : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem)
-                     : "memory");
-}
-
-template <class M>
-__device__ __forceinline__ void pipe_issue(void *const *state, unsigned char *stage,
-                                           int64_t p)
-{
-    using L = PipeLayout<M>;
-#pragma unroll
-    for (int v = 0; v < M::NS; ++v) {
-        const int es = L::esize(v);
-        cp_async_bytes(stage + L::offset(v) + threadIdx.x * es,
-                       (const unsigned char *)state[v] + p * es, es);
-    }
-}
-
-template <class M, int ST>
-__global__ void __launch_bounds__(kThreads, (MinBlocks<M, float>::value))
-    k_step_pipe(StepK<float> k)
-{
-    using L = PipeLayout<M>;
-    extern __shared__ __align__(16) unsigned char pipe_smem[];
-    const Params<float, M::NP> P = load_params<float, M::NP>(k.params);
-    const float dt = k.dt;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    bool myo_p = p < k.n && k.myo[p];
-    if (myo_p) pipe_issue<M>(k.state, pipe_smem, p);
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-    int64_t pn = p + stride;
-    bool myo_n = pn < k.n && k.myo[pn];
-    for (int j = 0; p < k.n; ++j) {
-        const int sg = j & 1;
-        const int64_t pnn = pn + stride;
-        // the flag of the node after next, read one iteration before it is
-        // needed
-        const bool myo_nn = pnn < k.n && k.myo[pnn];
-        if (myo_n) pipe_issue<M>(k.state, pipe_smem + (sg ^ 1) * L::stage_bytes(), pn);
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        const float uc = k.u[p];
-        if (k.n_at | k.n_lat) track(k, p, uc);
-        if (myo_p) {
-            float un;
-            if constexpr (ST == FW_STENCIL_ANISO19_XY) {
-                if (k.wrow)
-                    un = diffuse_row_xy<float>(k.u, k.wrow + (int64_t)k.widx[p] * 12, p,
-                                               k.si, k.sj);
-                else
-                    un = diffuse_node<ST, float>(k.u, k.w, p, k.n, k.si, k.sj);
-            } else {
-                un = diffuse_node<ST, float>(k.u, k.w, p, k.n, k.si, k.sj);
-            }
-            unsigned char *base = pipe_smem + sg * L::stage_bytes();
-            void *sptr[M::NS];
-#pragma unroll
-            for (int v = 0; v < M::NS; ++v) sptr[v] = base + L::offset(v);
-            auto st = M::template load<float>(sptr, threadIdx.x);
-            un = M::template update<float>(uc, un, st, P, dt);
-            M::template store<float>(k.state, p, st);
-            k.un[p] = un;
-            if (!isfinite(un) && k.status) atomicOr(k.status, FW_DEV_NONFINITE);
-        }
-        p = pn;
-        pn = pnn;
-        myo_p = myo_n;
-        myo_n = myo_nn;
-    }
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
 struct ProbeOne {
@@ -657,23 +545,8 @@ int run_plain(const fw_step_args *a, int64_t n_begin, int64_t n_steps,
                                         L.cross_steps, L.cross_count,
                                         L.capacity};
             }
-        bool launched = false;
-        if constexpr (std::is_same<T, float>::value && HasConcLayout<M>::value) {
-            if (!(a->debug_flags & FW_DEBUG_NO_PREFETCH)) {
-                constexpr int smem = 2 * PipeLayout<M>::stage_bytes();
-                if (s == 0)
-                    FW_CUDA_CHECK(cudaFuncSetAttribute(
-                        k_step_pipe<M, ST>,
-                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-                k_step_pipe<M, ST><<<blocks, kThreads, smem, stream>>>(k);
-                FW_CHECK_LAUNCH("k_step_pipe");
-                launched = true;
-            }
-        }
-        if (!launched) {
-            k_step<M, ST, T><<<blocks, kThreads, 0, stream>>>(k);
-            FW_CHECK_LAUNCH("k_step");
-        }
+        k_step<M, ST, T><<<blocks, kThreads, 0, stream>>>(k);
+        FW_CHECK_LAUNCH("k_step");
         pk.n = 0;
         for (int i = 0; i < a->n_probe; ++i) {
             const fw_probe_tracker &P = a->probe[i];

@@ -56,12 +56,8 @@ extern "C" {
  * FW_DEBUG_FORCE_TIMEOUT makes the TMA kernels treat their first pipeline
  * wait as timed out after the awaited copy has in fact arrived, so the
  * timeout exit (status bit, waits for copies in flight, early return) runs
- * on a healthy GPU.  The results of such a call are not defined.
- * FW_DEBUG_NO_PREFETCH runs the float32 plain step of the detailed models
- * (TP06, Courtemanche, Luo-Rudy 1991) without its shared-memory prefetch of
- * the next node's state (the same results; for comparing the two). */
+ * on a healthy GPU.  The results of such a call are not defined. */
 #define FW_DEBUG_FORCE_TIMEOUT 1
-#define FW_DEBUG_NO_PREFETCH 2
 
 /* ------------------------------------------------------------ enumerations */
 enum fw_model {

@@ -106,34 +106,6 @@ def test_detailed_f32_close_to_f64(gc, name, dim):
             assert d < F32_GATE_ATOL, (v, d)
 
 
-@pytest.mark.parametrize("dim", [2, 3])
-@pytest.mark.parametrize("name", ["tp06", "crn"])
-def test_detailed_f32_prefetch_bitwise(gc, name, dim):
-    """The float32 plain step of the detailed models prefetches each
-    thread's next myocyte's state into shared memory (cp.async) while it
-    updates the current one; the arithmetic is the step's own, so the
-    potential, every state variable and the probe traces are bitwise those
-    of the same step without the prefetch (FW_DEBUG_NO_PREFETCH)."""
-    from finitewave_gb300 import _ffi
-    case, _ = _case(name, dim)
-    m1, o1 = gc.build(case, npfloat="float32")
-    m1.run()
-    m2, o2 = gc.build(case, npfloat="float32")
-    m2._debug_flags = _ffi.FW_DEBUG_NO_PREFETCH
-    m2.run()
-    assert int(m1._status.item()) == 0 and int(m2._status.item()) == 0
-    assert m1.step == m2.step == 2000
-    for v in ["u"] + list(m1._state_names):
-        assert np.array_equal(getattr(m1, v), getattr(m2, v)), v
-    for t1, t2 in zip(o1, o2):
-        a, b = t1.output, t2.output
-        if isinstance(a, dict):
-            for v in a:
-                assert np.array_equal(np.asarray(a[v]), np.asarray(b[v])), v
-        else:
-            assert np.array_equal(np.asarray(a), np.asarray(b))
-
-
 @pytest.mark.parametrize("name", ["tp06", "crn"])
 def test_detailed_ionic_callable(gc, oracle, name):
     """run_ionic_kernel on random states in the physiological range equals
