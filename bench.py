@@ -176,6 +176,48 @@ def batched_tissue(fg, spec, npfloat):
     return model
 
 
+def batched_kernel_rate(args, fg, torch, reps, specs):
+    """The batched kernel alone on a subset of the batched configuration's
+    tissues: CUDA events over one fw_batch_run of `chunk` steps after a
+    warm-up through TissueBatch.run; myocyte-steps/s and the fraction of the
+    measured copy bandwidth on the subset's myocyte-weighted algorithmic
+    bytes."""
+    models = [batched_tissue(fg, s, "float32") for s in specs]
+    for m in models:
+        m.initialize()
+    myo = [int(m._myo_d.sum().item()) for m in models]
+    b_alg = sum(B_ALG_BATCH[(s["model"], "aniso9" if s["aniso"] else "iso5")]
+                * k for s, k in zip(specs, myo)) / sum(myo)
+    batch = fg.TissueBatch(models, kernel=args.batch_kernel)
+    for _ in range(max(1, args.warmup)):
+        for m in models:
+            m.t_max = m.t + args.chunk * m.dt
+        batch.run(initialize=False)
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fg._ffi.call("fw_batch_run", ctypes.byref(batch._batch),
+                     batch._scratch.data_ptr(), 0, args.chunk,
+                     stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    kms = sorted(times)[1]
+    value = reps.whole_job(sum(myo) * args.chunk, kms / 1e3)
+    peak, _ = peaks()
+    achieved = b_alg * value / reps.world / 1e9
+    del batch, models
+    torch.cuda.empty_cache()
+    return {"tissues": len(specs), "myocytes": sum(myo),
+            "kernel_value": value, "unit": UNIT,
+            "ms_per_time_step": kms / args.chunk,
+            "alg_bytes_per_myocyte_step": b_alg,
+            "frac": achieved / peak}
+
+
 def run_batched(args, fg, torch, reps):
     """Batched float32 throughput through TissueBatch.run (one persistent
     launch per 4 steps over all tissues), the same tissues in the float64
@@ -230,6 +272,9 @@ def run_batched(args, fg, torch, reps):
     batch_kernel = batch._batch.kernel
     del batch, models
     torch.cuda.empty_cache()
+    # the Aliev-Panfilov tissues of the same configuration on their own
+    ap_only = batched_kernel_rate(args, fg, torch, reps,
+                                  [s for s in specs if s["model"] == "ap"])
 
     # the same tissues, float64 plain form, one tissue after the other
     s64 = 20
@@ -264,6 +309,7 @@ def run_batched(args, fg, torch, reps):
             "fp64_plain": {"value": fp64_value, "unit": UNIT,
                            "time_steps": s64},
             "speedup_fp32_batched_over_fp64_plain": value / fp64_value,
+            "aliev_panfilov_only": ap_only,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "alg_bytes_per_myocyte_step": b_alg},
