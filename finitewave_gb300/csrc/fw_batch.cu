@@ -726,27 +726,27 @@ __global__ void __launch_bounds__(kTmaNT, 1)
     for (int it = 0;; ++it) {
         const int sg = it & 1;
         if (S.tile[sg] >= t_end) break;
-        if (tid == 0) {
-            // the other stage's readers finished at the barrier that closed
-            // the previous iteration
-            batch_issue<M, ST, PAIR>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1,
-                                     t_next,
-                               b_next, acquired);
-            t_next = next_tile();
-            b_next = t_next < t_end ? tiles[t_next] : none;
-        }
         const unsigned ph = (parity >> sg) & 1u;
         const bool arrived = fused::mbar_wait(&S.t.bar[sg], ph);
         parity ^= 1u << sg;
         if (__syncthreads_or(!arrived)) {
             if (tid == 0) {
-                // flag it, then wait (bounded) for the copies in flight
+                // flag it, then wait (bounded) for the copy in flight (the
+                // other stage's next tile is issued after this point)
                 if (tissues[0].f.status) atomicOr(tissues[0].f.status, FW_DEV_TIMEOUT);
                 if (!arrived) fused::mbar_wait(&S.t.bar[sg], ph);
-                if (S.tile[sg ^ 1] < t_end)
-                    fused::mbar_wait(&S.t.bar[sg ^ 1], (parity >> (sg ^ 1)) & 1u);
             }
             break;
+        }
+        if (tid == 0) {
+            // the next tile into the other stage, whose readers finished at
+            // the barrier that closed the previous iteration; issued here,
+            // after the wait, so that the other warps start this tile while
+            // thread 0 claims, acquires and issues
+            batch_issue<M, ST, PAIR>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1,
+                                     t_next, b_next, acquired);
+            t_next = next_tile();
+            b_next = t_next < t_end ? tiles[t_next] : none;
         }
         if (S.ok[sg]) {
             const fused::FusedK &f = S.f[sg];

@@ -658,20 +658,23 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
             nj_ -= tj;
             ++ni_;
         }
+        const unsigned ph = (parity >> sg) & 1u;
+        const bool arrived = mbar_wait(&S.bar[sg], ph);
+        parity ^= 1u << sg;
+        if (__syncthreads_or(!arrived || k.force_timeout)) {
+            // the next tile is issued after this point: only this stage's
+            // copy can be in flight
+            if (tid == 0) tma_abandon(k, S.bar, sg, ph, parity, arrived, k.tiles);
+            return;
+        }
         // prefetch the next tile into the other stage (its readers finished
-        // at the barrier that closed the previous iteration)
+        // at the barrier that closed the previous iteration); issued after
+        // the wait, so the other warps start this tile meanwhile
         const int next = tile + gridDim.x;
         if (tid == 0 && next < k.tiles) {
             fence_proxy_async();
             issue_tile<KMAX, LH, NS, NWO, false, FLY>(k, S.stage[sg ^ 1],
                                                       &S.bar[sg ^ 1], ni_, nj_);
-        }
-        const unsigned ph = (parity >> sg) & 1u;
-        const bool arrived = mbar_wait(&S.bar[sg], ph);
-        parity ^= 1u << sg;
-        if (__syncthreads_or(!arrived || k.force_timeout)) {
-            if (tid == 0) tma_abandon(k, S.bar, sg, ph, parity, arrived, next);
-            return;
         }
         const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
         bi = ni_;
