@@ -760,8 +760,14 @@ __global__ void __launch_bounds__(kTmaNT, 1)
                 fused::tma_tile<M, ST, KMAX, LH, kTmaR>(f, S.t.stage[sg], S.t,
                                                        S.oi[sg], S.oj[sg], own_c,
                                                        ring_c, P);
+        } else {
+            // a skipped tile has no sub-step barrier to publish thread 0's
+            // record of the next tile
+            __syncthreads();
         }
-        __syncthreads();
+        // no barrier here otherwise: the tile's sub-step barriers publish
+        // that record, and the next iteration's wait ends in one before any
+        // thread touches the ping-pong rows or this stage is refilled
     }
     if (tid == 0) {
         // this grid completes only after the group's kernel launched before

@@ -679,8 +679,9 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
         const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
         bi = ni_;
         bj = nj_;
+        // no barrier here: the next iteration's wait ends in one, before any
+        // thread touches the ping-pong rows or thread 0 refills this stage
         tma_tile<M, ST, KMAX, LH, R, FLY>(f, G, S, oi, oj, own_c, ring_c, P);
-        __syncthreads();
     }
 }
 
