@@ -732,11 +732,12 @@ def run_accuracy(args, fg, torch, reps):
                **_accuracy_pair(fg, accuracy_ap(fg, args.grid,
                                                 args.accuracy_tmax), None)),
            "cfg3_slab": dict(
-               grid=[128, 128, 16], t_max=450.0, units="mV; ms",
-               note="the 512x512x64 slab's generator at 128x128x16, S1 only "
+               grid=list(args.accuracy_slab), t_max=450.0, units="mV; ms",
+               note="the 512x512x64 slab's generator at %dx%dx%d, S1 only "
                     "(one beat); float64 of the full slab for one beat is "
-                    "~45 min of GPU time",
-               **_accuracy_pair(fg, accuracy_slab(fg), None)),
+                    "~45 min of GPU time" % tuple(args.accuracy_slab),
+               **_accuracy_pair(fg, accuracy_slab(
+                   fg, tuple(args.accuracy_slab)), None)),
            "tp06_2d_192": dict(
                units="mV; ms",
                **_accuracy_pair(fg, accuracy_tp06(fg), None)),
@@ -1194,6 +1195,9 @@ def main():
                     help="skip the serving trace")
     ap.add_argument("--accuracy-tmax", type=float, default=200.0,
                     help="model time of the 4096^2 float32-vs-float64 run")
+    ap.add_argument("--accuracy-slab", type=int, nargs=3,
+                    default=(128, 128, 16),
+                    help="grid of the TP06 slab float32-vs-float64 run")
     ap.add_argument("--lead-in", type=int, default=3200,
                     help="untimed time steps before the warm-up: the timed "
                          "window starts after the S2 (step 3100)")

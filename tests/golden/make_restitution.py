@@ -24,8 +24,9 @@ travel times to it after the S2.  ERP is bisected
 over CI in [0.05, 1] BCL to 1/256 of that interval; the recorded ERP is the
 shortest tested interval that propagated.
 
-Test infrastructure: run in the build container (CPU only), about a minute
-per model with one process per model.  ``bench.py`` carries the resulting
+Test infrastructure: run in the build container (CPU only), a few minutes
+per model with one process per model (the oracle's kernels on one thread
+each).  ``bench.py`` carries the resulting
 ranges as constants; ``tests/test_host.py`` checks that they match
 ``restitution.json``.
 """
