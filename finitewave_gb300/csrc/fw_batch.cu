@@ -540,7 +540,12 @@ struct BatchTmaSmem {
     int tile[2];           // the stage's tile index (>= the group's end: none)
     int oi[2], oj[2];      // its region origin
     int ok[2];             // 0 for a skipped tile
+    // tissues whose tensor maps thread 0 has acquired in this launch: a
+    // direct-mapped table (tissue % kAcq -> tissue, -1: none); the maps do
+    // not change during a launch, so one acquire per tissue and CTA suffices
+    int acq[64];
 };
+constexpr int kAcq = 64;
 
 // The batch's (model, stencil) groups, in the order the plan sorts tiles;
 // each group is advanced by its own instantiation of k_batch_tma.
@@ -606,13 +611,14 @@ __device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned b
 }
 
 // Thread 0: stage tile t (list entry bt) into stage sg.  The tensor maps
-// of a tissue are acquired once for a run of tiles of the same tissue.
+// of a tissue are acquired the first time the CTA meets the tissue in the
+// launch (S.acq; a table collision only repeats an acquire).
 // PAIR: the column-pair kernel, whose weight map is the column-pair view.
 template <class M, int ST, bool PAIR, class Sm>
 __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
                                          int32_t t_end, int32_t n_tissues,
                                          int32_t in_buf, Sm &S, int sg, int t,
-                                         BTileT bt, int &acquired)
+                                         BTileT bt)
 {
     constexpr int NWO = fused::Stencil2D<ST>::NWO;
     S.tile[sg] = t;
@@ -635,6 +641,7 @@ __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
     S.oj[sg] = bt.oj;
     const fused::TmaMaps &Mp = T.maps;
     const bool lat = (bt.key & kTileLat) != 0;
+    int &acquired = S.acq[bt.tissue & (kAcq - 1)];
     if (bt.tissue != acquired) {
         tensormap_acquire(&Mp.w);
         tensormap_acquire(&Mp.myo);
@@ -692,7 +699,7 @@ __global__ void __launch_bounds__(kTmaNT, 1)
     // one tissue, whose tensor maps are then acquired once per run), each
     // run's start taken from counters[0] one run ahead; the list entry of
     // tile i + 1 is read while tile i is computed
-    int run_cur = t_end, run_end = t_end, run_next = t_end, acquired = -1;
+    int run_cur = t_end, run_end = t_end, run_next = t_end;
     auto take_run = [&]() -> int {
         const int64_t s =
             (int64_t)t_begin + (int64_t)atomicAdd(&counters[0], 1u) * kRun;
@@ -714,11 +721,12 @@ __global__ void __launch_bounds__(kTmaNT, 1)
         fused::mbar_init(&S.t.bar[1], 1);
         fused::mbar_fence_init();
         S.ftissue[0] = S.ftissue[1] = -1;
+        for (int i = 0; i < kAcq; ++i) S.acq[i] = -1;
         run_next = take_run();
         const int t0 = next_tile();
         t_next = next_tile();
         batch_issue<M, ST, PAIR>(tissues, t_end, n_tissues, in_buf, S, 0, t0,
-                           t0 < t_end ? tiles[t0] : none, acquired);
+                           t0 < t_end ? tiles[t0] : none);
         if (t_next < t_end) b_next = tiles[t_next];
     }
     __syncthreads();
@@ -744,7 +752,7 @@ __global__ void __launch_bounds__(kTmaNT, 1)
             // after the wait, so that the other warps start this tile while
             // thread 0 claims, acquires and issues
             batch_issue<M, ST, PAIR>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1,
-                                     t_next, b_next, acquired);
+                                     t_next, b_next);
             t_next = next_tile();
             b_next = t_next < t_end ? tiles[t_next] : none;
         }
