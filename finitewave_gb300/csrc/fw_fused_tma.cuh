@@ -250,6 +250,45 @@ __device__ __forceinline__ void issue_tile(const TmaK &k, TmaStage<LH, NS, NWO> 
                                             k.f.n_lat > 0);
 }
 
+// issue_tile's copies (stored weights, strip layout) spread over the first
+// lanes of warps 0, 1 and 2 (tid 0, 32, 64), so that no single warp carries
+// the whole issue into the tile's first sub-step: tid 0 announces the
+// stage's bytes (the barrier's one arrival) and copies the weights, tid 32
+// the potential and the state, tid 64 the flags and the centre weights.
+// Copies may complete before the announcement: the phase cannot end before
+// the arrival, which carries the full byte count.
+template <int KMAX, int LH, int NS, int NWO>
+__device__ __forceinline__ void issue_tile_split(const TmaK &k,
+                                                 TmaStage<LH, NS, NWO> &G,
+                                                 uint64_t *bar, int bi, int bj,
+                                                 int tid)
+{
+    constexpr int TI = LH - 2 * KMAX, TJ = kTW - 2 * KMAX;
+    if (tid != 0 && tid != 32 && tid != 64) return;
+    fence_proxy_async();
+    const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
+    const int x4 = floor_to(oj - 1, 4), x16 = floor_to(oj, 16);
+    const bool lat = k.f.n_lat > 0;
+    if (tid == 0) {
+        const unsigned bytes = (unsigned)(sizeof(G.wa) * (NWO == 8 ? 2 : 1) +
+                                          sizeof(G.u) + NS * sizeof(G.s[0]) +
+                                          sizeof(G.myo) + sizeof(G.wc)) +
+                               (lat ? (unsigned)sizeof(G.act) : 0u);
+        mbar_expect_tx(bar, bytes);
+        tma_3d(&G.wa[0][0], &k.maps.w, 0, oj, oi, bar);
+        if constexpr (NWO == 8) tma_3d(&G.wb[0][0], &k.maps.w, 4, oj, oi, bar);
+    } else if (tid == 32) {
+        tma_2d(&G.u[0][0], &k.maps.u[k.in_buf], x4, oi - 1, bar);
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+            tma_2d(&G.s[q][0][0], &k.maps.s[k.in_buf][q], x4, oi, bar);
+    } else {
+        tma_2d(&G.myo[0][0], &k.maps.myo, x16, oi, bar);
+        tma_2d(&G.wc[0][0], &k.maps.wc, x4, oi, bar);
+        if (lat) tma_2d(&G.act[0][0], &k.maps.act, x16, oi, bar);
+    }
+}
+
 // minor_component (asymmetric_stencil_2d.py:204-259) in float32.
 __device__ __forceinline__ void minor_f32(float d, int m0, int m1, int m2, int m3,
                                           int m4, int m5, float r[6])
@@ -671,10 +710,17 @@ __global__ void __launch_bounds__(kTW *(LH / R), 1)
         // at the barrier that closed the previous iteration); issued after
         // the wait, so the other warps start this tile meanwhile
         const int next = tile + gridDim.x;
-        if (tid == 0 && next < k.tiles) {
-            fence_proxy_async();
-            issue_tile<KMAX, LH, NS, NWO, false, FLY>(k, S.stage[sg ^ 1],
-                                                      &S.bar[sg ^ 1], ni_, nj_);
+        if (next < k.tiles) {
+            if constexpr (FLY) {
+                if (tid == 0) {
+                    fence_proxy_async();
+                    issue_tile<KMAX, LH, NS, NWO, false, FLY>(k, S.stage[sg ^ 1],
+                                                              &S.bar[sg ^ 1], ni_, nj_);
+                }
+            } else {
+                issue_tile_split<KMAX, LH, NS, NWO>(k, S.stage[sg ^ 1], &S.bar[sg ^ 1],
+                                                    ni_, nj_, tid);
+            }
         }
         const int oi = bi * TI - KMAX, oj = bj * TJ - KMAX;
         bi = ni_;
