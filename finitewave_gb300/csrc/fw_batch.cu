@@ -532,6 +532,8 @@ struct BTileT {
 // staged with the region
 constexpr int32_t kTileLat = 1 << 8;
 
+constexpr int kAcq = 64;   // entries of the table of acquired tissues
+
 template <int NS, int NWO>
 struct BatchTmaSmem {
     fused::TmaSmem<LH, NS, NWO> t;
@@ -543,9 +545,8 @@ struct BatchTmaSmem {
     // tissues whose tensor maps thread 0 has acquired in this launch: a
     // direct-mapped table (tissue % kAcq -> tissue, -1: none); the maps do
     // not change during a launch, so one acquire per tissue and CTA suffices
-    int acq[64];
+    int acq[kAcq];
 };
-constexpr int kAcq = 64;
 
 // The batch's (model, stencil) groups, in the order the plan sorts tiles;
 // each group is advanced by its own instantiation of k_batch_tma.
@@ -696,7 +697,7 @@ __global__ void __launch_bounds__(kTmaNT, 1)
                                             (tid / fused::kTW) * kTmaR, own_c, ring_c);
     const BTileT none{-1, -1, 0, 0};
     // thread 0's tiles: runs of kRun consecutive list entries (mostly of
-    // one tissue, whose tensor maps are then acquired once per run), each
+    // one tissue), each
     // run's start taken from counters[0] one run ahead; the list entry of
     // tile i + 1 is read while tile i is computed
     int run_cur = t_end, run_end = t_end, run_next = t_end;
