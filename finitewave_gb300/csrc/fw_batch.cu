@@ -546,6 +546,12 @@ struct BatchTmaSmem {
     // direct-mapped table (tissue % kAcq -> tissue, -1: none); the maps do
     // not change during a launch, so one acquire per tissue and CTA suffices
     int acq[kAcq];
+    // the split issue of the loop (batch_issue_split): the next tile and its
+    // list entry, published by thread 0 before the stage wait, and the
+    // tables of tissues acquired by each of the three issuing lanes
+    int nt;
+    BTileT nbt;
+    int acq3[3][kAcq];
 };
 
 // The batch's (model, stencil) groups, in the order the plan sorts tiles;
@@ -668,6 +674,91 @@ __device__ __noinline__ void batch_issue(const BTissueT *__restrict__ tissues,
     }
 }
 
+// The loop's per-tile issue of the strip kernel, spread over one lane of
+// each of warps 0, 1 and 2 (tid 0, 32, 64) so that no warp carries all of
+// it into the tile's first sub-step: the next tile (S.nt) and its list
+// entry (S.nbt) were published by thread 0 before the stage wait; tid 0
+// records the tile, announces the stage's bytes (the barrier's one
+// arrival) and copies the weights and, when the stage's last tile was of
+// another tissue, the launch description; tid 32 copies the potential and
+// the state, tid 64 the myocyte flags, the centre weights and the local
+// activation flags.  Each lane acquires the tensor maps it uses, once per
+// tissue and launch (its own table).  Copies may complete before the
+// announcement: the phase cannot end before the arrival.
+template <class M, int ST, class Sm>
+__device__ __noinline__ void batch_issue_split(const BTissueT *__restrict__ tissues,
+                                               int32_t t_end, int32_t n_tissues,
+                                               int32_t in_buf, Sm &S, int sg, int tid)
+{
+    constexpr int NWO = fused::Stencil2D<ST>::NWO;
+    constexpr int NS = M::NS;
+    const int part = tid >> 5;
+    const int t = S.nt;
+    const BTileT bt = S.nbt;
+    if (part == 0) S.tile[sg] = t;
+    if (t >= t_end) return;
+    uint64_t *bar = &S.t.bar[sg];
+    fused::fence_proxy_async();
+    if (bt.tissue < 0 || bt.tissue >= n_tissues) {
+        // a corrupted plan: flag it and complete the stage's phase without
+        // data, so that the tile is skipped
+        if (part == 0) {
+            S.ok[sg] = 0;
+            if (tissues[0].f.status) atomicOr(tissues[0].f.status, FW_DEV_BATCH_FAULT);
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(
+                             fused::smem_u32(bar))
+                         : "memory");
+        }
+        return;
+    }
+    const BTissueT &T = tissues[bt.tissue];
+    const fused::TmaMaps &Mp = T.maps;
+    const bool lat = (bt.key & kTileLat) != 0;
+    int &acquired = S.acq3[part][bt.tissue & (kAcq - 1)];
+    const bool acq = bt.tissue != acquired;
+    if (acq) acquired = bt.tissue;
+    auto &G = S.t.stage[sg];
+    const int x4 = fused::floor_to(bt.oj - 1, 4), x16 = fused::floor_to(bt.oj, 16);
+    if (part == 0) {
+        S.ok[sg] = 1;
+        S.oi[sg] = bt.oi;
+        S.oj[sg] = bt.oj;
+        if (acq) tensormap_acquire(&Mp.w);
+        constexpr unsigned kF = (unsigned)sizeof(fused::FusedK);
+        const bool fresh = S.ftissue[sg] != bt.tissue;
+        const unsigned bytes =
+            (unsigned)(sizeof(G.wa) * (NWO == 8 ? 2 : 1) + sizeof(G.u) +
+                       NS * sizeof(G.s[0]) + sizeof(G.myo) + sizeof(G.wc)) +
+            (lat ? (unsigned)sizeof(G.act) : 0u) + (fresh ? kF : 0u);
+        fused::mbar_expect_tx(bar, bytes);
+        fused::tma_3d(&G.wa[0][0], &Mp.w, 0, bt.oj, bt.oi, bar);
+        if constexpr (NWO == 8) fused::tma_3d(&G.wb[0][0], &Mp.w, 4, bt.oj, bt.oi, bar);
+        if (fresh) {
+            bulk_copy(&S.f[sg], &T.f, kF, bar);
+            S.ftissue[sg] = bt.tissue;
+        }
+    } else if (part == 1) {
+        if (acq) {
+            tensormap_acquire(&Mp.u[in_buf]);
+#pragma unroll
+            for (int q = 0; q < NS; ++q) tensormap_acquire(&Mp.s[in_buf][q]);
+        }
+        fused::tma_2d(&G.u[0][0], &Mp.u[in_buf], x4, bt.oi - 1, bar);
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+            fused::tma_2d(&G.s[q][0][0], &Mp.s[in_buf][q], x4, bt.oi, bar);
+    } else {
+        if (acq) {
+            tensormap_acquire(&Mp.myo);
+            tensormap_acquire(&Mp.wc);
+            if (lat) tensormap_acquire(&Mp.act);
+        }
+        fused::tma_2d(&G.myo[0][0], &Mp.myo, x16, bt.oi, bar);
+        fused::tma_2d(&G.wc[0][0], &Mp.wc, x4, bt.oi, bar);
+        if (lat) fused::tma_2d(&G.act[0][0], &Mp.act, x16, bt.oi, bar);
+    }
+}
+
 // One (model, stencil) group of the batch: tiles [t_begin, t_end) of the
 // list, claimed kRun at a time from counters[0] (counters[1] counts the
 // CTAs that are done; the last one zeroes both).  PAIR (kernel 3): the tile
@@ -723,6 +814,7 @@ __global__ void __launch_bounds__(kTmaNT, 1)
         fused::mbar_fence_init();
         S.ftissue[0] = S.ftissue[1] = -1;
         for (int i = 0; i < kAcq; ++i) S.acq[i] = -1;
+        for (int i = 0; i < 3 * kAcq; ++i) S.acq3[i / kAcq][i % kAcq] = -1;
         run_next = take_run();
         const int t0 = next_tile();
         t_next = next_tile();
@@ -735,6 +827,11 @@ __global__ void __launch_bounds__(kTmaNT, 1)
     for (int it = 0;; ++it) {
         const int sg = it & 1;
         if (S.tile[sg] >= t_end) break;
+        if (!PAIR && tid == 0) {
+            // the next tile, for the three issuing lanes after the wait
+            S.nt = t_next;
+            S.nbt = b_next;
+        }
         const unsigned ph = (parity >> sg) & 1u;
         const bool arrived = fused::mbar_wait(&S.t.bar[sg], ph);
         parity ^= 1u << sg;
@@ -747,13 +844,19 @@ __global__ void __launch_bounds__(kTmaNT, 1)
             }
             break;
         }
+        // the next tile into the other stage, whose readers finished before
+        // the wait above ended; issued here, after the wait, so that the
+        // other warps start this tile meanwhile
+        if constexpr (PAIR) {
+            if (tid == 0)
+                batch_issue<M, ST, PAIR>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1,
+                                         t_next, b_next);
+        } else {
+            if (tid == 0 || tid == 32 || tid == 64)
+                batch_issue_split<M, ST>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1,
+                                         tid);
+        }
         if (tid == 0) {
-            // the next tile into the other stage, whose readers finished at
-            // the barrier that closed the previous iteration; issued here,
-            // after the wait, so that the other warps start this tile while
-            // thread 0 claims, acquires and issues
-            batch_issue<M, ST, PAIR>(tissues, t_end, n_tissues, in_buf, S, sg ^ 1,
-                                     t_next, b_next);
             t_next = next_tile();
             b_next = t_next < t_end ? tiles[t_next] : none;
         }
