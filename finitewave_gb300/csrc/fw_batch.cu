@@ -496,16 +496,18 @@ int64_t tissue_tiles(const fw_step_args *a)
 // list: one persistent 512-thread CTA per SM, two shared-memory stages, the
 // tile computed by the fused kernels' tile code (tma_tile), so a tissue
 // advanced here is bitwise the same as when run alone by k_fused_tma.
-// Everything a tile needs arrives asynchronously: thread 0 issues, for the
-// tile after the current one, one bulk copy of its tissue's launch
-// description (a FusedK kept in the plan, whose per-launch fields
-// k_batch_events fills before each launch) and the TMA copies of its region
-// through the tissue's own tensor maps (also in the plan), all completing
-// on the stage's mbarrier.  Thread 0 claims runs of consecutive tiles from
-// the counter one run ahead and reads each list entry one tile ahead, so
-// none of its loads is waited for on the way.  Tissues need rows of a multiple of 16
-// nodes, which the caller provides as a row pitch (fw_step_args.pitch) on
-// copies of the TMA-read arrays.
+// Everything a tile needs arrives asynchronously: for the tile after the
+// current one, one bulk copy of its tissue's launch description (a FusedK
+// kept in the plan, whose per-launch fields k_batch_events fills before
+// each launch) and the TMA copies of its region through the tissue's own
+// tensor maps (also in the plan), all completing on the stage's mbarrier,
+// issued right after the wait for the current tile's stage (by one lane
+// each of warps 0, 1 and 2 in the strip kernel, batch_issue_split).
+// Thread 0 claims runs of consecutive tiles from the counter one run ahead
+// and reads each list entry one tile ahead, so none of its loads is waited
+// for on the way.  Tissues need rows of a multiple of 16 nodes, which the
+// caller provides as a row pitch (fw_step_args.pitch) on copies of the
+// TMA-read arrays.
 
 constexpr int kTmaR = 4;                           // rows per thread
 constexpr int kRun = 4;                            // tiles per counter claim

@@ -3,11 +3,14 @@
 // Same per-tile algorithm as fw_fused_kernel.cuh (temporal blocking of up to
 // KMAX steps on a 64 x LH region, halo recomputed), organised for Blackwell:
 //   * one persistent CTA per SM walks the tiles (tile, tile + gridDim.x, ...);
-//   * its region is staged by the Tensor Memory Accelerator: thread 0 issues
+//   * its region is staged by the Tensor Memory Accelerator:
 //     cp.async.bulk.tensor copies (packed weights, potential, state,
 //     myocyte flags) that complete on an mbarrier;
 //   * two stages: while the CTA computes tile i from one stage, the TMA
-//     fills the other with tile i + 1, so HBM traffic overlaps compute.
+//     fills the other with tile i + 1, so HBM traffic overlaps compute; the
+//     copies of tile i + 1 are issued right after the wait for tile i's,
+//     by one lane each of warps 0, 1 and 2 (k_fused_tma), so that the other
+//     warps start on tile i meanwhile.
 // Every wait on an mbarrier is bounded; a timeout sets FW_DEV_TIMEOUT in the
 // status word and the CTA returns once its copies in flight have landed
 // (again a bounded wait).  The sub-steps form the diffusion sum as
