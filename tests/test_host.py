@@ -618,3 +618,25 @@ def test_batched_restitution_ranges_match_measurement():
     for s in specs:
         lo, hi = bench.RESTITUTION[s["model"]]
         assert lo <= s["ci"] <= hi
+
+
+def test_restitution_protocol_reproduces_recorded_travel_time():
+    """The float64 pacing protocol of tests/golden/make_restitution.py
+    (oracle kernels, one thread) reproduces the recorded arrival of the
+    first Aliev-Panfilov S1 wave at the probe node, and an S2 one BCL after
+    the last S1 is a ninth crossing (a propagated response)."""
+    import importlib.util
+    import json
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location(
+        "make_restitution", os.path.join(root, "tests", "golden",
+                                         "make_restitution.py"))
+    mr = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mr)
+    with open(os.path.join(root, "tests", "golden", "restitution.json")) as f:
+        rec = json.load(f)["models"]["ap"]
+    first = mr._pace("ap", None, stop_after=mr.BCL["ap"])
+    assert first and abs(first[0] - rec["travel_to_probe"]) < 1e-6
+    bcl = mr.BCL["ap"]
+    late = mr._pace("ap", bcl, stop_after=8 * bcl + 3 * first[0])
+    assert len(late) >= 9
